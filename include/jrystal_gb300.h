@@ -1,0 +1,138 @@
+/*
+ * jrystal_gb300 — C ABI of the GB300 (sm_103a) direct-minimisation
+ * energy-and-gradient library.
+ *
+ * Every entry point takes caller-owned device pointers, plain sizes and a
+ * cudaStream_t; none allocates device memory.  Scratch memory is a caller
+ * workspace of jrg_workspace_size() bytes (256-byte aligned).  Functions
+ * return a jrg_status; on failure jrg_last_error() gives a thread-local
+ * message.  Numerical faults (Cholesky breakdown, non-finite values) are
+ * reported through the status word of the call, never by trapping.
+ *
+ * The entry points replace the device work of these jrystal functions
+ * (paths relative to the jrystal project):
+ *   jrg_coeff          pw.coeff / unitary_module.unitary_matrix
+ *                      jrystal/_src/pw.py:94-137, unitary_module.py:30-80
+ *   jrg_density        pw.density_grid with occupation
+ *                      jrystal/_src/pw.py:214-284 (+ utils.py:257-281 scatter)
+ *   jrg_energy_grad    value_and_grad of total_energy in the ground-state
+ *                      driver, calc/calc_ground_state_energy_all_electrons.py:119-181
+ *                      (energy.kinetic/hartree/external/xc_energy,
+ *                      jrystal/_src/energy.py:29-211)
+ *   jrg_potential      potential.effective (non-Kohn-Sham and Kohn-Sham)
+ *                      jrystal/_src/potential.py:203-279
+ *   jrg_fft3d          spmd.fft.fftn3d / ifftn3d and jnp.fft.fftn over the
+ *                      last three axes, jrystal/_src/spmd/fft.py:37-75
+ *   jrg_adam_update    optax.adam update + apply_updates,
+ *                      calc/opt_utils.py:153-168, calc driver :179-180
+ *   jrg_ewald          ewald.ewald_coulomb_repulsion, jrystal/_src/ewald.py:21-86
+ *   jrg_precond_*      learned diagonal preconditioner (no jrystal counterpart)
+ */
+#ifndef JRYSTAL_GB300_H_
+#define JRYSTAL_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  JRG_OK = 0,
+  JRG_ERR_INVALID = 1,      /* bad argument, shape or pointer */
+  JRG_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  JRG_ERR_NUMERIC = 3,      /* Cholesky breakdown or non-finite result */
+  JRG_ERR_UNSUPPORTED = 4   /* size/precision the kernels do not cover */
+} jrg_status;
+
+/* exchange-correlation terms, OR-ed: "lda_x" and "lda_c_vwn" */
+#define JRG_XC_LDA_X 1
+#define JRG_XC_LDA_C_VWN 2
+
+typedef struct jrg_plan jrg_plan;
+
+typedef struct {
+  int precision;            /* 32: complex64/float32 arrays, 64: complex128/float64 */
+  int grid[3];              /* FFT grid (x, y, z), each 7-smooth */
+  double cell[9];           /* lattice vectors as rows, bohr */
+  int num_atom;
+  const double* positions;  /* host [num_atom][3], bohr */
+  const double* charges;    /* host [num_atom] */
+  int num_spin;             /* 1 (spin restricted) or 2 */
+  int num_kpt;
+  int num_band;
+  const double* kpts;       /* host [num_kpt][3], cartesian */
+  int num_g;                /* plane-wave sphere size */
+  const int32_t* sphere_index; /* host [num_g]: (x*ny + y)*nz + z of each
+                                  True entry of the frequency mask, strictly
+                                  increasing (row-major mask order) */
+  int xc;                   /* JRG_XC_* flags */
+} jrg_plan_desc;
+
+/* Library version and the last error message of the calling thread. */
+int jrg_version(void);
+const char* jrg_last_error(void);
+
+/* Plans: geometry tables (sphere maps, twiddles, kinetic and external
+ * potential tables) on the current device.  Creating a plan allocates its
+ * tables and synchronises the device; all other calls only enqueue work. */
+int jrg_plan_create(const jrg_plan_desc* desc, jrg_plan** out);
+int jrg_plan_destroy(jrg_plan* plan);
+/* Caller workspace needed by the entry points below (bytes). */
+int jrg_workspace_size(const jrg_plan* plan, size_t* bytes);
+
+/* Orthonormal coefficients from raw parameters.
+ * w_re, w_im: [S][K][G][B] real; coeff: [S][K][G][B] interleaved complex.
+ * Columns equal jnp.linalg.qr's Q up to a unit phase per band. */
+int jrg_coeff(const jrg_plan* plan, const void* w_re, const void* w_im, void* coeff,
+              void* workspace, cudaStream_t stream);
+
+/* Occupation-weighted density on the grid from sphere coefficients.
+ * coeff: [S][K][G][B] complex; occupation: device double [S][K][B];
+ * density: [S][nx][ny][nz] real. */
+int jrg_density(const jrg_plan* plan, const void* coeff, const double* occupation,
+                void* density, void* workspace, cudaStream_t stream);
+
+/* Loss and gradient of the direct-minimisation path.
+ * energies (device double[8]): kinetic, external, hartree, xc, total,
+ *   then max |C^H C - I| over k, and two reserved slots.
+ * grad_re/grad_im: [S][K][G][B] d total / d w_re, d w_im (may be NULL for
+ * energy only). */
+int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
+                    const double* occupation, double* energies, void* grad_re,
+                    void* grad_im, void* workspace, cudaStream_t stream);
+
+/* Effective potential from a density [S][nx][ny][nz] (S must be 1):
+ * out [3][nx][ny][nz] real = Hartree, external, xc parts (split form) with
+ * jrystal's conventions: kohn_sham=0 halves Hartree and gives the xc energy
+ * density, kohn_sham=1 gives the full Hartree and v_xc. */
+int jrg_potential(const jrg_plan* plan, const void* density, int kohn_sham, void* out,
+                  void* workspace, cudaStream_t stream);
+
+/* Batched complex 3-D FFT over the last three axes of [batch][nx][ny][nz].
+ * direction -1: forward (unnormalised, jnp.fft.fftn); +1: inverse with the
+ * 1/(nx ny nz) factor (jnp.fft.ifftn).  in and out may alias.  workspace
+ * needs jrg_fft3d_workspace_size bytes. */
+int jrg_fft3d_workspace_size(int precision, const int grid[3], int batch, size_t* bytes);
+int jrg_fft3d(int precision, const int grid[3], int batch, int direction, const void* in,
+              void* out, void* workspace, cudaStream_t stream);
+
+/* One Adam step over n elements (optax.adam: eps outside the sqrt after bias
+ * correction).  step is the 1-based count after this update.  scale, when not
+ * NULL, multiplies each update element (learned preconditioner). */
+int jrg_adam_update(int precision, int64_t n, void* param, const void* grad, void* m, void* v,
+                    const float* scale, int step, double lr, double b1, double b2, double eps,
+                    cudaStream_t stream);
+
+/* Ewald nuclear repulsion (FP64), the jrystal formula with the translation
+ * grid of grid.translation_vectors(cell, cutoff) and the reciprocal sum over
+ * the plan's FFT G grid.  result: device double[1]. */
+int jrg_ewald(const jrg_plan* plan, double eta, double cutoff, double* result,
+              void* workspace, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JRYSTAL_GB300_H_ */

@@ -1,0 +1,8 @@
+"""GB300-native direct-minimisation energy-and-gradient path of jrystal.
+
+The modules keep jrystal's public names and signatures (``pw``, ``energy``,
+``potential``, ``kinetic``, ``occupation``, ``hamiltonian``, ``grid``,
+``crystal``, ``ewald``, ``entropy``, ``braket``) over a C-ABI CUDA library of
+hand-written sm_103a kernels (``libjrystal_gb300.so``).
+"""
+__version__ = "0.1.0"

@@ -1,0 +1,99 @@
+"""ctypes binding of the C ABI in ``include/jrystal_gb300.h``.
+
+The library is the in-tree ``libjrystal_gb300.so``; loading fails loudly when
+it is missing -- there is no CPU or PyTorch fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import threading
+
+from . import build as _build
+
+_LOCK = threading.Lock()
+_LIB = None
+
+JRG_OK = 0
+JRG_ERR_INVALID = 1
+JRG_ERR_CUDA = 2
+JRG_ERR_NUMERIC = 3
+JRG_ERR_UNSUPPORTED = 4
+XC_FLAGS = {"lda_x": 1, "lda_c_vwn": 2}
+
+# exported entry points and their argument types
+_vp = ct.c_void_p
+_SIGS = {
+  "jrg_version": ([], ct.c_int),
+  "jrg_last_error": ([], ct.c_char_p),
+  "jrg_plan_create": ([_vp, ct.POINTER(_vp)], ct.c_int),
+  "jrg_plan_destroy": ([_vp], ct.c_int),
+  "jrg_workspace_size": ([_vp, ct.POINTER(ct.c_size_t)], ct.c_int),
+  "jrg_coeff": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
+  "jrg_density": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
+  "jrg_energy_grad": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
+  "jrg_potential": ([_vp, _vp, ct.c_int, _vp, _vp, _vp], ct.c_int),
+  "jrg_fft3d_workspace_size": ([ct.c_int, ct.POINTER(ct.c_int), ct.c_int,
+                                ct.POINTER(ct.c_size_t)], ct.c_int),
+  "jrg_fft3d": ([ct.c_int, ct.POINTER(ct.c_int), ct.c_int, ct.c_int, _vp, _vp, _vp,
+                 _vp], ct.c_int),
+  "jrg_adam_update": ([ct.c_int, ct.c_int64, _vp, _vp, _vp, _vp, _vp, ct.c_int,
+                       ct.c_double, ct.c_double, ct.c_double, ct.c_double, _vp], ct.c_int),
+  "jrg_ewald": ([_vp, ct.c_double, ct.c_double, _vp, _vp, _vp], ct.c_int),
+}
+
+
+class PlanDesc(ct.Structure):
+  _fields_ = [
+    ("precision", ct.c_int),
+    ("grid", ct.c_int * 3),
+    ("cell", ct.c_double * 9),
+    ("num_atom", ct.c_int),
+    ("positions", ct.POINTER(ct.c_double)),
+    ("charges", ct.POINTER(ct.c_double)),
+    ("num_spin", ct.c_int),
+    ("num_kpt", ct.c_int),
+    ("num_band", ct.c_int),
+    ("kpts", ct.POINTER(ct.c_double)),
+    ("num_g", ct.c_int),
+    ("sphere_index", ct.POINTER(ct.c_int32)),
+    ("xc", ct.c_int),
+  ]
+
+
+def library_path() -> str:
+  return _build.LIB
+
+
+def exported_symbols():
+  return list(_SIGS)
+
+
+def load(build_if_missing: bool = True):
+  """Load (building first if allowed and needed) the CUDA library."""
+  global _LIB
+  with _LOCK:
+    if _LIB is not None:
+      return _LIB
+    path = _build.LIB
+    if build_if_missing and _build.needs_build():
+      _build.build()
+    if not os.path.exists(path):
+      raise RuntimeError(
+        f"jrystal_gb300 CUDA library not found at {path}; run "
+        "jrystal_gb300.build.build() (nvcc required). There is no CPU fallback.")
+    lib = ct.CDLL(path)
+    for name, (args, res) in _SIGS.items():
+      fn = getattr(lib, name)
+      fn.argtypes = args
+      fn.restype = res
+    _LIB = lib
+    return lib
+
+
+def check(status: int, what: str = ""):
+  if status != JRG_OK:
+    msg = load().jrg_last_error().decode(errors="replace")
+    kind = {JRG_ERR_INVALID: ValueError, JRG_ERR_UNSUPPORTED: NotImplementedError}.get(
+      status, RuntimeError)
+    raise kind(f"{what} failed (status {status}): {msg}")

@@ -1,0 +1,556 @@
+// C ABI of the library: plan construction, workspace layout and the entry
+// points declared in include/jrystal_gb300.h.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "plan.h"
+
+namespace jrg {
+
+// ---- launchers implemented in the kernel files ----
+template <typename R> int launch_plane_inv_sphere(const jrg_plan*, const void*, void*, int, cudaStream_t);
+template <typename R> int launch_line_density(const jrg_plan*, const void*, void*, const double*, double, int, int, int, cudaStream_t);
+template <typename R> int launch_line_apply_v(const jrg_plan*, const void*, void*, const void*, int, int, cudaStream_t);
+template <typename R> int launch_plane_fwd_sphere(const jrg_plan*, const void*, const void*, void*, const double*, int, int, double, cudaStream_t);
+template <typename R> int launch_fft3d_dense(const FftAxis*, const C_t<R>*, int, int, bool, const void*, C_t<R>*, C_t<R>*, double, cudaStream_t);
+template <typename R> int launch_pack_params(const void*, const void*, void*, int, int, int, bool, cudaStream_t);
+template <typename R> int launch_unpack(const void*, void*, void*, void*, int, int, int, double, cudaStream_t);
+template <typename R> int launch_gram(const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t);
+int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, cudaStream_t);
+int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t);
+template <typename R> int launch_rotate(int, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, cudaStream_t);
+template <typename R> int launch_reduce_density(const void*, void*, int, int, long long, cudaStream_t);
+template <typename R> int launch_recip_terms(const void*, const double*, const void*, void*, double*, double*, int, long long, double, cudaStream_t);
+template <typename R> int launch_potential(const void*, const void*, double, void*, double*, int, long long, int, double, cudaStream_t);
+template <typename R> int launch_xc_field(const void*, void*, long long, int, int, cudaStream_t);
+template <typename R> int launch_real_part(const void*, void*, long long, double, cudaStream_t);
+template <typename R> int launch_hartree_g(const void*, const double*, void*, long long, double, cudaStream_t);
+template <typename R> int launch_kinetic(const void*, const double*, const double*, double*, int, int, int, int, cudaStream_t);
+int launch_sum_slots(const double*, const int*, double*, int, const int*, cudaStream_t);
+template <typename R> int launch_geometry_tables(double*, double*, void*, const double*, const double*, const double*, int, int, int, int, double, cudaStream_t);
+int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
+template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t);
+int launch_twiddles(int n, int prec, void* out, cudaStream_t st);
+
+static thread_local std::string g_err;
+void set_error(const std::string& m) { g_err = m; }
+int fail(int code, const std::string& m) { g_err = m; return code; }
+int cuda_fail(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return JRG_ERR_CUDA;
+}
+
+bool factor_axis(int n, FftAxis* ax) {
+  ax->n = n;
+  ax->nrad = 0;
+  int m = n;
+  const int rads[5] = {4, 2, 3, 5, 7};
+  for (int r : rads) {
+    while (m % r == 0) {
+      if (ax->nrad >= kMaxRadices) return false;
+      ax->rad[ax->nrad++] = r;
+      m /= r;
+    }
+  }
+  return m == 1 && n >= 1;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// energy slot layout
+constexpr int kRecipBlocks = 256;
+constexpr int kXcBlocks = 256;
+constexpr int kEwaldBlocks = 512;
+
+static int csize(int prec) { return prec == 64 ? 16 : 8; }
+static int rsize(int prec) { return prec == 64 ? 8 : 4; }
+
+static void layout_workspace(jrg_plan* P) {
+  Workspace& w = P->ws;
+  const size_t C = csize(P->prec), Rz = rsize(P->prec);
+  const size_t nsk = (size_t)P->ns * P->nk, nbt = nsk * P->nb;
+  const size_t b2 = (size_t)P->nb * P->nb * sizeof(double2);
+  w.gram_splits = std::max(1, std::min(64, (int)((P->ng + 1023) / 1024)));
+  w.ngroups = (int)nsk;
+  w.nepart = (int)nbt + 2 * kRecipBlocks + kXcBlocks;
+  if (w.nepart < 2 * kEwaldBlocks) w.nepart = 2 * kEwaldBlocks;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t r = o; o += align256(bytes); return r; };
+  w.wc = take(nbt * P->ng * C);
+  w.c = take(nbt * P->ng * C);
+  w.gram_part = take(nsk * w.gram_splits * b2);
+  w.gram = take(nsk * b2);
+  w.rmat = take(nsk * b2);
+  w.rinv = take(nsk * b2);
+  w.adj = take(nsk * b2);
+  w.kmat = take(2 * nsk * b2);          // R^{-H} and -K R^{-H}
+  w.t = take(nbt * P->nact * (size_t)P->ny * P->nz * C);
+  w.u = w.t;                            // adjoint line pass works in place
+  w.rho_part = take((size_t)w.ngroups * P->ngrid * Rz);
+  w.rho = take((size_t)P->ns * P->ngrid * Rz);
+  w.rhog = take((size_t)P->ngrid * C);
+  w.fft_scratch = take((size_t)P->ngrid * C);
+  w.vr = take((size_t)P->ngrid * Rz);
+  w.gc = take(nbt * P->ng * C);
+  w.adj_part = w.gram_part;
+  w.epart = take((size_t)w.nepart * sizeof(double));
+  w.flags = take(64);
+  w.total = o;
+}
+
+}  // namespace jrg
+
+using namespace jrg;
+
+extern "C" {
+
+int jrg_version(void) { return 1; }
+const char* jrg_last_error(void) { return g_err.c_str(); }
+
+int jrg_plan_destroy(jrg_plan* P) {
+  if (!P) return JRG_OK;
+  void* ptrs[] = {P->d.gidx, P->d.sph_yz, P->d.plane_x, P->d.plane_off, P->d.row_off, P->d.rows,
+                  P->d.xact, P->d.tk, P->d.tw, P->d.vext, P->d.ginv, P->d.gvec};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (P->slot_begin) cudaFree(P->slot_begin);
+  if (P->d_cell) cudaFree(P->d_cell);
+  if (P->d_atoms) cudaFree(P->d_atoms);
+  delete P;
+  return JRG_OK;
+}
+
+int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
+  if (!d || !out) return fail(JRG_ERR_INVALID, "jrg_plan_create: null argument");
+  *out = nullptr;
+  if (d->precision != 32 && d->precision != 64)
+    return fail(JRG_ERR_INVALID, "precision must be 32 or 64");
+  if (d->num_spin != 1 && d->num_spin != 2) return fail(JRG_ERR_INVALID, "num_spin must be 1 or 2");
+  if (d->num_kpt < 1 || d->num_band < 1 || d->num_g < 1 || d->num_atom < 0)
+    return fail(JRG_ERR_INVALID, "num_kpt, num_band, num_g must be positive");
+  if (d->num_band > d->num_g) return fail(JRG_ERR_INVALID, "num_band exceeds the sphere size");
+  if (!d->sphere_index || !d->kpts || (d->num_atom > 0 && (!d->positions || !d->charges)))
+    return fail(JRG_ERR_INVALID, "null table pointer");
+  jrg_plan* P = new jrg_plan();
+  P->prec = d->precision;
+  P->nx = d->grid[0]; P->ny = d->grid[1]; P->nz = d->grid[2];
+  for (int a = 0; a < 3; ++a) {
+    if (!factor_axis(d->grid[a], &P->ax[a])) {
+      delete P;
+      return fail(JRG_ERR_UNSUPPORTED, "grid size must be a product of 2, 3, 5, 7");
+    }
+  }
+  P->ngrid = (long long)P->nx * P->ny * P->nz;
+  P->ns = d->num_spin; P->nk = d->num_kpt; P->nb = d->num_band; P->ng = d->num_g;
+  P->xc = d->xc;
+  std::memcpy(P->cell, d->cell, sizeof(P->cell));
+  {
+    const double* a = d->cell;
+    const double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                       a[2] * (a[3] * a[7] - a[4] * a[6]);
+    if (!(std::fabs(det) > 0)) { delete P; return fail(JRG_ERR_INVALID, "singular cell"); }
+    P->vol = std::fabs(det);
+    // reciprocal vectors b = 2 pi inv(a)^T, rows b_i
+    double inv[9];
+    inv[0] = (a[4] * a[8] - a[5] * a[7]) / det; inv[1] = (a[2] * a[7] - a[1] * a[8]) / det;
+    inv[2] = (a[1] * a[5] - a[2] * a[4]) / det; inv[3] = (a[5] * a[6] - a[3] * a[8]) / det;
+    inv[4] = (a[0] * a[8] - a[2] * a[6]) / det; inv[5] = (a[2] * a[3] - a[0] * a[5]) / det;
+    inv[6] = (a[3] * a[7] - a[4] * a[6]) / det; inv[7] = (a[1] * a[6] - a[0] * a[7]) / det;
+    inv[8] = (a[0] * a[4] - a[1] * a[3]) / det;
+    const double tpi = 2.0 * 3.14159265358979323846;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) P->recip[3 * i + j] = tpi * inv[3 * j + i];
+  }
+  P->pos.assign(d->positions, d->positions + 3 * d->num_atom);
+  P->charge.assign(d->charges, d->charges + d->num_atom);
+  P->kpts.assign(d->kpts, d->kpts + 3 * d->num_kpt);
+  // sphere tables
+  const int ng = P->ng;
+  std::vector<int> gidx(d->sphere_index, d->sphere_index + ng), sph_yz(ng);
+  std::vector<int> plane_x, plane_off, row_off, rows, xact(P->nx, -1);
+  const long long nyz = (long long)P->ny * P->nz;
+  for (int e = 0; e < ng; ++e) {
+    if (gidx[e] < 0 || gidx[e] >= P->ngrid || (e > 0 && gidx[e] <= gidx[e - 1])) {
+      delete P;
+      return fail(JRG_ERR_INVALID, "sphere_index must be strictly increasing grid indices");
+    }
+    const int x = (int)(gidx[e] / nyz);
+    const int yz = (int)(gidx[e] % nyz);
+    const int y = yz / P->nz;
+    sph_yz[e] = yz;
+    if (plane_x.empty() || plane_x.back() != x) {
+      xact[x] = (int)plane_x.size();
+      plane_x.push_back(x);
+      plane_off.push_back(e);
+      row_off.push_back((int)rows.size());
+      rows.push_back(y);
+    } else if (rows.back() != y) {
+      rows.push_back(y);
+    }
+  }
+  plane_off.push_back(ng);
+  row_off.push_back((int)rows.size());
+  P->nact = (int)plane_x.size();
+  P->max_rows = 0;
+  for (int p = 0; p < P->nact; ++p) P->max_rows = std::max(P->max_rows, row_off[p + 1] - row_off[p]);
+  // kinetic table |G+k|^2/2
+  std::vector<double> tk((size_t)P->nk * ng);
+  auto ff = [](int i, int n) { return (i < (n + 1) / 2) ? i : i - n; };
+  for (int e = 0; e < ng; ++e) {
+    const int x = (int)(gidx[e] / nyz), y = (sph_yz[e]) / P->nz, z = sph_yz[e] % P->nz;
+    const double m0 = ff(x, P->nx), m1 = ff(y, P->ny), m2 = ff(z, P->nz);
+    double g[3];
+    for (int c = 0; c < 3; ++c) g[c] = m0 * P->recip[c] + m1 * P->recip[3 + c] + m2 * P->recip[6 + c];
+    for (int k = 0; k < P->nk; ++k) {
+      double s = 0.0;
+      for (int c = 0; c < 3; ++c) { const double v = g[c] + P->kpts[3 * k + c]; s += v * v; }
+      tk[(size_t)k * ng + e] = 0.5 * s;
+    }
+  }
+  // shared-memory limits of the slab kernels
+  {
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) { delete P; return cuda_fail(ce, "cudaGetDevice"); }
+    P->device = dev;
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t C = csize(P->prec), Rz = rsize(P->prec);
+    const size_t plane_b = C * (P->ny + P->nz + 2 * (size_t)P->ny * P->nz) + 4 * (P->max_rows + 1);
+    const size_t line_b = C * (P->nx + 2 * (size_t)P->nx * P->nz) + Rz * P->nx * P->nz +
+                          4 * (P->nx + P->nact);
+    if ((long long)plane_b > optin || (long long)line_b > optin || P->nx * P->nz > 256 * 48) {
+      delete P;
+      return fail(JRG_ERR_UNSUPPORTED, "grid too large for the shared-memory slab kernels at this precision");
+    }
+  }
+  // upload
+  auto up = [&](void** dst, const void* src, size_t bytes) -> int {
+    cudaError_t e = cudaMalloc(dst, bytes ? bytes : 4);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(plan table)");
+    if (bytes) {
+      e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(plan table)");
+    }
+    return JRG_OK;
+  };
+  int rc = JRG_OK;
+#define UP(field, vec) \
+  if (!rc) rc = up((void**)&P->d.field, vec.data(), vec.size() * sizeof(vec[0]));
+  UP(gidx, gidx) UP(sph_yz, sph_yz) UP(plane_x, plane_x) UP(plane_off, plane_off)
+  UP(row_off, row_off) UP(rows, rows) UP(xact, xact) UP(tk, tk)
+#undef UP
+  // twiddles (host, double precision): x, y, z tables
+  if (!rc) {
+    const int nt = P->nx + P->ny + P->nz;
+    std::vector<double> tw(2 * (size_t)nt);
+    int o = 0;
+    for (int a = 0; a < 3; ++a) {
+      const int n = P->ax[a].n;
+      for (int t = 0; t < n; ++t) {
+        const double ang = -2.0 * 3.14159265358979323846 * (double)t / (double)n;
+        tw[2 * (o + t)] = std::cos(ang);
+        tw[2 * (o + t) + 1] = std::sin(ang);
+      }
+      o += n;
+    }
+    if (P->prec == 64) {
+      rc = up(&P->d.tw, tw.data(), tw.size() * sizeof(double));
+    } else {
+      std::vector<float> twf(tw.begin(), tw.end());
+      rc = up(&P->d.tw, twf.data(), twf.size() * sizeof(float));
+    }
+  }
+  // geometry tables on the device (FP64)
+  double* d_recip = nullptr; double* d_pos = nullptr; double* d_chg = nullptr;
+  if (!rc) {
+    std::vector<double> cr(18);
+    std::memcpy(cr.data(), P->cell, 9 * sizeof(double));
+    std::memcpy(cr.data() + 9, P->recip, 9 * sizeof(double));
+    rc = up((void**)&P->d_cell, cr.data(), cr.size() * sizeof(double));
+    d_recip = P->d_cell + 9;
+  }
+  std::vector<double> atoms(4 * std::max(1, d->num_atom), 0.0);
+  for (int i = 0; i < d->num_atom; ++i) {
+    for (int c = 0; c < 3; ++c) atoms[3 * i + c] = P->pos[3 * i + c];
+    atoms[3 * d->num_atom + i] = P->charge[i];
+  }
+  if (!rc) rc = up((void**)&P->d_atoms, atoms.data(), atoms.size() * sizeof(double));
+  if (!rc) { d_pos = P->d_atoms; d_chg = P->d_atoms + 3 * d->num_atom; }
+  if (!rc) {
+    cudaError_t e = cudaMalloc((void**)&P->d.gvec, 3 * P->ngrid * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&P->d.ginv, P->ngrid * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&P->d.vext, P->ngrid * csize(P->prec));
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(geometry tables)");
+  }
+  if (!rc) {
+    if (P->prec == 64)
+      rc = launch_geometry_tables<double>(P->d.gvec, P->d.ginv, P->d.vext, d_recip, d_pos, d_chg,
+                                          d->num_atom, P->nx, P->ny, P->nz, P->vol, 0);
+    else
+      rc = launch_geometry_tables<float>(P->d.gvec, P->d.ginv, P->d.vext, d_recip, d_pos, d_chg,
+                                         d->num_atom, P->nx, P->ny, P->nz, P->vol, 0);
+  }
+  layout_workspace(P);
+  // energy slot boundaries: kinetic, external, hartree, xc
+  if (!rc) {
+    const int nbt = P->ns * P->nk * P->nb;
+    std::vector<int> sb = {0, nbt, nbt + kRecipBlocks, nbt + 2 * kRecipBlocks,
+                           nbt + 2 * kRecipBlocks + kXcBlocks};
+    rc = up((void**)&P->slot_begin, sb.data(), sb.size() * sizeof(int));
+  }
+  if (!rc) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) rc = cuda_fail(e, "plan setup");
+  }
+  if (rc) { jrg_plan_destroy(P); return rc; }
+  *out = P;
+  return JRG_OK;
+}
+
+int jrg_workspace_size(const jrg_plan* P, size_t* bytes) {
+  if (!P || !bytes) return fail(JRG_ERR_INVALID, "null argument");
+  *bytes = P->ws.total;
+  return JRG_OK;
+}
+
+}  // extern "C"
+
+namespace jrg {
+
+static inline char* wsp(void* ws, size_t off) { return reinterpret_cast<char*>(ws) + off; }
+
+template <typename R>
+static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im, void* ws,
+                          cudaStream_t st) {
+  const Workspace& w = P->ws;
+  const int nsk = P->ns * P->nk;
+  int rc;
+  if ((rc = launch_pack_params<R>(w_re, w_im, wsp(ws, w.wc), nsk, P->ng, P->nb, false, st))) return rc;
+  if ((rc = launch_gram<R>(wsp(ws, w.wc), wsp(ws, w.wc), (double2*)wsp(ws, w.gram_part),
+                           (double2*)wsp(ws, w.gram), nsk, P->ng, P->nb, w.gram_splits, st)))
+    return rc;
+  if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram), (double2*)wsp(ws, w.rmat),
+                                (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags), st)))
+    return rc;
+  return launch_rotate<R>(0, wsp(ws, w.wc), (double2*)wsp(ws, w.rinv), nullptr, nullptr,
+                          wsp(ws, w.c), nullptr, nsk, P->ng, P->nb, 1.0, st);
+}
+
+// density of the band-major coefficients held in workspace slot c
+template <typename R>
+static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* rho_out,
+                          cudaStream_t st) {
+  const Workspace& w = P->ws;
+  const int nbt = P->ns * P->nk * P->nb;
+  int rc;
+  if ((rc = launch_plane_inv_sphere<R>(P, wsp(ws, w.c), wsp(ws, w.t), nbt, st))) return rc;
+  if ((rc = launch_line_density<R>(P, wsp(ws, w.t), wsp(ws, w.rho_part), occ, 1.0 / P->vol, 0, nbt,
+                                   P->nb, st)))
+    return rc;
+  return launch_reduce_density<R>(wsp(ws, w.rho_part), rho_out, P->nk, P->ns, P->ngrid, st);
+}
+
+template <typename R>
+static int energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
+                       double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
+  using C = C_t<R>;
+  const Workspace& w = P->ws;
+  const int nsk = P->ns * P->nk;
+  const int nbt = nsk * P->nb;
+  const double N = (double)P->ngrid;
+  int rc;
+  JRG_CUDA(cudaMemsetAsync(wsp(ws, w.flags), 0, 64, st));
+  if ((rc = orthonormalise<R>(P, w_re, w_im, ws, st))) return rc;
+  double* slots = (double*)wsp(ws, w.epart);
+  if ((rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, occ, slots, nbt, P->ng, P->nb, P->nk, st))) return rc;
+  void* rho = wsp(ws, w.rho);
+  if ((rc = density_from_c<R>(P, occ, ws, rho, st))) return rc;
+  C* rhog = (C*)wsp(ws, w.rhog);
+  C* scratch = (C*)wsp(ws, w.fft_scratch);
+  const C* tw = (const C*)P->d.tw;
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+  // Hartree / external (slots after the kinetic ones) and dE/drho in G space (in place)
+  const double pref = P->vol / (N * N);
+  if ((rc = launch_recip_terms<R>(rhog, P->d.ginv, P->d.vext, rhog, slots + nbt + kRecipBlocks,
+                                  slots + nbt, kRecipBlocks, P->ngrid, pref, st)))
+    return rc;
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st))) return rc;
+  if ((rc = launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks,
+                                kXcBlocks, P->ngrid, P->xc, P->vol / N, st)))
+    return rc;
+  if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st))) return rc;
+  if (!g_re && !g_im) return JRG_OK;
+  if (!g_re || !g_im) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
+  // adjoint: planes -> x lines (x V) -> planes -> sphere gradient
+  if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), wsp(ws, w.vr), nbt, P->nb, st))) return rc;
+  if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), wsp(ws, w.c), wsp(ws, w.gc), occ, 0, nbt,
+                                       1.0 / N, st)))
+    return rc;
+  // orthonormalisation adjoint
+  if ((rc = launch_gram<R>(wsp(ws, w.c), wsp(ws, w.gc), (double2*)wsp(ws, w.adj_part),
+                           (double2*)wsp(ws, w.adj), nsk, P->ng, P->nb, w.gram_splits, st)))
+    return rc;
+  double2* rh = (double2*)wsp(ws, w.kmat);
+  double2* negm2 = rh + (size_t)nsk * P->nb * P->nb;
+  if ((rc = launch_adjoint_small((double2*)wsp(ws, w.adj), (double2*)wsp(ws, w.rinv), rh, negm2, nsk,
+                                 P->nb, st)))
+    return rc;
+  return launch_rotate<R>(2, wsp(ws, w.gc), rh, wsp(ws, w.c), negm2, g_re, g_im, nsk, P->ng, P->nb,
+                          2.0, st);
+}
+
+template <typename R>
+static int density_entry(const jrg_plan* P, const void* coeff, const double* occ, void* rho, void* ws,
+                         cudaStream_t st) {
+  const int nsk = P->ns * P->nk;
+  int rc = launch_pack_params<R>(coeff, nullptr, wsp(ws, P->ws.c), nsk, P->ng, P->nb, true, st);
+  if (rc) return rc;
+  return density_from_c<R>(P, occ, ws, rho, st);
+}
+
+template <typename R>
+static int coeff_entry(const jrg_plan* P, const void* w_re, const void* w_im, void* coeff, void* ws,
+                       cudaStream_t st) {
+  const Workspace& w = P->ws;
+  const int nsk = P->ns * P->nk;
+  JRG_CUDA(cudaMemsetAsync(wsp(ws, w.flags), 0, 64, st));
+  int rc;
+  if ((rc = launch_pack_params<R>(w_re, w_im, wsp(ws, w.wc), nsk, P->ng, P->nb, false, st))) return rc;
+  if ((rc = launch_gram<R>(wsp(ws, w.wc), wsp(ws, w.wc), (double2*)wsp(ws, w.gram_part),
+                           (double2*)wsp(ws, w.gram), nsk, P->ng, P->nb, w.gram_splits, st)))
+    return rc;
+  if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram), (double2*)wsp(ws, w.rmat),
+                                (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags), st)))
+    return rc;
+  return launch_rotate<R>(1, wsp(ws, w.wc), (double2*)wsp(ws, w.rinv), nullptr, nullptr, coeff,
+                          nullptr, nsk, P->ng, P->nb, 1.0, st);
+}
+
+template <typename R>
+static int potential_entry(const jrg_plan* P, const void* rho, int ks, void* out, void* ws,
+                           cudaStream_t st) {
+  using C = C_t<R>;
+  const Workspace& w = P->ws;
+  const double N = (double)P->ngrid;
+  C* rhog = (C*)wsp(ws, w.rhog);
+  C* scratch = (C*)wsp(ws, w.fft_scratch);
+  const C* tw = (const C*)P->d.tw;
+  R* o = (R*)out;
+  int rc;
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+  if ((rc = launch_hartree_g<R>(rhog, P->d.ginv, rhog, P->ngrid, ks ? 1.0 : 0.5, st))) return rc;
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st))) return rc;
+  if ((rc = launch_real_part<R>(rhog, o, P->ngrid, 1.0, st))) return rc;
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, P->d.vext, scratch, rhog, 1.0 / N, st))) return rc;
+  if ((rc = launch_real_part<R>(rhog, o + P->ngrid, P->ngrid, 1.0, st))) return rc;
+  return launch_xc_field<R>(rho, o + 2 * P->ngrid, P->ngrid, P->xc, ks, st);
+}
+
+}  // namespace jrg
+
+extern "C" {
+
+int jrg_coeff(const jrg_plan* P, const void* w_re, const void* w_im, void* coeff, void* ws,
+              cudaStream_t st) {
+  if (!P || !w_re || !w_im || !coeff || !ws) return fail(JRG_ERR_INVALID, "jrg_coeff: null argument");
+  return P->prec == 64 ? coeff_entry<double>(P, w_re, w_im, coeff, ws, st)
+                       : coeff_entry<float>(P, w_re, w_im, coeff, ws, st);
+}
+
+int jrg_density(const jrg_plan* P, const void* coeff, const double* occ, void* rho, void* ws,
+                cudaStream_t st) {
+  if (!P || !coeff || !occ || !rho || !ws) return fail(JRG_ERR_INVALID, "jrg_density: null argument");
+  return P->prec == 64 ? density_entry<double>(P, coeff, occ, rho, ws, st)
+                       : density_entry<float>(P, coeff, occ, rho, ws, st);
+}
+
+int jrg_energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
+                    double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
+  if (!P || !w_re || !w_im || !occ || !energies || !ws)
+    return fail(JRG_ERR_INVALID, "jrg_energy_grad: null argument");
+  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad: spin-polarised LDA is not implemented");
+  return P->prec == 64 ? energy_grad<double>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st)
+                       : energy_grad<float>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st);
+}
+
+int jrg_potential(const jrg_plan* P, const void* rho, int ks, void* out, void* ws, cudaStream_t st) {
+  if (!P || !rho || !out || !ws) return fail(JRG_ERR_INVALID, "jrg_potential: null argument");
+  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_potential: spin-polarised LDA is not implemented");
+  return P->prec == 64 ? potential_entry<double>(P, rho, ks, out, ws, st)
+                       : potential_entry<float>(P, rho, ks, out, ws, st);
+}
+
+int jrg_fft3d_workspace_size(int prec, const int grid[3], int batch, size_t* bytes) {
+  if (!grid || !bytes || batch < 1 || (prec != 32 && prec != 64))
+    return fail(JRG_ERR_INVALID, "jrg_fft3d_workspace_size: bad argument");
+  const size_t c = csize(prec);
+  *bytes = align256(c * (size_t)(grid[0] + grid[1] + grid[2])) +
+           align256(c * (size_t)batch * grid[0] * grid[1] * grid[2]);
+  return JRG_OK;
+}
+
+int jrg_fft3d(int prec, const int grid[3], int batch, int direction, const void* in, void* out,
+              void* ws, cudaStream_t st) {
+  if (!grid || !in || !out || !ws || batch < 1 || (direction != 1 && direction != -1) ||
+      (prec != 32 && prec != 64))
+    return fail(JRG_ERR_INVALID, "jrg_fft3d: bad argument");
+  FftAxis ax[3];
+  for (int a = 0; a < 3; ++a)
+    if (!factor_axis(grid[a], &ax[a])) return fail(JRG_ERR_UNSUPPORTED, "grid size must be 7-smooth");
+  {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t c = csize(prec);
+    const size_t pb = c * (grid[1] + grid[2] + 2 * (size_t)grid[1] * grid[2]) + 4;
+    const size_t lb = c * (grid[0] + 2 * (size_t)grid[0] * grid[2]);
+    if ((long long)pb > optin || (long long)lb > optin)
+      return fail(JRG_ERR_UNSUPPORTED, "grid too large for the shared-memory slab kernels");
+  }
+  const int nt = grid[0] + grid[1] + grid[2];
+  char* tw = (char*)ws;
+  char* scratch = tw + align256((size_t)csize(prec) * nt);
+  int rc = JRG_OK;
+  int off = 0;
+  for (int a = 0; a < 3 && !rc; ++a) {
+    rc = launch_twiddles(grid[a], prec, tw + (size_t)csize(prec) * off, st);
+    off += grid[a];
+  }
+  if (rc) return rc;
+  const double scale = direction > 0 ? 1.0 / ((double)grid[0] * grid[1] * grid[2]) : 1.0;
+  if (prec == 64)
+    return launch_fft3d_dense<double>(ax, (const double2*)tw, batch, direction, false, in,
+                                      (double2*)scratch, (double2*)out, scale, st);
+  return launch_fft3d_dense<float>(ax, (const float2*)tw, batch, direction, false, in,
+                                   (float2*)scratch, (float2*)out, scale, st);
+}
+
+int jrg_adam_update(int prec, int64_t n, void* param, const void* grad, void* m, void* v,
+                    const float* scale, int step, double lr, double b1, double b2, double eps,
+                    cudaStream_t st) {
+  if (!param || !grad || !m || !v || n < 0 || step < 1 || (prec != 32 && prec != 64))
+    return fail(JRG_ERR_INVALID, "jrg_adam_update: bad argument");
+  const double c1 = 1.0 - std::pow(b1, step), c2 = 1.0 - std::pow(b2, step);
+  if (prec == 64) return launch_adam<double>(param, grad, m, v, scale, n, lr, b1, b2, c1, c2, eps, st);
+  return launch_adam<float>(param, grad, m, v, scale, n, lr, b1, b2, c1, c2, eps, st);
+}
+
+int jrg_ewald(const jrg_plan* P, double eta, double cutoff, double* result, void* ws, cudaStream_t st) {
+  if (!P || !result || !ws || !(eta > 0) || !(cutoff > 0)) return fail(JRG_ERR_INVALID, "jrg_ewald: bad argument");
+  // translation grid: n = ceil(cutoff / |a1 + a2 + a3|^2) per axis, fftfreq ordering
+  double s[3] = {0, 0, 0};
+  for (int i = 0; i < 3; ++i)
+    for (int c = 0; c < 3; ++c) s[c] += P->cell[3 * i + c];
+  const double nrm2 = s[0] * s[0] + s[1] * s[1] + s[2] * s[2];
+  const int nt = (int)std::ceil(cutoff / nrm2);
+  if (nt < 1 || nt > 4096) return fail(JRG_ERR_UNSUPPORTED, "jrg_ewald: translation grid out of range");
+  const int na = (int)P->charge.size();
+  return launch_ewald(P->d_cell, P->d.gvec, P->d_atoms, P->d_atoms + 3 * na, na, nt, P->ngrid, eta,
+                      P->vol, (double*)wsp(ws, P->ws.epart), kEwaldBlocks, result, st);
+}
+
+}  // extern "C"

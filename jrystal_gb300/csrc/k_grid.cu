@@ -1,0 +1,464 @@
+// Single-grid kernels: density reduction, reciprocal-space Hartree and
+// external energies, LDA exchange-correlation, potential assembly, kinetic
+// energy on the sphere, energy-slot reduction, geometry tables and Ewald.
+// Energy sums are accumulated in FP64 per block and reduced deterministically.
+#include "plan.h"
+
+namespace jrg {
+
+// rho[s][i] = sum over the groups of spin s of part[g][i] (FP64 sum)
+template <typename R>
+__global__ void k_reduce_density(const R* __restrict__ part, R* __restrict__ rho, int groups_per_spin,
+                                 int ns, long long ngrid) {
+  const long long n = (long long)ns * ngrid;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long s = e / ngrid, i = e % ngrid;
+    double acc = 0.0;
+    for (int g = 0; g < groups_per_spin; ++g) acc += (double)part[((long long)s * groups_per_spin + g) * ngrid + i];
+    rho[e] = (R)acc;
+  }
+}
+
+// Reciprocal-space terms of a single (spin-summed) density transform rhog:
+//   E_H  = vol/N^2 * sum 1/2 ginv |rho_G|^2          (ginv = 4 pi/|G|^2, 0 at G=0)
+//   E_ext= vol/N^2 * sum Re(conj(Vext_G) rho_G)
+//   vg   = ginv * rho_G + Vext_G   (dE/d rho, reciprocal form, before the 1/N of the IFFT)
+template <typename R>
+__global__ void __launch_bounds__(256) k_recip_terms(const C_t<R>* __restrict__ rhog,
+                                                     const double* __restrict__ ginv,
+                                                     const C_t<R>* __restrict__ vext,
+                                                     C_t<R>* __restrict__ vg, double* __restrict__ slot_h,
+                                                     double* __restrict__ slot_e, long long ngrid,
+                                                     double pref) {
+  __shared__ double red[32];
+  double eh = 0.0, ee = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
+       i += (long long)gridDim.x * blockDim.x) {
+    const C_t<R> r = rhog[i];
+    const C_t<R> v = vext[i];
+    const double gi = ginv[i];
+    const double rx = r.x, ry = r.y;
+    eh += 0.5 * gi * (rx * rx + ry * ry);
+    ee += (double)v.x * rx + (double)v.y * ry;
+    C_t<R> o;
+    o.x = (R)(gi * rx + (double)v.x);
+    o.y = (R)(gi * ry + (double)v.y);
+    if (vg) vg[i] = o;
+  }
+  eh = block_sum(eh, red);
+  ee = block_sum(ee, red);
+  if (threadIdx.x == 0) { slot_h[blockIdx.x] = eh * pref; slot_e[blockIdx.x] = ee * pref; }
+}
+
+// LDA: Slater exchange + VWN (1980) paramagnetic correlation fit.
+__device__ __forceinline__ void lda_eps_v(double rho, int xc, double* eps, double* v) {
+  double e = 0.0, vv = 0.0;
+  if (rho > 1e-15) {
+    if (xc & JRG_XC_LDA_X) {
+      const double cx = 0.7385587663820224;   // (3/4) (3/pi)^(1/3)
+      const double ex = -cx * cbrt(rho);
+      e += ex;
+      vv += 4.0 / 3.0 * ex;
+    }
+    if (xc & JRG_XC_LDA_C_VWN) {
+      const double A = 0.0310907, b = 3.72744, c = 12.9352, x0 = -0.10498;
+      const double q = sqrt(4.0 * c - b * b);
+      const double xx0 = x0 * x0 + b * x0 + c;
+      const double rs = cbrt(3.0 / (4.0 * 3.14159265358979323846 * rho));
+      const double x = sqrt(rs);
+      const double xx = x * x + b * x + c;
+      const double at = atan(q / (2.0 * x + b));
+      const double ec = A * (log(x * x / xx) + 2.0 * b / q * at -
+                             b * x0 / xx0 * (log((x - x0) * (x - x0) / xx) + 2.0 * (b + 2.0 * x0) / q * at));
+      const double den = (2.0 * x + b) * (2.0 * x + b) + q * q;
+      const double dec = A * (2.0 / x - (2.0 * x + b) / xx - 4.0 * b / den -
+                              b * x0 / xx0 * (2.0 / (x - x0) - (2.0 * x + b) / xx - 4.0 * (b + 2.0 * x0) / den));
+      e += ec;
+      vv += ec - x / 6.0 * dec;
+    }
+  }
+  *eps = e;
+  *v = vv;
+}
+
+// V(r) = Re(vri)*vscale + v_xc(rho) (when vr is given);  E_xc = vol/N * sum eps(rho) rho.
+template <typename R>
+__global__ void __launch_bounds__(256) k_potential(const R* __restrict__ rho,
+                                                   const C_t<R>* __restrict__ vri, double vscale,
+                                                   R* __restrict__ vr, double* __restrict__ slot_x,
+                                                   long long ngrid, int xc, double pref) {
+  __shared__ double red[32];
+  double ex = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double r = rho[i];
+    double eps, v;
+    lda_eps_v(r, xc, &eps, &v);
+    ex += eps * r;
+    if (vr) vr[i] = (R)((double)vri[i].x * vscale + v);
+  }
+  ex = block_sum(ex, red);
+  if (threadIdx.x == 0) slot_x[blockIdx.x] = ex * pref;
+}
+
+// xc energy density (kohn_sham = 0) or v_xc (kohn_sham = 1) on the grid
+template <typename R>
+__global__ void k_xc_field(const R* __restrict__ rho, R* __restrict__ out, long long ngrid, int xc,
+                           int kohn_sham) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
+       i += (long long)gridDim.x * blockDim.x) {
+    double eps, v;
+    lda_eps_v((double)rho[i], xc, &eps, &v);
+    out[i] = (R)(kohn_sham ? v : eps);
+  }
+}
+
+// real part of a complex grid times a factor
+template <typename R>
+__global__ void k_real_part(const C_t<R>* __restrict__ in, R* __restrict__ out, long long n,
+                            double fac) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = (R)((double)in[i].x * fac);
+}
+
+// reciprocal Hartree potential (x fac) of a density transform
+template <typename R>
+__global__ void k_hartree_g(const C_t<R>* __restrict__ rhog, const double* __restrict__ ginv,
+                            C_t<R>* __restrict__ out, long long n, double fac) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double g = ginv[i] * fac;
+    C_t<R> o;
+    o.x = (R)(g * rhog[i].x);
+    o.y = (R)(g * rhog[i].y);
+    out[i] = o;
+  }
+}
+
+// kinetic energy per band: f * sum_g tk[k][g] |c[b][g]|^2, one block per band
+template <typename R>
+__global__ void __launch_bounds__(256) k_kinetic(const C_t<R>* __restrict__ coef,
+                                                 const double* __restrict__ tk,
+                                                 const double* __restrict__ occ,
+                                                 double* __restrict__ slot, int ng, int nb, int nk) {
+  __shared__ double red[32];
+  const int band = blockIdx.x;           // global (s, k, b)
+  const int k = (band / nb) % nk;
+  const C_t<R>* c = coef + (size_t)band * ng;
+  const double* t = tk + (size_t)k * ng;
+  double acc = 0.0;
+  for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+    const double x = c[g].x, y = c[g].y;
+    acc += t[g] * (x * x + y * y);
+  }
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) slot[band] = acc * occ[band];
+}
+
+// energies[t] = sum of its slots, t = 0..3; energies[4] = total
+__global__ void k_sum_slots(const double* __restrict__ slots, const int* __restrict__ slot_begin,
+                            double* __restrict__ energies, int nterms, const int* __restrict__ flags) {
+  __shared__ double red[32];
+  __shared__ double tot;
+  if (threadIdx.x == 0) tot = 0.0;
+  for (int t = 0; t < nterms; ++t) {
+    double acc = 0.0;
+    for (int i = slot_begin[t] + threadIdx.x; i < slot_begin[t + 1]; i += blockDim.x) acc += slots[i];
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) { energies[t] = acc; tot += acc; }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    energies[nterms] = tot;
+    energies[nterms + 2] = flags ? (double)flags[0] : 0.0;
+  }
+}
+
+// ------------------------------------------------------------------------
+// geometry tables (FP64): G vectors, 4 pi/|G|^2, external potential
+//   Vext(G) = -(4 pi N/vol) sum_a Z_a exp(-i G.R_a)/(|G|^2 + 1e-10), 0 at G=0
+// ------------------------------------------------------------------------
+__device__ __forceinline__ int fftfreq_int(int i, int n) { return (i < (n + 1) / 2) ? i : i - n; }
+
+template <typename R>
+__global__ void k_geometry_tables(double* __restrict__ gvec, double* __restrict__ ginv,
+                                  C_t<R>* __restrict__ vext, const double* __restrict__ recip,
+                                  const double* __restrict__ pos, const double* __restrict__ chg,
+                                  int natom, int nx, int ny, int nz, double vol) {
+  const long long n = (long long)nx * ny * nz;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(i / ((long long)ny * nz));
+    const int iy = (int)((i / nz) % ny);
+    const int iz = (int)(i % nz);
+    const double m0 = fftfreq_int(ix, nx), m1 = fftfreq_int(iy, ny), m2 = fftfreq_int(iz, nz);
+    double g[3];
+    for (int d = 0; d < 3; ++d) g[d] = m0 * recip[0 + d] + m1 * recip[3 + d] + m2 * recip[6 + d];
+    gvec[3 * i + 0] = g[0]; gvec[3 * i + 1] = g[1]; gvec[3 * i + 2] = g[2];
+    const double g2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+    const bool zero = (i == 0);
+    ginv[i] = zero ? 0.0 : 4.0 * 3.14159265358979323846 / g2;
+    double sx = 0.0, sy = 0.0;
+    if (!zero) {
+      for (int a = 0; a < natom; ++a) {
+        const double ph = g[0] * pos[3 * a] + g[1] * pos[3 * a + 1] + g[2] * pos[3 * a + 2];
+        double sn, cs;
+        sincos(ph, &sn, &cs);
+        sx += chg[a] * cs;
+        sy -= chg[a] * sn;
+      }
+      const double f = -4.0 * 3.14159265358979323846 * (double)n / vol / (g2 + 1e-10);
+      sx *= f; sy *= f;
+    }
+    vext[i] = cmk<C_t<R>>(sx, sy);
+  }
+}
+
+// ------------------------------------------------------------------------
+// Ewald nuclear repulsion (FP64)
+// real space:  1/2 sum_ij Z_i Z_j sum_t erfc(eta d)/d,  d = |R_j - R_i - t| (d <= 1e-9 skipped)
+// reciprocal:  (4 pi/vol) 1/2 sum_{G != 0} exp(-|G|^2/(4 eta^2))/|G|^2 |sum_i Z_i exp(i G.R_i)|^2
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_ewald_real(const double* __restrict__ cell,
+                                                    const double* __restrict__ pos,
+                                                    const double* __restrict__ chg, int natom,
+                                                    int nt, double eta, double* __restrict__ slot) {
+  __shared__ double red[32];
+  const long long ntot = (long long)nt * nt * nt;
+  double acc = 0.0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ntot;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int a0 = fftfreq_int((int)(t / ((long long)nt * nt)), nt);
+    const int a1 = fftfreq_int((int)((t / nt) % nt), nt);
+    const int a2 = fftfreq_int((int)(t % nt), nt);
+    double tv[3];
+    for (int d = 0; d < 3; ++d) tv[d] = a0 * cell[d] + a1 * cell[3 + d] + a2 * cell[6 + d];
+    for (int i = 0; i < natom; ++i) {
+      for (int j = 0; j < natom; ++j) {
+        const double dx = pos[3 * j] - pos[3 * i] - tv[0];
+        const double dy = pos[3 * j + 1] - pos[3 * i + 1] - tv[1];
+        const double dz = pos[3 * j + 2] - pos[3 * i + 2] - tv[2];
+        const double d = sqrt(dx * dx + dy * dy + dz * dz + 1e-20);
+        if (d > 1e-9) acc += chg[i] * chg[j] * erfc(eta * d) / d;
+      }
+    }
+  }
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) slot[blockIdx.x] = 0.5 * acc;
+}
+
+__global__ void __launch_bounds__(256) k_ewald_recip(const double* __restrict__ gvec,
+                                                     const double* __restrict__ pos,
+                                                     const double* __restrict__ chg, int natom,
+                                                     long long ngrid, double eta, double vol,
+                                                     double* __restrict__ slot) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (long long i = 1 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double gx = gvec[3 * i], gy = gvec[3 * i + 1], gz = gvec[3 * i + 2];
+    const double g2 = gx * gx + gy * gy + gz * gz;
+    const double kern = exp(-g2 / 4.0 / (eta * eta)) / g2;
+    if (kern == 0.0) continue;
+    double sx = 0.0, sy = 0.0;
+    for (int a = 0; a < natom; ++a) {
+      double sn, cs;
+      sincos(gx * pos[3 * a] + gy * pos[3 * a + 1] + gz * pos[3 * a + 2], &sn, &cs);
+      sx += chg[a] * cs;
+      sy += chg[a] * sn;
+    }
+    acc += kern * (sx * sx + sy * sy);
+  }
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) slot[blockIdx.x] = 0.5 * 4.0 * 3.14159265358979323846 / vol * acc;
+}
+
+__global__ void k_ewald_finish(const double* __restrict__ slots, int nslots, const double* __restrict__ chg,
+                               int natom, double eta, double vol, double* __restrict__ out) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nslots; i += blockDim.x) acc += slots[i];
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) {
+    double z2 = 0.0, z = 0.0;
+    for (int a = 0; a < natom; ++a) { z2 += chg[a] * chg[a]; z += chg[a]; }
+    const double pi = 3.14159265358979323846;
+    double self = -z2 * 2.0 * eta / sqrt(pi) / 2.0;
+    self -= z * z * pi / (eta * eta) / vol / 2.0;
+    out[0] = acc + self;
+  }
+}
+
+// ------------------------------------------------------------------------
+// Adam (optax placement of eps) with optional elementwise update scale
+// ------------------------------------------------------------------------
+template <typename R>
+__global__ void k_adam(R* __restrict__ p, const R* __restrict__ g, R* __restrict__ m,
+                       R* __restrict__ v, const float* __restrict__ scale, long long n, R lr, R b1,
+                       R b2, R c1, R c2, R eps) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const R gi = g[i];
+    const R mi = b1 * m[i] + (1 - b1) * gi;
+    const R vi = b2 * v[i] + (1 - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    R u = -lr * (mi / c1) / (sqrt(vi / c2) + eps);
+    if (scale) u *= (R)scale[i];
+    p[i] += u;
+  }
+}
+
+// twiddle table W_n^t = exp(-2 pi i t/n), t < n, evaluated in FP64
+template <typename R>
+__global__ void k_twiddles(int n, C_t<R>* __restrict__ out) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(-2.0 * (double)t / (double)n, &s, &c);
+    out[t] = cmk<C_t<R>>(c, s);
+  }
+}
+
+// ------------------------------------------------------------------------
+// launch helpers
+// ------------------------------------------------------------------------
+static inline unsigned grid_for(long long n, int per = 256, int cap = 4096) {
+  long long b = (n + per - 1) / per;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+template <typename R>
+int launch_reduce_density(const void* part, void* rho, int groups_per_spin, int ns, long long ngrid,
+                          cudaStream_t st) {
+  k_reduce_density<R><<<grid_for(ns * ngrid), 256, 0, st>>>(
+      reinterpret_cast<const R*>(part), reinterpret_cast<R*>(rho), groups_per_spin, ns, ngrid);
+  JRG_LAUNCH_CHECK("k_reduce_density");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_recip_terms(const void* rhog, const double* ginv, const void* vext, void* vg,
+                       double* slot_h, double* slot_e, int nblocks, long long ngrid, double pref,
+                       cudaStream_t st) {
+  k_recip_terms<R><<<nblocks, 256, 0, st>>>(
+      reinterpret_cast<const C_t<R>*>(rhog), ginv, reinterpret_cast<const C_t<R>*>(vext),
+      reinterpret_cast<C_t<R>*>(vg), slot_h, slot_e, ngrid, pref);
+  JRG_LAUNCH_CHECK("k_recip_terms");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_potential(const void* rho, const void* vri, double vscale, void* vr, double* slot_x,
+                     int nblocks, long long ngrid, int xc, double pref, cudaStream_t st) {
+  k_potential<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const R*>(rho),
+                                          reinterpret_cast<const C_t<R>*>(vri), vscale,
+                                          reinterpret_cast<R*>(vr), slot_x, ngrid, xc, pref);
+  JRG_LAUNCH_CHECK("k_potential");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_xc_field(const void* rho, void* out, long long ngrid, int xc, int ks, cudaStream_t st) {
+  k_xc_field<R><<<grid_for(ngrid), 256, 0, st>>>(reinterpret_cast<const R*>(rho),
+                                                 reinterpret_cast<R*>(out), ngrid, xc, ks);
+  JRG_LAUNCH_CHECK("k_xc_field");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_real_part(const void* in, void* out, long long n, double fac, cudaStream_t st) {
+  k_real_part<R><<<grid_for(n), 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(in),
+                                              reinterpret_cast<R*>(out), n, fac);
+  JRG_LAUNCH_CHECK("k_real_part");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_hartree_g(const void* rhog, const double* ginv, void* out, long long n, double fac,
+                     cudaStream_t st) {
+  k_hartree_g<R><<<grid_for(n), 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(rhog), ginv,
+                                               reinterpret_cast<C_t<R>*>(out), n, fac);
+  JRG_LAUNCH_CHECK("k_hartree_g");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_kinetic(const void* coef, const double* tk, const double* occ, double* slot, int nbands,
+                   int ng, int nb, int nk, cudaStream_t st) {
+  k_kinetic<R><<<nbands, 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(coef), tk, occ, slot, ng, nb,
+                                       nk);
+  JRG_LAUNCH_CHECK("k_kinetic");
+  return JRG_OK;
+}
+
+int launch_sum_slots(const double* slots, const int* slot_begin, double* energies, int nterms,
+                     const int* flags, cudaStream_t st) {
+  k_sum_slots<<<1, 256, 0, st>>>(slots, slot_begin, energies, nterms, flags);
+  JRG_LAUNCH_CHECK("k_sum_slots");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_geometry_tables(double* gvec, double* ginv, void* vext, const double* recip,
+                           const double* pos, const double* chg, int natom, int nx, int ny, int nz,
+                           double vol, cudaStream_t st) {
+  k_geometry_tables<R><<<grid_for((long long)nx * ny * nz), 256, 0, st>>>(
+      gvec, ginv, reinterpret_cast<C_t<R>*>(vext), recip, pos, chg, natom, nx, ny, nz, vol);
+  JRG_LAUNCH_CHECK("k_geometry_tables");
+  return JRG_OK;
+}
+
+int launch_ewald(const double* cell, const double* gvec, const double* pos, const double* chg,
+                 int natom, int nt, long long ngrid, double eta, double vol, double* slots,
+                 int nslots_half, double* out, cudaStream_t st) {
+  k_ewald_real<<<nslots_half, 256, 0, st>>>(cell, pos, chg, natom, nt, eta, slots);
+  JRG_LAUNCH_CHECK("k_ewald_real");
+  k_ewald_recip<<<nslots_half, 256, 0, st>>>(gvec, pos, chg, natom, ngrid, eta, vol,
+                                             slots + nslots_half);
+  JRG_LAUNCH_CHECK("k_ewald_recip");
+  k_ewald_finish<<<1, 256, 0, st>>>(slots, 2 * nslots_half, chg, natom, eta, vol, out);
+  JRG_LAUNCH_CHECK("k_ewald_finish");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_adam(void* p, const void* g, void* m, void* v, const float* scale, long long n, double lr,
+                double b1, double b2, double c1, double c2, double eps, cudaStream_t st) {
+  k_adam<R><<<grid_for(n, 256, 8192), 256, 0, st>>>(
+      reinterpret_cast<R*>(p), reinterpret_cast<const R*>(g), reinterpret_cast<R*>(m),
+      reinterpret_cast<R*>(v), scale, n, (R)lr, (R)b1, (R)b2, (R)c1, (R)c2, (R)eps);
+  JRG_LAUNCH_CHECK("k_adam");
+  return JRG_OK;
+}
+
+int launch_twiddles(int n, int prec, void* out, cudaStream_t st) {
+  if (prec == 64) k_twiddles<double><<<1, 128, 0, st>>>(n, reinterpret_cast<double2*>(out));
+  else k_twiddles<float><<<1, 128, 0, st>>>(n, reinterpret_cast<float2*>(out));
+  JRG_LAUNCH_CHECK("k_twiddles");
+  return JRG_OK;
+}
+
+#define JRG_INST_GRID(R)                                                                        \
+  template int launch_reduce_density<R>(const void*, void*, int, int, long long, cudaStream_t);   \
+  template int launch_recip_terms<R>(const void*, const double*, const void*, void*, double*,     \
+                                     double*, int, long long, double, cudaStream_t);            \
+  template int launch_potential<R>(const void*, const void*, double, void*, double*, int,         \
+                                   long long, int, double, cudaStream_t);                       \
+  template int launch_xc_field<R>(const void*, void*, long long, int, int, cudaStream_t);         \
+  template int launch_real_part<R>(const void*, void*, long long, double, cudaStream_t);          \
+  template int launch_hartree_g<R>(const void*, const double*, void*, long long, double,          \
+                                   cudaStream_t);                                               \
+  template int launch_kinetic<R>(const void*, const double*, const double*, double*, int, int,    \
+                                 int, int, cudaStream_t);                                       \
+  template int launch_geometry_tables<R>(double*, double*, void*, const double*, const double*,   \
+                                         const double*, int, int, int, int, double, cudaStream_t); \
+  template int launch_adam<R>(void*, const void*, void*, void*, const float*, long long, double,  \
+                              double, double, double, double, double, cudaStream_t);
+JRG_INST_GRID(float)
+JRG_INST_GRID(double)
+
+}  // namespace jrg

@@ -1,0 +1,73 @@
+// Internal plan layout shared by the kernels and the C ABI.
+#pragma once
+#include <string>
+#include <vector>
+#include "../../include/jrystal_gb300.h"
+#include "fft_smem.cuh"
+
+namespace jrg {
+
+// Thread-local error reporting for the C ABI.
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define JRG_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return ::jrg::cuda_fail(e_, #call); \
+  } while (0)
+
+#define JRG_LAUNCH_CHECK(what)                           \
+  do {                                                   \
+    cudaError_t e_ = cudaGetLastError();                 \
+    if (e_ != cudaSuccess) return ::jrg::cuda_fail(e_, what); \
+  } while (0)
+
+bool factor_axis(int n, FftAxis* ax);
+
+// Device tables of one plan.
+struct PlanTables {
+  int* gidx = nullptr;        // [ng] flattened grid index
+  int* sph_yz = nullptr;      // [ng] y*nz + z
+  int* plane_x = nullptr;     // [nact] x index of each active plane
+  int* plane_off = nullptr;   // [nact+1] sphere offsets per plane
+  int* row_off = nullptr;     // [nact+1] offsets into rows
+  int* rows = nullptr;        // active y rows per plane
+  int* xact = nullptr;        // [nx] active-plane slot of x, or -1
+  double* tk = nullptr;       // [nk][ng] |G+k|^2 / 2
+  void* tw = nullptr;         // twiddles: x table, y table, z table (C_t<R>)
+  void* vext = nullptr;       // [ngrid] complex V_ext(G) in precision R
+  double* ginv = nullptr;     // [ngrid] 4 pi / |G|^2, 0 at G = 0
+  double* gvec = nullptr;     // [ngrid][3] cartesian G vectors
+};
+
+// Workspace offsets (bytes) of one plan.
+struct Workspace {
+  size_t wc, c, gram_part, gram, rmat, rinv, t, u, rho_part, rho, rhog, fft_scratch, vr,
+      gc, adj_part, adj, kmat, epart, flags, total;
+  int gram_splits;
+  int ngroups;    // density partial groups
+  int nepart;     // energy partial slots
+};
+
+}  // namespace jrg
+
+struct jrg_plan {
+  int prec;                 // 32 or 64
+  int nx, ny, nz;
+  long long ngrid;
+  int ns, nk, nb, ng;
+  int nact;                 // active x planes
+  int max_rows;             // max active rows in a plane
+  double cell[9], recip[9], vol;
+  std::vector<double> pos, charge, kpts;
+  int xc;
+  jrg::FftAxis ax[3];
+  jrg::PlanTables d;
+  jrg::Workspace ws;
+  int device;
+  int* slot_begin = nullptr;  // energy slot boundaries [5]
+  double* d_cell = nullptr;   // cell (9) then reciprocal vectors (9)
+  double* d_atoms = nullptr;  // positions [natom][3] then charges [natom]
+};

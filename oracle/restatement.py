@@ -1,0 +1,654 @@
+"""FP64 NumPy restatement of jrystal's direct-minimisation path.
+
+TEST INFRASTRUCTURE ONLY: the oracle the CUDA library is checked against.
+Product code never imports this module.
+
+Array conventions follow jrystal: parameters ``w_re``/``w_im`` of shape
+(spin, kpt, num_g, band); dense coefficient grids (spin, kpt, band, x, y, z);
+densities (spin, x, y, z); G vectors in fftfreq order.
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+# jrystal/_src/const.py:18 (the Angstrom->Bohr factor jrystal applies on read).
+ANGSTROM2BOHR = 1.8897259886
+
+_SYMBOLS = (
+  "X H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co "
+  "Ni Cu Zn Ga Ge As Se Br Kr Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te "
+  "I Xe Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho Er Tm Yb Lu Hf Ta W Re Os Ir "
+  "Pt Au Hg Tl Pb Bi Po At Rn"
+).split()
+ATOMIC_NUMBER = {s: i for i, s in enumerate(_SYMBOLS) if i > 0}
+
+
+# --------------------------------------------------------------------------
+# crystal / geometry   (jrystal/_src/crystal.py:124-152, utils.py:133-158)
+# --------------------------------------------------------------------------
+@dataclass
+class Crystal:
+  charges: np.ndarray
+  positions: np.ndarray       # bohr
+  cell_vectors: np.ndarray    # bohr, rows are lattice vectors
+  spin: int = 0
+  symbols: list = field(default_factory=list)
+
+  @property
+  def vol(self):
+    return abs(np.linalg.det(self.cell_vectors))
+
+  @property
+  def scaled_positions(self):
+    return self.positions @ np.linalg.inv(self.cell_vectors).T
+
+  @property
+  def reciprocal_vectors(self):
+    return 2 * np.pi * np.linalg.inv(self.cell_vectors).T
+
+  @property
+  def num_electron(self):
+    return int(np.sum(self.charges))
+
+
+def read_xyz(path: str, spin: Optional[int] = None) -> Crystal:
+  """Extended-xyz reader (Lattice="..." header, species + Cartesian Å).
+
+  Follows ``Crystal.create_from_file`` (jrystal/_src/crystal.py:124-152):
+  positions and cell in Å times ANGSTROM2BOHR; spin defaults to the parity
+  of the electron count (crystal.py:143-145).
+  """
+  with open(path) as f:
+    lines = [ln.rstrip("\n") for ln in f]
+  nat = int(lines[0].split()[0])
+  header = lines[1]
+  i = header.index('Lattice="') + len('Lattice="')
+  j = header.index('"', i)
+  cell = np.array([float(v) for v in header[i:j].split()]).reshape(3, 3)
+  symbols, pos = [], []
+  for ln in lines[2:2 + nat]:
+    parts = ln.split()
+    symbols.append(parts[0])
+    pos.append([float(v) for v in parts[1:4]])
+  charges = np.array([ATOMIC_NUMBER[s] for s in symbols])
+  positions = np.array(pos) * ANGSTROM2BOHR
+  cell = cell * ANGSTROM2BOHR
+  if spin is None:
+    spin = int(np.sum(charges)) % 2
+  return Crystal(charges, positions, cell, spin, symbols)
+
+
+# --------------------------------------------------------------------------
+# grids   (jrystal/_src/grid.py, utils.py:227-254)
+# --------------------------------------------------------------------------
+def fft_sizes(limit: int = 2048):
+  """7-smooth sizes up to ``limit`` (the table jrystal/_src/const.py:265)."""
+  out = set()
+  p2 = 1
+  while p2 <= limit:
+    p3 = p2
+    while p3 <= limit:
+      p5 = p3
+      while p5 <= limit:
+        p7 = p5
+        while p7 <= limit:
+          out.add(p7)
+          p7 *= 7
+        p5 *= 5
+      p3 *= 3
+    p2 *= 2
+  return sorted(out)
+
+
+def fft_factor(n: int) -> int:
+  """jrystal/_src/utils.py:227-254."""
+  if n > 2048:
+    raise ValueError(f"The grid number {n} is too large!")
+  for v in fft_sizes():
+    if v >= n:
+      return v
+  raise ValueError(n)
+
+
+def proper_grid_size(grid_sizes):
+  """jrystal/_src/grid.py:181-210."""
+  if hasattr(grid_sizes, "__len__"):
+    g = np.array(grid_sizes)
+  else:
+    g = np.ones(3, dtype=int) * int(grid_sizes)
+  return np.array([fft_factor(int(i)) for i in g])
+
+
+def _vector_grid(basis, grid_sizes, normalize=False):
+  """jrystal/_src/grid.py:93-119 (fftfreq-ordered lattice combination)."""
+  dim = len(grid_sizes)
+  out = 0.
+  for i in range(dim):
+    shape = tuple(grid_sizes[i] if a == i else 1 for a in range(dim)) + (dim,)
+    freq = np.fft.fftfreq(grid_sizes[i], 1 if normalize else 1 / grid_sizes[i])
+    out = out + np.reshape(np.outer(freq, basis[i]), shape)
+  return out
+
+
+def g_vectors(cell_vectors, grid_sizes):
+  """jrystal/_src/grid.py:122-149."""
+  b = 2 * np.pi * np.linalg.inv(cell_vectors).T
+  return _vector_grid(b, list(grid_sizes))
+
+
+def r_vectors(cell_vectors, grid_sizes):
+  """jrystal/_src/grid.py:152-178."""
+  return _vector_grid(np.asarray(cell_vectors), list(grid_sizes), True)
+
+
+def monkhorst_pack(size):
+  """ase.dft.kpoints.monkhorst_pack: fractional (i + 1/2)/n - 1/2."""
+  size = np.asarray(size)
+  idx = np.indices(size).transpose((1, 2, 3, 0)).reshape((-1, 3))
+  return (idx + 0.5) / size - 0.5
+
+
+def k_vectors(cell_vectors, grid_sizes):
+  """jrystal/_src/grid.py:239-262."""
+  b = 2 * np.pi * np.linalg.inv(cell_vectors).T
+  return monkhorst_pack(grid_sizes) @ b
+
+
+def spherical_mask(cell_vectors, grid_sizes, cutoff_energy):
+  """jrystal/_src/grid.py:265-293."""
+  g = g_vectors(cell_vectors, grid_sizes)
+  return np.linalg.norm(g, axis=-1)**2 <= cutoff_energy * 2
+
+
+def cubic_mask(grid_sizes):
+  """jrystal/_src/grid.py:296-325."""
+  masks = []
+  for size in grid_sizes:
+    g_max = (size - 1) // 2
+    lo, hi = -g_max // 2, g_max // 2
+    m = np.ones((size,), dtype=bool)
+    m[hi + 1:lo] = False
+    masks.append(m)
+  return np.einsum("i,j,k->ijk", *masks)
+
+
+def translation_vectors(cell_vectors, cutoff=1e4):
+  """jrystal/_src/grid.py:213-236."""
+  n = int(np.ceil(cutoff / np.linalg.norm(np.sum(cell_vectors, axis=0))**2))
+  grid = _vector_grid(np.asarray(cell_vectors), [n, n, n])
+  return np.reshape(grid, [-1, 3])
+
+
+def alias_free_cutoff(cell_vectors, n):
+  """Largest alias-free sphere for an n^3 grid: 1/2 (R/2)^2 with
+  R = (n/2) 2pi / max|a_i| (the cutoff convention of the benchmark cells)."""
+  r = (n / 2) * 2 * np.pi / np.max(np.linalg.norm(cell_vectors, axis=1))
+  return 0.5 * (r / 2)**2
+
+
+# --------------------------------------------------------------------------
+# plane-wave map   (jrystal/_src/pw.py, unitary_module.py, utils.py)
+# --------------------------------------------------------------------------
+def unitary_householder(w_re, w_im):
+  """Reduced QR of W = w_re + i w_im over (num_g, band): unitary_module.py:64-80."""
+  w = np.asarray(w_re) + 1j * np.asarray(w_im)
+  q, _ = np.linalg.qr(w, mode="reduced")
+  return q
+
+
+def cholesky_qr(w_re, w_im):
+  """Q = W R^{-1} with R^H R = W^H W (R upper, positive diagonal).
+
+  Equal to the Householder Q of unitary_module.py:74-80 up to a unit-modulus
+  phase per column, which every energy term is invariant to.
+  """
+  w = np.asarray(w_re) + 1j * np.asarray(w_im)
+  s = np.einsum("...gi,...gj->...ij", w.conj(), w)
+  low = np.linalg.cholesky(s)                # s = L L^H
+  r = np.swapaxes(low.conj(), -1, -2)        # R = L^H
+  rinv = np.linalg.inv(r)
+  return w @ rinv, r
+
+
+def expand_coefficient(coeff_compact, mask):
+  """jrystal/_src/utils.py:257-281: (s,k,g,b) -> (s,k,b,x,y,z)."""
+  c = np.swapaxes(coeff_compact, -1, -2)
+  out = np.zeros(c.shape[:-1] + mask.shape, dtype=c.dtype)
+  out[..., mask] = c
+  return out
+
+
+def squeeze_coefficient(coeff, mask):
+  """jrystal/_src/utils.py:284-308: (s,k,b,x,y,z) -> (s,k,g,b)."""
+  return np.swapaxes(coeff[..., mask], -1, -2)
+
+
+def coeff(w_re, w_im, mask):
+  """jrystal/_src/pw.py:94-137 (dense grid of orthonormal coefficients)."""
+  return expand_coefficient(unitary_householder(w_re, w_im), mask)
+
+
+def wave_grid(coeff_dense, vol):
+  """jrystal/_src/pw.py:140-211: IFFT_3 * N / sqrt(vol)."""
+  n = np.prod(coeff_dense.shape[-3:])
+  return np.fft.ifftn(coeff_dense, axes=(-3, -2, -1)) * n / np.sqrt(vol)
+
+
+def wave_r(r, coeff_dense, cell_vectors, g_vector_grid=None):
+  """jrystal/_src/pw.py:337-379: direct O(G) evaluation at one point."""
+  vol = abs(np.linalg.det(cell_vectors))
+  if g_vector_grid is None:
+    g_vector_grid = g_vectors(cell_vectors, coeff_dense.shape[-3:])
+  phase = np.exp(1j * g_vector_grid @ r)
+  return np.einsum("...xyz,xyz->...", coeff_dense, phase) / np.sqrt(vol)
+
+
+def wave_to_density(wave, occupation=None):
+  """jrystal/_src/utils.py:161-197."""
+  dens = np.real(np.conj(wave) * wave)
+  if occupation is not None:
+    dens = np.einsum("skb...,skb->s...", dens, occupation)
+  return dens
+
+
+def density_grid(coeff_dense, vol, occupation=None):
+  """jrystal/_src/pw.py:214-284."""
+  return wave_to_density(wave_grid(coeff_dense, vol), occupation)
+
+
+def density_grid_reciprocal(coeff_dense, vol, occupation=None):
+  """jrystal/_src/pw.py:287-334 (unnormalised forward FFT)."""
+  return np.fft.fftn(density_grid(coeff_dense, vol, occupation),
+                     axes=(-3, -2, -1))
+
+
+# --------------------------------------------------------------------------
+# occupations, entropy   (jrystal/_src/occupation.py, entropy.py)
+# --------------------------------------------------------------------------
+def uniform_occupation(num_k, num_electrons, spin=0, num_bands=None,
+                       spin_restricted=True):
+  """jrystal/_src/occupation.py:147-190."""
+  num_bands = num_electrons if num_bands is None else num_bands
+  occ = np.zeros([2, num_k, num_bands])
+  occ[0, :, :(num_electrons + spin) // 2] = 1 / num_k
+  occ[1, :, :(num_electrons - spin) // 2] = 1 / num_k
+  if spin_restricted:
+    return np.sum(occ, axis=0, keepdims=True)
+  return occ
+
+
+def gamma_occupation(num_k, num_electrons, spin=0, num_bands=None,
+                     spin_restricted=True):
+  """jrystal/_src/occupation.py:193-237."""
+  num_bands = num_electrons if num_bands is None else num_bands
+  occ = np.zeros([2, num_k, num_bands])
+  occ[0, 0, :(num_electrons + spin) // 2] = 1
+  occ[1, 0, :(num_electrons - spin) // 2] = 1
+  if spin_restricted:
+    return np.sum(occ, axis=0, keepdims=True)
+  return occ
+
+
+def fermi_dirac_entropy(occ, eps=1e-8):
+  """jrystal/_src/entropy.py:19-54."""
+  num_spin, num_k, _ = occ.shape
+  top = (3 - num_spin) / num_k
+  return -np.sum(occ * np.log(eps + occ) + (top - occ) * np.log(eps + top - occ))
+
+
+# --------------------------------------------------------------------------
+# exchange-correlation: jax_xc 0.0.8 lda_x + lda_c_vwn (unpolarised)
+# restated from Slater exchange and the VWN (1980) paramagnetic fit.
+# --------------------------------------------------------------------------
+DENS_THRESHOLD = 1e-15
+VWN_A, VWN_B, VWN_C, VWN_X0 = 0.0310907, 3.72744, 12.9352, -0.10498
+
+
+def lda_x(rho):
+  """Slater exchange energy per particle and its potential d(rho e)/d rho."""
+  rho = np.asarray(rho, dtype=np.float64)
+  ok = rho > DENS_THRESHOLD
+  r = np.where(ok, rho, 1.0)
+  eps = -0.75 * (3.0 / np.pi)**(1.0 / 3.0) * np.cbrt(r)
+  return np.where(ok, eps, 0.0), np.where(ok, 4.0 / 3.0 * eps, 0.0)
+
+
+def lda_c_vwn(rho):
+  """VWN5 paramagnetic correlation energy per particle and potential."""
+  rho = np.asarray(rho, dtype=np.float64)
+  ok = rho > DENS_THRESHOLD
+  r = np.where(ok, rho, 1.0)
+  a, b, c, x0 = VWN_A, VWN_B, VWN_C, VWN_X0
+  q = math.sqrt(4 * c - b * b)
+  xx0 = x0 * x0 + b * x0 + c
+  rs = np.cbrt(3.0 / (4.0 * np.pi * r))
+  x = np.sqrt(rs)
+  xx = x * x + b * x + c
+  at = np.arctan(q / (2 * x + b))
+  eps = a * (np.log(x * x / xx) + 2 * b / q * at - b * x0 / xx0 *
+             (np.log((x - x0)**2 / xx) + 2 * (b + 2 * x0) / q * at))
+  den = (2 * x + b)**2 + q * q
+  deps_dx = a * (2 / x - (2 * x + b) / xx - 4 * b / den - b * x0 / xx0 *
+                 (2 / (x - x0) - (2 * x + b) / xx - 4 * (b + 2 * x0) / den))
+  # v = eps + rho d eps/d rho, and rho d/d rho = -(rs/3) d/d rs = -(x/6) d/dx
+  v = eps - x / 6.0 * deps_dx
+  return np.where(ok, eps, 0.0), np.where(ok, v, 0.0)
+
+
+_XC = {"lda_x": lda_x, "lda_c_vwn": lda_c_vwn}
+
+
+def xc_eps_v(rho, xc_type="lda_x"):
+  """Sum over the '+'-separated parts (jrystal/_src/xc.py:242-253)."""
+  eps = np.zeros_like(rho, dtype=np.float64)
+  v = np.zeros_like(rho, dtype=np.float64)
+  for name in xc_type.split("+"):
+    if name not in _XC:
+      raise NotImplementedError(f"xc functional {name!r} is not restated")
+    e, vv = _XC[name](rho)
+    eps += e
+    v += vv
+  return eps, v
+
+
+def xc_density(density_grid, kohn_sham=False, xc_type="lda_x"):
+  """jrystal/_src/xc.py:222-253 (LDA branch, unpolarised)."""
+  if density_grid.shape[0] != 1:
+    raise NotImplementedError("polarised xc is not restated")
+  eps, v = xc_eps_v(density_grid[0], xc_type)
+  return v[None] if kohn_sham else eps
+
+
+# --------------------------------------------------------------------------
+# potentials and energies   (jrystal/_src/potential.py, energy.py, braket.py)
+# --------------------------------------------------------------------------
+def _g2_safe(g_vector_grid):
+  g2 = np.sum(g_vector_grid**2, axis=-1)
+  return g2
+
+
+def hartree_reciprocal(density_grid_reciprocal, g_vector_grid,
+                       kohn_sham=False):
+  """jrystal/_src/potential.py:24-77."""
+  rho_g = np.sum(density_grid_reciprocal, axis=0)
+  g2 = _g2_safe(g_vector_grid).copy()
+  g2[0, 0, 0] = 1.0
+  out = rho_g / g2
+  out[0, 0, 0] = 0.0
+  out = out * 4 * np.pi
+  if not kohn_sham:
+    out = out / 2
+  return out
+
+
+def external_reciprocal(position, charge, g_vector_grid, vol):
+  """jrystal/_src/potential.py:121-166."""
+  g2 = _g2_safe(g_vector_grid)[..., None]
+  si = np.exp(-1j * (g_vector_grid @ np.asarray(position).T))
+  num = np.prod(g_vector_grid.shape[:-1])
+  vi = np.asarray(charge, dtype=np.float64)[None, None, None] / (g2 + 1e-10)
+  vi[0, 0, 0] = 0.0
+  vi = vi * 4 * np.pi
+  return -np.sum(vi * si, axis=-1) * num / vol
+
+
+def reciprocal_braket(bra, ket, vol):
+  """jrystal/_src/braket.py:27-72."""
+  num = np.prod(bra.shape)
+  return (np.sum(np.conj(bra) * ket) / num * vol / num).real
+
+
+def real_braket(bra, ket, vol):
+  """jrystal/_src/braket.py:75-114."""
+  num = np.prod(bra.shape)
+  return np.sum(bra * ket) * vol / num
+
+
+def expectation(bra, hamiltonian, vol, diagonal=True, mode="real"):
+  """jrystal/_src/braket.py:117-206 (diagonal=True/False, 3/4-dim operator)."""
+  num = np.prod(bra.shape[-3:])
+  factor = {"real": vol / num, "reciprocal": vol / num / num,
+            "kinetic": 1.0}[mode]
+  h = hamiltonian if hamiltonian.ndim == 4 else hamiltonian[None]
+  hb = h[None, :, None] * bra                   # (s,k,b,x,y,z)
+  if diagonal:
+    out = np.einsum("skbxyz,skbxyz->skb", np.conj(bra), hb)
+  else:
+    out = np.einsum("skixyz,skjxyz->skij", np.conj(bra), hb)
+  return out * factor
+
+
+def hartree_energy(density_grid_reciprocal, g_vector_grid, vol,
+                   kohn_sham=False):
+  """jrystal/_src/energy.py:29-82."""
+  v = hartree_reciprocal(density_grid_reciprocal, g_vector_grid, kohn_sham)
+  return reciprocal_braket(v[None], density_grid_reciprocal, vol)
+
+
+def external_energy(density_grid_reciprocal, position, charge, g_vector_grid,
+                    vol):
+  """jrystal/_src/energy.py:85-135."""
+  v = external_reciprocal(position, charge, g_vector_grid, vol)
+  return reciprocal_braket(v[None], density_grid_reciprocal, vol)
+
+
+def kinetic_operator(g_vector_grid, kpts=None):
+  """jrystal/_src/kinetic.py:21-44."""
+  kpts = np.zeros([1, 3]) if kpts is None else np.asarray(kpts)
+  return np.sum((g_vector_grid[None] + kpts[:, None, None, None])**2,
+                axis=-1) / 2
+
+
+def kinetic_energy(g_vector_grid, kpts, coeff_dense, occupation=None):
+  """jrystal/_src/energy.py:138-182."""
+  ek = 2 * kinetic_operator(g_vector_grid, kpts)           # (k,x,y,z)
+  e = np.einsum("kxyz,skbxyz->skb", ek, np.abs(coeff_dense)**2)
+  if occupation is not None:
+    return np.sum(e * occupation) / 2
+  return e / 2
+
+
+def xc_energy(density_grid, vol, xc_type="lda_x", kohn_sham=False):
+  """jrystal/_src/energy.py:185-211."""
+  num = np.prod(density_grid.shape[-3:])
+  e = xc_density(density_grid, kohn_sham, xc_type)
+  return np.sum(e * density_grid) * vol / num
+
+
+def effective(density_grid, position, charge, g_vector_grid, vol,
+              split=False, xc_type="lda_x", kohn_sham=False):
+  """jrystal/_src/potential.py:203-279."""
+  if density_grid.ndim == 3:
+    density_grid = density_grid[None]
+  rho_g = np.fft.fftn(density_grid, axes=(-3, -2, -1))
+  v_h = np.fft.ifftn(hartree_reciprocal(rho_g, g_vector_grid, kohn_sham))
+  v_e = np.fft.ifftn(external_reciprocal(position, charge, g_vector_grid, vol))
+  v_xc = xc_density(density_grid, kohn_sham, xc_type)
+  if split:
+    return v_h, v_e, v_xc
+  return v_h[None] + v_e[None] + v_xc
+
+
+def total_energy(coeff_dense, position, charge, g_vector_grid, kpts, vol,
+                 occupation=None, kohn_sham=False, xc="lda_x", split=False):
+  """jrystal/_src/energy.py:246-307 (no Ewald term)."""
+  wave = wave_grid(coeff_dense, vol)
+  if occupation is None:
+    occupation = np.ones(coeff_dense.shape[:3])
+  rho = wave_to_density(wave, occupation)
+  rho_g = np.fft.fftn(rho, axes=(-3, -2, -1))
+  e_kin = kinetic_energy(g_vector_grid, kpts, coeff_dense, occupation)
+  e_ext = external_energy(rho_g, position, charge, g_vector_grid, vol)
+  e_har = hartree_energy(rho_g, g_vector_grid, vol, kohn_sham)
+  e_xc = xc_energy(rho, vol, xc, kohn_sham)
+  if split:
+    return e_kin, e_ext, e_har, e_xc
+  return e_kin + e_ext + e_har + e_xc
+
+
+def hamiltonian_matrix_trace(coeff_dense, position, charge, density_grid,
+                             g_vector_grid, kpts, vol, xc="lda_x",
+                             kohn_sham=True, keep_kpts_axis=False):
+  """jrystal/_src/hamiltonian.py:105-168."""
+  v_eff = effective(density_grid, position, charge, g_vector_grid, vol,
+                    False, xc, kohn_sham)
+  wave = wave_grid(coeff_dense, vol)
+  f_eff = expectation(wave, v_eff, vol, diagonal=True, mode="real")
+  t_kin = kinetic_operator(g_vector_grid, kpts)
+  f_kin = expectation(coeff_dense, t_kin, vol, diagonal=True, mode="kinetic")
+  tr = (f_eff + f_kin).real
+  return np.sum(tr, axis=(1, 2)) if keep_kpts_axis else np.sum(tr)
+
+
+def ewald_coulomb_repulsion(positions, charges, g_vector_grid, vol, ewald_eta,
+                            ewald_grid):
+  """jrystal/_src/ewald.py:21-86, evaluated pair by pair (same sums)."""
+  from scipy.special import erfc
+  positions = np.asarray(positions, dtype=np.float64)
+  charges = np.asarray(charges, dtype=np.float64)
+  na = positions.shape[0]
+  g2 = np.sum(g_vector_grid**2, axis=-1)
+  g2 = g2.copy()
+  g2[0, 0, 0] = 1e16
+  kernel = np.exp(-g2 / 4 / ewald_eta**2) / g2
+  kernel[0, 0, 0] = 0.0
+  ovlp = np.zeros((na, na))
+  rec = np.zeros((na, na))
+  for i in range(na):
+    for j in range(na):
+      tau = positions[j] - positions[i]
+      d = tau[None] - ewald_grid
+      nrm = np.sqrt(np.sum(d**2, axis=-1) + 1e-20)
+      nrm = np.where(nrm <= 1e-9, 1e20, nrm)
+      ovlp[i, j] = np.sum(erfc(ewald_eta * nrm) / nrm)
+      rec[i, j] = np.sum(kernel * np.cos(g_vector_grid @ tau))
+  rec = rec * 4 * np.pi / vol
+  ew_aa = charges @ (ovlp + rec) @ charges / 2
+  ew_a = -np.sum(charges**2) * 2 * ewald_eta / np.sqrt(np.pi) / 2
+  ew_a -= np.sum(charges)**2 * np.pi / ewald_eta**2 / vol / 2
+  return ew_aa + ew_a
+
+
+def nuclear_repulsion(position, charge, cell_vectors, g_vector_grid, vol,
+                      ewald_eta, ewald_cutoff):
+  """jrystal/_src/energy.py:214-243."""
+  tgrid = translation_vectors(cell_vectors, ewald_cutoff)
+  return ewald_coulomb_repulsion(position, charge, g_vector_grid, vol,
+                                 ewald_eta, tgrid)
+
+
+# --------------------------------------------------------------------------
+# energy + hand-derived gradient of the direct-minimisation loss
+# (calc/calc_ground_state_energy_all_electrons.py:119-147, value_and_grad :178)
+# --------------------------------------------------------------------------
+@dataclass
+class System:
+  """Everything the energy path needs besides the parameters."""
+  cell_vectors: np.ndarray
+  positions: np.ndarray
+  charges: np.ndarray
+  grid: tuple
+  mask: np.ndarray
+  kpts: np.ndarray
+  occupation: np.ndarray     # (spin, kpt, band)
+  xc: str = "lda_x+lda_c_vwn"
+
+  @property
+  def vol(self):
+    return abs(np.linalg.det(self.cell_vectors))
+
+  @property
+  def g_vector_grid(self):
+    return g_vectors(self.cell_vectors, self.grid)
+
+
+def energy_terms(w_re, w_im, sysm: System, with_grad=True):
+  """Energy terms of the loss and d loss / d {w_re, w_im}.
+
+  Forward follows total_energy in
+  calc/calc_ground_state_energy_all_electrons.py:119-137.  The gradient is
+  the analytic adjoint: per band g_C = f (T c + sqrt(vol)/N FFT(V psi))|_sphere
+  and through the orthonormalisation g_W = (g_C - C K) R^{-H} with K the
+  Hermitian completion of the upper triangle of C^H g_C; dE/dw_re = 2 Re g_W,
+  dE/dw_im = 2 Im g_W.
+  """
+  vol = sysm.vol
+  gvec = sysm.g_vector_grid
+  mask = sysm.mask
+  occ = sysm.occupation
+  c, r = cholesky_qr(w_re, w_im)                 # (s,k,g,b)
+  dense = expand_coefficient(c, mask)             # (s,k,b,x,y,z)
+  n = np.prod(sysm.grid)
+  wave = np.fft.ifftn(dense, axes=(-3, -2, -1)) * n / np.sqrt(vol)
+  rho = wave_to_density(wave, occ)                # (s,x,y,z)
+  rho_g = np.fft.fftn(rho, axes=(-3, -2, -1))
+  e_kin = kinetic_energy(gvec, sysm.kpts, dense, occ)
+  e_ext = external_energy(rho_g, sysm.positions, sysm.charges, gvec, vol)
+  e_har = hartree_energy(rho_g, gvec, vol, False)
+  e_xc = xc_energy(rho, vol, sysm.xc, False)
+  terms = dict(kinetic=e_kin, external=e_ext, hartree=e_har, xc=e_xc)
+  terms["total"] = e_kin + e_ext + e_har + e_xc
+  if not with_grad:
+    return terms
+  # dE/d rho(r) = (vol/N) V(r)
+  v_g = (hartree_reciprocal(rho_g, gvec, kohn_sham=True) +
+         external_reciprocal(sysm.positions, sysm.charges, gvec, vol))
+  _, v_xc = xc_eps_v(rho[0], sysm.xc)
+  v_r = np.real(np.fft.ifftn(v_g)) + v_xc
+  hpsi = np.fft.fftn(v_r[None, None, None] * wave, axes=(-3, -2, -1))
+  hpsi = hpsi[..., mask] * (np.sqrt(vol) / n)     # (s,k,b,g)
+  tk = kinetic_operator(gvec, sysm.kpts)[:, mask]  # (k,g)
+  g_c = occ[..., None] * (tk[None, :, None, :] * np.swapaxes(c, -1, -2) + hpsi)
+  g_c = np.swapaxes(g_c, -1, -2)                   # (s,k,g,b)
+  a = np.einsum("...gi,...gj->...ij", c.conj(), g_c)
+  up = np.triu(a, 1)
+  kmat = up + np.swapaxes(up.conj(), -1, -2)
+  kmat = kmat + np.einsum("...ii->...i", a).real[..., None] * np.eye(a.shape[-1])
+  rinv_h = np.swapaxes(np.linalg.inv(r).conj(), -1, -2)
+  g_w = (g_c - c @ kmat) @ rinv_h
+  return terms, 2 * g_w.real, 2 * g_w.imag, v_r
+
+
+# --------------------------------------------------------------------------
+# optimiser (optax.adam; calc/opt_utils.py:153-168) and convergence check
+# --------------------------------------------------------------------------
+def adam_update(param, grad, m, v, step, lr, b1=0.9, b2=0.99, eps=1e-8,
+                scale=None):
+  """One Adam step, optax placement of eps (outside the sqrt, after bias
+  correction).  ``step`` is the 1-based count after this update.  ``scale``
+  multiplies the update elementwise (the learned diagonal preconditioner)."""
+  m = b1 * m + (1 - b1) * grad
+  v = b2 * v + (1 - b2) * grad * grad
+  mh = m / (1 - b1**step)
+  vh = v / (1 - b2**step)
+  upd = -lr * mh / (np.sqrt(vh) + eps)
+  if scale is not None:
+    upd = upd * scale
+  return param + upd, m, v
+
+
+class ConvergenceChecker:
+  """calc/convergence.py:13-35."""
+
+  def __init__(self, window_size=20, threshold=1e-5):
+    self.window_size = window_size
+    self.threshold = threshold
+    self.history = []
+
+  def check(self, value):
+    self.history.append(value)
+    if len(self.history) > self.window_size:
+      self.history.pop(0)
+    if len(self.history) < self.window_size:
+      return False
+    return bool(np.std(self.history) < self.threshold)
+
+
+def geometry_path(name):
+  return os.path.join(os.path.dirname(__file__), "..", "tests", "golden",
+                      name)

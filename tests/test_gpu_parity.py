@@ -1,0 +1,139 @@
+"""CUDA path vs the FP64 oracle, called through the C ABI (ctypes)."""
+import numpy as np
+import pytest
+
+from oracle import restatement as R
+from tests.systems import make_system, random_params
+
+pytestmark = pytest.mark.gpu
+
+# Tolerances: the FP64 path must agree with the FP64 oracle to rounding; the
+# FP32 path (FFT/density/potential in FP32, Gram/Cholesky/energy sums in FP64)
+# within 2e-6 relative on each energy term and 1e-4 of the gradient scale.
+TOL = {64: dict(e_rel=1e-10, g_rel=1e-9), 32: dict(e_rel=2e-6, g_rel=1e-4)}
+
+
+def _torch():
+  import torch
+  return torch
+
+
+def _plan(sysm, prec):
+  from jrystal_gb300.engine import PlaneWavePlan
+  return PlaneWavePlan(sysm.cell_vectors, sysm.positions, sysm.charges, sysm.grid, sysm.mask,
+                       sysm.kpts, sysm.occupation.shape[-1], 1, prec, sysm.xc)
+
+
+CASES = [
+  dict(kind="diamond", grid=(12, 12, 12), kgrid=(2, 1, 1), nb=4, nocc=2),
+  dict(kind="si2", grid=(16, 16, 16), kgrid=(2, 2, 2), nb=8, nocc=4),
+  dict(kind="diamond", grid=(14, 15, 16), kgrid=(1, 1, 1), nb=3, nocc=3),
+  dict(kind="si2", grid=(10, 12, 9), kgrid=(1, 2, 1), nb=5, nocc=2, mask="cubic"),
+]
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_energy_and_grad(prec, case):
+  torch = _torch()
+  sysm = make_system(**CASES[case])
+  wr, wi = random_params(sysm, seed=case)
+  terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+  plan = _plan(sysm, prec)
+  dt = torch.float64 if prec == 64 else torch.float32
+  twr = torch.tensor(wr, dtype=dt, device="cuda")
+  twi = torch.tensor(wi, dtype=dt, device="cuda")
+  e, tgr, tgi = plan.energy_and_grad(twr, twi, sysm.occupation)
+  e = e.cpu().numpy()
+  tol = TOL[prec]
+  for i, name in enumerate(["kinetic", "external", "hartree", "xc", "total"]):
+    ref = terms[name]
+    assert abs(e[i] - ref) <= tol["e_rel"] * max(1.0, abs(ref)), (name, e[i], ref)
+  assert e[6] == 0.0
+  scale = max(np.abs(gr).max(), np.abs(gi).max())
+  err = max(np.abs(tgr.cpu().numpy() - gr).max(), np.abs(tgi.cpu().numpy() - gi).max())
+  assert err <= tol["g_rel"] * scale, (err, scale)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_coeff_orthonormal_and_density(prec):
+  torch = _torch()
+  sysm = make_system(**CASES[1])
+  wr, wi = random_params(sysm, seed=7)
+  plan = _plan(sysm, prec)
+  dt = torch.float64 if prec == 64 else torch.float32
+  c = plan.coeff(torch.tensor(wr, dtype=dt, device="cuda"), torch.tensor(wi, dtype=dt, device="cuda"))
+  cn = c.cpu().numpy().astype(np.complex128)
+  ovl = np.einsum("skgi,skgj->skij", cn.conj(), cn)
+  eye = np.eye(cn.shape[-1])
+  assert np.abs(ovl - eye).max() < (1e-12 if prec == 64 else 2e-6)
+  # same column space and phase-equal columns as Householder QR
+  q = R.unitary_householder(wr, wi)
+  ph = np.einsum("skgb,skgb->skb", q.conj(), cn)
+  assert np.abs(np.abs(ph) - 1).max() < (1e-10 if prec == 64 else 1e-5)
+  rho = plan.density(c, sysm.occupation).cpu().numpy()
+  dense = R.expand_coefficient(cn, sysm.mask)
+  rref = R.density_grid(dense, sysm.vol, sysm.occupation)
+  assert np.abs(rho - rref).max() <= (1e-12 if prec == 64 else 1e-6) * np.abs(rref).max()
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("grid", [(12, 12, 12), (7, 10, 12), (16, 9, 20), (24, 27, 32)])
+def test_fft3d(prec, grid):
+  torch = _torch()
+  from jrystal_gb300.engine import fft3d
+  rng = np.random.default_rng(3)
+  x = rng.normal(size=(2,) + grid) + 1j * rng.normal(size=(2,) + grid)
+  dt = torch.complex128 if prec == 64 else torch.complex64
+  tx = torch.tensor(x, dtype=dt, device="cuda")
+  f = fft3d(tx).cpu().numpy()
+  fi = fft3d(tx, inverse=True).cpu().numpy()
+  rf = np.fft.fftn(x, axes=(-3, -2, -1))
+  ri = np.fft.ifftn(x, axes=(-3, -2, -1))
+  tol = 1e-12 if prec == 64 else 2e-6
+  assert np.abs(f - rf).max() <= tol * np.abs(rf).max()
+  assert np.abs(fi - ri).max() <= tol * np.abs(ri).max()
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_potential_split(prec):
+  torch = _torch()
+  sysm = make_system(**CASES[0])
+  wr, wi = random_params(sysm, seed=11)
+  dense = R.coeff(wr, wi, sysm.mask)
+  rho = R.density_grid(dense, sysm.vol, sysm.occupation)
+  plan = _plan(sysm, prec)
+  for ks in (False, True):
+    vh, ve, vx = R.effective(rho, sysm.positions, sysm.charges, sysm.g_vector_grid, sysm.vol,
+                             split=True, xc_type=sysm.xc, kohn_sham=ks)
+    out = plan.potential(torch.tensor(rho, device="cuda"), kohn_sham=ks).cpu().numpy()
+    tol = 1e-11 if prec == 64 else 2e-5
+    for got, ref in ((out[0], vh.real), (out[1], ve.real), (out[2], np.reshape(vx, out[2].shape))):
+      assert np.abs(got - ref).max() <= tol * max(1.0, np.abs(ref).max())
+
+
+def test_ewald_matches_oracle():
+  sysm = make_system(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 1), nb=2, nocc=1)
+  plan = _plan(sysm, 64)
+  got = plan.ewald(0.1, 2e3)
+  tgrid = R.translation_vectors(sysm.cell_vectors, 2e3)
+  ref = R.ewald_coulomb_repulsion(sysm.positions, sysm.charges, sysm.g_vector_grid, sysm.vol, 0.1,
+                                  tgrid)
+  assert abs(got - ref) <= 1e-10 * abs(ref)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_adam_matches_oracle(prec):
+  torch = _torch()
+  from jrystal_gb300.engine import adam_update
+  rng = np.random.default_rng(5)
+  p, g = rng.normal(size=1000), rng.normal(size=1000)
+  m, v = np.zeros(1000), np.zeros(1000)
+  dt = torch.float64 if prec == 64 else torch.float32
+  tp, tm, tv = (torch.tensor(a, dtype=dt, device="cuda") for a in (p, m, v))
+  for step in (1, 2, 3):
+    tg = torch.tensor(g * step, dtype=dt, device="cuda")
+    adam_update(tp, tg, tm, tv, step, 1e-2)
+    p, m, v = R.adam_update(p, g * step, m, v, step, 1e-2)
+  tol = 1e-14 if prec == 64 else 1e-6
+  assert np.abs(tp.cpu().numpy() - p).max() < tol * 10
