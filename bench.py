@@ -1,0 +1,332 @@
+#!/usr/bin/env python
+"""Energy+gradient evaluations/s of the direct-minimisation step on one GB300.
+
+A step is one optimiser iteration of jrystal's ground-state loop
+(calc/calc_ground_state_energy_all_electrons.py:175-181): orthonormalise the
+parameters, energy and hand-written gradient, and the Adam update of all
+parameters.  The default workload is the all-electron Si 8-atom cubic cell
+(a = 10.26 bohr, LDA, 64^3 grid, 17071 plane waves, 3x3x3 k-grid, 24 bands of
+which 16 doubly occupied, complex64 parameters drawn N(0,1) from seed 1).
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
+same path on the host cores instead (the reference arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+  sys.path.insert(0, ROOT)
+
+METRIC = "energy+grad evals/s (direct-minimisation step incl. Adam)"
+UNIT = "evals/s"
+
+
+def _args():
+  p = argparse.ArgumentParser()
+  p.add_argument("--gpus", type=int, default=1)
+  p.add_argument("--steps", type=int, default=20)
+  p.add_argument("--warmup", type=int, default=3)
+  p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+  p.add_argument("--workload", default="si8_cubic_64")
+  p.add_argument("--no-cpu-baseline", action="store_true")
+  p.add_argument("--cpu-sample-kpts", type=int, default=1)
+  return p.parse_args()
+
+
+def _dist():
+  ws = int(os.environ.get("WORLD_SIZE", "1"))
+  rank = int(os.environ.get("RANK", "0"))
+  local = int(os.environ.get("LOCAL_RANK", "0"))
+  return ws, rank, local
+
+
+def _peaks():
+  path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+  try:
+    with open(path) as f:
+      d = json.load(f)
+    return float(d["hbm_gbs"]), "measured"
+  except Exception:
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+  """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+  Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+       "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+       "clocks_event_reasons.sw_power_cap")
+
+  def __init__(self, index):
+    self.index = index
+    self.proc = None
+    self.lines = []
+
+  def __enter__(self):
+    try:
+      self.proc = subprocess.Popen(
+        ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+         "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+      self.t = threading.Thread(target=self._read, daemon=True)
+      self.t.start()
+    except Exception:
+      self.proc = None
+    return self
+
+  def _read(self):
+    for ln in self.proc.stdout:
+      self.lines.append(ln.strip())
+
+  def __exit__(self, *a):
+    if self.proc:
+      self.proc.terminate()
+      try:
+        self.proc.wait(timeout=5)
+      except Exception:
+        self.proc.kill()
+
+  def summary(self):
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in self.lines:
+      parts = [p.strip() for p in ln.split(",")]
+      if len(parts) < 7:
+        continue
+      try:
+        sm.append(float(parts[0]))
+        mx.append(float(parts[1]))
+      except ValueError:
+        continue
+      for n, v in zip(names, parts[3:7]):
+        if v.lower() in ("active", "1", "yes"):
+          reasons.add(n)
+    if not sm:
+      return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def cpu_sample(wl, nk_sample, workers, repeats=1):
+  """Seconds per full evaluation of the FP64 CPU restatement, estimated from
+  a sample of nk_sample k-points (all bands, full grid), scaled by K."""
+  from oracle import restatement as R
+  R.FFT_WORKERS = workers
+  occ = wl.occupation[:, :nk_sample]
+  sysm = R.System(wl.cell, wl.positions, wl.charges, wl.grid_sizes, wl.mask,
+                  wl.kpts[:nk_sample], occ, wl.xc)
+  wr, wi = wl.init_params()
+  wr = wr[:, :nk_sample].astype(np.float64)
+  wi = wi[:, :nk_sample].astype(np.float64)
+  m = np.zeros_like(wr)
+  v = np.zeros_like(wr)
+  times = []
+  for it in range(repeats):
+    t0 = time.perf_counter()
+    _, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+    R.adam_update(wr, gr, m, v, it + 1, wl.lr)
+    R.adam_update(wi, gi, m, v, it + 1, wl.lr)
+    times.append(time.perf_counter() - t0)
+  t = min(times)
+  return t * wl.num_kpt / nk_sample, t
+
+
+def run_reference(args, wl):
+  ws, rank, _ = _dist()
+  if rank != 0:
+    return
+  workers = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+  nks = max(1, min(args.cpu_sample_kpts, wl.num_kpt))
+  for _ in range(args.warmup):
+    cpu_sample(wl, nks, workers)
+  per_eval = []
+  for _ in range(args.steps):
+    per_eval.append(cpu_sample(wl, nks, workers)[0])
+  t = statistics.median(per_eval)
+  val = 1.0 / t
+  sample = (f"FP64 NumPy/SciPy restatement of the path (not jrystal: jax is absent), "
+            f"{nks} of {wl.num_kpt} k-points per step (all {wl.num_band} bands, full "
+            f"{wl.grid_sizes[0]}^3 grid), time scaled by {wl.num_kpt}/{nks}")
+  out = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+         "data": "synthetic", "config": _config(wl, args.gpus),
+         "cpu_baseline": {"value": val, "unit": UNIT, "cores": workers, "kind": "port",
+                          "sample": sample},
+         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+  print(json.dumps(out))
+
+
+def _config(wl, n):
+  return {"workload": wl.name, "cell": "all-electron Si", "grid": list(wl.grid_sizes),
+          "num_g": int(wl.mask.sum()), "kpts": wl.num_kpt, "bands": wl.num_band,
+          "occupied": wl.num_occ, "xc": wl.xc, "precision": f"fp{wl.precision}",
+          "parallelism": f"replicas{n}" if n > 1 else "single-gpu",
+          "l2": "no explicit flush: each step streams >0.7 GB of plane buffers, >5x the 129 MB L2"}
+
+
+# algorithmic bytes per call of each phase of jrg_energy_grad
+def phase_bytes(plan):
+  c = 8 if plan.precision == 32 else 16
+  r = c // 2
+  nbt = plan.num_spin * plan.num_kpt * plan.num_band
+  nsk = plan.num_spin * plan.num_kpt
+  nx, ny, nz = plan.grid
+  ngrid = nx * ny * nz
+  nact = int(np.unique(np.flatnonzero(plan.mask.reshape(-1)) // (ny * nz)).size)
+  planes = nact * ny * nz * c
+  sph = plan.num_g * c
+  return {
+    "pack_params": 2 * nbt * sph,
+    "gram": nbt * sph,
+    "rotate": 2 * nbt * sph,
+    "kinetic": nbt * sph + plan.num_kpt * plan.num_g * 8,
+    "plane_inv_sphere": nbt * (sph + planes),
+    "line_density": nbt * planes + nsk * ngrid * r,
+    "reduce_density": nsk * ngrid * r + ngrid * r,
+    "line_apply_v": nbt * 2 * planes + nsk * ngrid * r,
+    "plane_fwd_sphere": nbt * (planes + 2 * sph) + plan.num_kpt * plan.num_g * 8,
+    "adj_gram": 2 * nbt * sph,
+    "adj_rotate": 2 * nbt * sph + nbt * sph,
+  }
+
+
+def run_ours(args, wl):
+  import torch
+  import torch.distributed as dist
+  from jrystal_gb300 import _lib
+  from jrystal_gb300.engine import PlaneWavePlan, adam_update
+
+  ws, rank, local = _dist()
+  if ws > 1:
+    dist.init_process_group("nccl")
+  torch.cuda.set_device(local)
+  dev = torch.device("cuda", local)
+  lib = _lib.load()
+  plan = PlaneWavePlan(wl.cell, wl.positions, wl.charges, wl.grid_sizes, wl.mask, wl.kpts,
+                       wl.num_band, 1, wl.precision, wl.xc, device=dev)
+  wr, wi = wl.init_params()
+  rdt = plan.rdtype
+  params = torch.tensor(np.stack([wr, wi]), dtype=rdt, device=dev).contiguous()
+  grads = torch.empty_like(params)
+  m = torch.zeros_like(params)
+  v = torch.zeros_like(params)
+  occ = torch.tensor(wl.occupation, dtype=torch.float64, device=dev)
+  state = {"t": 0}
+
+  def step(p):
+    e, _, _ = plan.energy_and_grad(p[0], p[1], occ, grads[0], grads[1])
+    state["t"] += 1
+    adam_update(p, grads, m, v, state["t"], wl.lr)
+    return e
+
+  def barrier():
+    if ws > 1:
+      dist.barrier()
+    torch.cuda.synchronize()
+
+  for _ in range(args.warmup):
+    step(params)
+  barrier()
+  lib.jrg_profile_enable(plan._h, args.steps)
+  launches0 = lib.jrg_launch_count()
+  stream = torch.cuda.current_stream()
+  t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  with ClockSampler(local) as clk:
+    barrier()
+    t0.record(stream)
+    for _ in range(args.steps):
+      e = step(params)
+    t1.record(stream)
+    barrier()
+  launches = lib.jrg_launch_count() - launches0
+  ms = t0.elapsed_time(t1) / args.steps
+  nph = lib.jrg_profile_num_phases()
+  import ctypes as ct
+  arr = (ct.c_double * nph)()
+  ncalls = ct.c_int()
+  _lib.check(lib.jrg_profile_read(plan._h, arr, ct.byref(ncalls), nph), "jrg_profile_read")
+  lib.jrg_profile_enable(plan._h, 0)
+  phases = {lib.jrg_profile_phase_name(i).decode(): arr[i] / max(1, ncalls.value) for i in range(nph)}
+  if ws > 1:
+    tt = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    ms = float(tt.item())
+  energies = e.cpu().numpy().tolist()
+
+  # end to end through the public API with host buffers: H2D of the step's
+  # parameters from pinned memory, energy+grad+Adam, D2H of the energies
+  host_params = params.cpu().pin_memory()
+  host_e = torch.empty(8, dtype=torch.float64).pin_memory()
+  for _ in range(max(1, args.warmup)):
+    params.copy_(host_params, non_blocking=True)
+    e = step(params)
+    host_e.copy_(e, non_blocking=True)
+  barrier()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record(stream)
+  for _ in range(args.steps):
+    params.copy_(host_params, non_blocking=True)
+    e = step(params)
+    host_e.copy_(e, non_blocking=True)
+  e1.record(stream)
+  barrier()
+  e2e_ms = e0.elapsed_time(e1) / args.steps
+  if ws > 1:
+    tt = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    e2e_ms = float(tt.item())
+
+  if rank == 0:
+    peak, peak_kind = _peaks()
+    pb = phase_bytes(plan)
+    top = max((k for k in phases if k in pb), key=lambda k: phases[k])
+    achieved = pb[top] / (phases[top] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "algorithmic_bytes": pb[top], "ms_per_launch": phases[top],
+            "phase_ms": {k: round(v, 4) for k, v in phases.items()}}
+    out = {"metric": METRIC, "value": 1000.0 / ms * ws, "unit": UNIT, "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32" if wl.precision == 32 else "f64", "data": "synthetic",
+           "config": _config(wl, ws), "clocks": clk.summary(),
+           "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": UNIT,
+                   "h2d_bytes_per_step": int(params.numel() * params.element_size()),
+                   "d2h_bytes_per_step": 64},
+           "gpu_launches": int(launches), "roofline": roof,
+           "energies_last_step": energies[:5]}
+    if not args.no_cpu_baseline:
+      workers = len(os.sched_getaffinity(0))
+      nks = max(1, min(args.cpu_sample_kpts, wl.num_kpt))
+      per_eval, t_sample = cpu_sample(wl, nks, workers)
+      out["cpu_baseline"] = {
+        "value": 1.0 / per_eval, "unit": UNIT, "cores": workers, "kind": "port",
+        "sample": f"FP64 CPU restatement, {nks}/{wl.num_kpt} k-points ({t_sample:.2f} s), "
+                  f"scaled by {wl.num_kpt}/{nks}"}
+    print(json.dumps(out))
+  if ws > 1:
+    dist.destroy_process_group()
+
+
+def main():
+  args = _args()
+  from jrystal_gb300 import workloads
+  wl = workloads.WORKLOADS[args.workload]()
+  if args.impl == "reference":
+    run_reference(args, wl)
+  else:
+    run_ours(args, wl)
+
+
+if __name__ == "__main__":
+  main()

@@ -71,9 +71,11 @@ typedef struct {
   int xc;                   /* JRG_XC_* flags */
 } jrg_plan_desc;
 
-/* Library version and the last error message of the calling thread. */
+/* Library version, the last error message of the calling thread, and the
+ * number of kernels this library has launched in the process so far. */
 int jrg_version(void);
 const char* jrg_last_error(void);
+long long jrg_launch_count(void);
 
 /* Plans: geometry tables (sphere maps, twiddles, kinetic and external
  * potential tables) on the current device.  Creating a plan allocates its
@@ -131,6 +133,16 @@ int jrg_adam_update(int precision, int64_t n, void* param, const void* grad, voi
  * the plan's FFT G grid.  result: device double[1]. */
 int jrg_ewald(const jrg_plan* plan, double eta, double cutoff, double* result,
               void* workspace, cudaStream_t stream);
+
+/* Per-phase CUDA-event timing of jrg_energy_grad (no reference counterpart;
+ * the reference only times whole steps, calc driver :207-211).  enable
+ * creates events for up to max_calls calls (0 disables); read synchronises
+ * on the recorded events and returns, per phase, the summed milliseconds and
+ * the number of recorded calls; phase_name gives a phase's name. */
+int jrg_profile_enable(jrg_plan* plan, int max_calls);
+int jrg_profile_read(jrg_plan* plan, double* ms, int* calls, int num_phases);
+const char* jrg_profile_phase_name(int phase);
+int jrg_profile_num_phases(void);
 
 #ifdef __cplusplus
 }

@@ -26,6 +26,7 @@ _vp = ct.c_void_p
 _SIGS = {
   "jrg_version": ([], ct.c_int),
   "jrg_last_error": ([], ct.c_char_p),
+  "jrg_launch_count": ([], ct.c_longlong),
   "jrg_plan_create": ([_vp, ct.POINTER(_vp)], ct.c_int),
   "jrg_plan_destroy": ([_vp], ct.c_int),
   "jrg_workspace_size": ([_vp, ct.POINTER(ct.c_size_t)], ct.c_int),
@@ -40,6 +41,10 @@ _SIGS = {
   "jrg_adam_update": ([ct.c_int, ct.c_int64, _vp, _vp, _vp, _vp, _vp, ct.c_int,
                        ct.c_double, ct.c_double, ct.c_double, ct.c_double, _vp], ct.c_int),
   "jrg_ewald": ([_vp, ct.c_double, ct.c_double, _vp, _vp, _vp], ct.c_int),
+  "jrg_profile_enable": ([_vp, ct.c_int], ct.c_int),
+  "jrg_profile_read": ([_vp, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int), ct.c_int], ct.c_int),
+  "jrg_profile_phase_name": ([ct.c_int], ct.c_char_p),
+  "jrg_profile_num_phases": ([], ct.c_int),
 }
 
 

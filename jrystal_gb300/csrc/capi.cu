@@ -1,6 +1,7 @@
 // C ABI of the library: plan construction, workspace layout and the entry
 // points declared in include/jrystal_gb300.h.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -36,6 +37,8 @@ template <typename R> int launch_adam(void*, const void*, void*, void*, const fl
 int launch_twiddles(int n, int prec, void* out, cudaStream_t st);
 
 static thread_local std::string g_err;
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void set_error(const std::string& m) { g_err = m; }
 int fail(int code, const std::string& m) { g_err = m; return code; }
 int cuda_fail(cudaError_t e, const char* what) {
@@ -108,6 +111,7 @@ using namespace jrg;
 extern "C" {
 
 int jrg_version(void) { return 1; }
+long long jrg_launch_count(void) { return g_launches.load(); }
 const char* jrg_last_error(void) { return g_err.c_str(); }
 
 int jrg_plan_destroy(jrg_plan* P) {
@@ -119,6 +123,10 @@ int jrg_plan_destroy(jrg_plan* P) {
   if (P->slot_begin) cudaFree(P->slot_begin);
   if (P->d_cell) cudaFree(P->d_cell);
   if (P->d_atoms) cudaFree(P->d_atoms);
+  if (P->prof) {
+    for (cudaEvent_t e : P->prof->ev) cudaEventDestroy(e);
+    delete P->prof;
+  }
   delete P;
   return JRG_OK;
 }
@@ -323,19 +331,52 @@ namespace jrg {
 
 static inline char* wsp(void* ws, size_t off) { return reinterpret_cast<char*>(ws) + off; }
 
+// phase timing: events of call `calls` (the call in progress)
+struct PhaseScope {
+  const jrg_plan* P;
+  int ph;
+  cudaStream_t st;
+  PhaseScope(const jrg_plan* p, int phase, cudaStream_t s) : P(p), ph(phase), st(s) {
+    Profiler* pr = P->prof;
+    if (pr && pr->calls < pr->max_calls) {
+      cudaEventRecord(pr->ev[((size_t)pr->calls * PH_COUNT + ph) * 2], st);
+      pr->used[(size_t)pr->calls * PH_COUNT + ph] = 1;
+    }
+  }
+  ~PhaseScope() {
+    Profiler* pr = P->prof;
+    if (pr && pr->calls < pr->max_calls)
+      cudaEventRecord(pr->ev[((size_t)pr->calls * PH_COUNT + ph) * 2 + 1], st);
+  }
+};
+#define PHASE(ph) PhaseScope phase_scope_##ph(P, ph, st)
+static void profile_call_done(const jrg_plan* P) {
+  if (P->prof && P->prof->calls < P->prof->max_calls) P->prof->calls++;
+}
+
 template <typename R>
 static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im, void* ws,
                           cudaStream_t st) {
   const Workspace& w = P->ws;
   const int nsk = P->ns * P->nk;
   int rc;
-  if ((rc = launch_pack_params<R>(w_re, w_im, wsp(ws, w.wc), nsk, P->ng, P->nb, false, st))) return rc;
-  if ((rc = launch_gram<R>(wsp(ws, w.wc), wsp(ws, w.wc), (double2*)wsp(ws, w.gram_part),
-                           (double2*)wsp(ws, w.gram), nsk, P->ng, P->nb, w.gram_splits, st)))
-    return rc;
-  if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram), (double2*)wsp(ws, w.rmat),
-                                (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags), st)))
-    return rc;
+  {
+    PHASE(PH_PACK);
+    if ((rc = launch_pack_params<R>(w_re, w_im, wsp(ws, w.wc), nsk, P->ng, P->nb, false, st))) return rc;
+  }
+  {
+    PHASE(PH_GRAM);
+    if ((rc = launch_gram<R>(wsp(ws, w.wc), wsp(ws, w.wc), (double2*)wsp(ws, w.gram_part),
+                             (double2*)wsp(ws, w.gram), nsk, P->ng, P->nb, w.gram_splits, st)))
+      return rc;
+  }
+  {
+    PHASE(PH_CHOL);
+    if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram), (double2*)wsp(ws, w.rmat),
+                                  (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags), st)))
+      return rc;
+  }
+  PHASE(PH_ROTATE);
   return launch_rotate<R>(0, wsp(ws, w.wc), (double2*)wsp(ws, w.rinv), nullptr, nullptr,
                           wsp(ws, w.c), nullptr, nsk, P->ng, P->nb, 1.0, st);
 }
@@ -347,16 +388,23 @@ static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* 
   const Workspace& w = P->ws;
   const int nbt = P->ns * P->nk * P->nb;
   int rc;
-  if ((rc = launch_plane_inv_sphere<R>(P, wsp(ws, w.c), wsp(ws, w.t), nbt, st))) return rc;
-  if ((rc = launch_line_density<R>(P, wsp(ws, w.t), wsp(ws, w.rho_part), occ, 1.0 / P->vol, 0, nbt,
-                                   P->nb, st)))
-    return rc;
+  {
+    PHASE(PH_PLANE_INV);
+    if ((rc = launch_plane_inv_sphere<R>(P, wsp(ws, w.c), wsp(ws, w.t), nbt, st))) return rc;
+  }
+  {
+    PHASE(PH_LINE_DENSITY);
+    if ((rc = launch_line_density<R>(P, wsp(ws, w.t), wsp(ws, w.rho_part), occ, 1.0 / P->vol, 0,
+                                     nbt, P->nb, st)))
+      return rc;
+  }
+  PHASE(PH_REDUCE_DENSITY);
   return launch_reduce_density<R>(wsp(ws, w.rho_part), rho_out, P->nk, P->ns, P->ngrid, st);
 }
 
 template <typename R>
-static int energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
-                       double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
+static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
+                            double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
   using C = C_t<R>;
   const Workspace& w = P->ws;
   const int nsk = P->ns * P->nk;
@@ -366,41 +414,72 @@ static int energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, co
   JRG_CUDA(cudaMemsetAsync(wsp(ws, w.flags), 0, 64, st));
   if ((rc = orthonormalise<R>(P, w_re, w_im, ws, st))) return rc;
   double* slots = (double*)wsp(ws, w.epart);
-  if ((rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, occ, slots, nbt, P->ng, P->nb, P->nk, st))) return rc;
+  {
+    PHASE(PH_KINETIC);
+    if ((rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, occ, slots, nbt, P->ng, P->nb, P->nk, st)))
+      return rc;
+  }
   void* rho = wsp(ws, w.rho);
   if ((rc = density_from_c<R>(P, occ, ws, rho, st))) return rc;
-  C* rhog = (C*)wsp(ws, w.rhog);
-  C* scratch = (C*)wsp(ws, w.fft_scratch);
-  const C* tw = (const C*)P->d.tw;
-  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
-  // Hartree / external (slots after the kinetic ones) and dE/drho in G space (in place)
-  const double pref = P->vol / (N * N);
-  if ((rc = launch_recip_terms<R>(rhog, P->d.ginv, P->d.vext, rhog, slots + nbt + kRecipBlocks,
-                                  slots + nbt, kRecipBlocks, P->ngrid, pref, st)))
-    return rc;
-  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st))) return rc;
-  if ((rc = launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks,
-                                kXcBlocks, P->ngrid, P->xc, P->vol / N, st)))
-    return rc;
-  if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st))) return rc;
+  {
+    PHASE(PH_GRID_TERMS);
+    C* rhog = (C*)wsp(ws, w.rhog);
+    C* scratch = (C*)wsp(ws, w.fft_scratch);
+    const C* tw = (const C*)P->d.tw;
+    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+    // Hartree / external (slots after the kinetic ones) and dE/drho in G space (in place)
+    const double pref = P->vol / (N * N);
+    if ((rc = launch_recip_terms<R>(rhog, P->d.ginv, P->d.vext, rhog, slots + nbt + kRecipBlocks,
+                                    slots + nbt, kRecipBlocks, P->ngrid, pref, st)))
+      return rc;
+    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st)))
+      return rc;
+    if ((rc = launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks,
+                                  kXcBlocks, P->ngrid, P->xc, P->vol / N, st)))
+      return rc;
+    if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st)))
+      return rc;
+  }
   if (!g_re && !g_im) return JRG_OK;
   if (!g_re || !g_im) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
   // adjoint: planes -> x lines (x V) -> planes -> sphere gradient
-  if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), wsp(ws, w.vr), nbt, P->nb, st))) return rc;
-  if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), wsp(ws, w.c), wsp(ws, w.gc), occ, 0, nbt,
-                                       1.0 / N, st)))
-    return rc;
+  {
+    PHASE(PH_LINE_APPLY_V);
+    if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), wsp(ws, w.vr), nbt, P->nb, st)))
+      return rc;
+  }
+  {
+    PHASE(PH_PLANE_FWD);
+    if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), wsp(ws, w.c), wsp(ws, w.gc), occ, 0, nbt,
+                                         1.0 / N, st)))
+      return rc;
+  }
   // orthonormalisation adjoint
-  if ((rc = launch_gram<R>(wsp(ws, w.c), wsp(ws, w.gc), (double2*)wsp(ws, w.adj_part),
-                           (double2*)wsp(ws, w.adj), nsk, P->ng, P->nb, w.gram_splits, st)))
-    return rc;
+  {
+    PHASE(PH_ADJ_GRAM);
+    if ((rc = launch_gram<R>(wsp(ws, w.c), wsp(ws, w.gc), (double2*)wsp(ws, w.adj_part),
+                             (double2*)wsp(ws, w.adj), nsk, P->ng, P->nb, w.gram_splits, st)))
+      return rc;
+  }
   double2* rh = (double2*)wsp(ws, w.kmat);
   double2* negm2 = rh + (size_t)nsk * P->nb * P->nb;
-  if ((rc = launch_adjoint_small((double2*)wsp(ws, w.adj), (double2*)wsp(ws, w.rinv), rh, negm2, nsk,
-                                 P->nb, st)))
-    return rc;
+  {
+    PHASE(PH_ADJ_SMALL);
+    if ((rc = launch_adjoint_small((double2*)wsp(ws, w.adj), (double2*)wsp(ws, w.rinv), rh, negm2,
+                                   nsk, P->nb, st)))
+      return rc;
+  }
+  PHASE(PH_ADJ_ROTATE);
   return launch_rotate<R>(2, wsp(ws, w.gc), rh, wsp(ws, w.c), negm2, g_re, g_im, nsk, P->ng, P->nb,
                           2.0, st);
+}
+
+template <typename R>
+static int energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
+                       double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
+  const int rc = energy_grad_impl<R>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st);
+  profile_call_done(P);
+  return rc;
 }
 
 template <typename R>
@@ -551,6 +630,66 @@ int jrg_ewald(const jrg_plan* P, double eta, double cutoff, double* result, void
   const int na = (int)P->charge.size();
   return launch_ewald(P->d_cell, P->d.gvec, P->d_atoms, P->d_atoms + 3 * na, na, nt, P->ngrid, eta,
                       P->vol, (double*)wsp(ws, P->ws.epart), kEwaldBlocks, result, st);
+}
+
+}  // extern "C"
+
+namespace {
+const char* kPhaseNames[jrg::PH_COUNT] = {
+  "pack_params", "gram", "cholesky_inv", "rotate", "kinetic", "plane_inv_sphere", "line_density",
+  "reduce_density", "grid_terms", "line_apply_v", "plane_fwd_sphere", "adj_gram", "adj_small",
+  "adj_rotate"};
+}
+
+extern "C" {
+
+int jrg_profile_num_phases(void) { return jrg::PH_COUNT; }
+
+const char* jrg_profile_phase_name(int ph) {
+  return (ph >= 0 && ph < jrg::PH_COUNT) ? kPhaseNames[ph] : "";
+}
+
+int jrg_profile_enable(jrg_plan* P, int max_calls) {
+  if (!P || max_calls < 0) return fail(JRG_ERR_INVALID, "jrg_profile_enable: bad argument");
+  if (P->prof) {
+    for (cudaEvent_t e : P->prof->ev) cudaEventDestroy(e);
+    delete P->prof;
+    P->prof = nullptr;
+  }
+  if (max_calls == 0) return JRG_OK;
+  Profiler* pr = new Profiler();
+  pr->max_calls = max_calls;
+  pr->ev.resize((size_t)max_calls * PH_COUNT * 2);
+  pr->used.assign((size_t)max_calls * PH_COUNT, 0);
+  for (auto& e : pr->ev) {
+    cudaError_t ce = cudaEventCreate(&e);
+    if (ce != cudaSuccess) {
+      delete pr;
+      return cuda_fail(ce, "cudaEventCreate");
+    }
+  }
+  P->prof = pr;
+  return JRG_OK;
+}
+
+int jrg_profile_read(jrg_plan* P, double* ms, int* calls, int n) {
+  if (!P || !ms || n < 1) return fail(JRG_ERR_INVALID, "jrg_profile_read: bad argument");
+  for (int i = 0; i < n; ++i) ms[i] = 0.0;
+  if (calls) *calls = 0;
+  Profiler* pr = P->prof;
+  if (!pr) return JRG_OK;
+  for (int c = 0; c < pr->calls; ++c) {
+    for (int ph = 0; ph < PH_COUNT && ph < n; ++ph) {
+      if (!pr->used[(size_t)c * PH_COUNT + ph]) continue;
+      cudaEvent_t a = pr->ev[((size_t)c * PH_COUNT + ph) * 2], b = pr->ev[((size_t)c * PH_COUNT + ph) * 2 + 1];
+      JRG_CUDA(cudaEventSynchronize(b));
+      float t = 0.f;
+      JRG_CUDA(cudaEventElapsedTime(&t, a, b));
+      ms[ph] += t;
+    }
+  }
+  if (calls) *calls = pr->calls;
+  return JRG_OK;
 }
 
 }  // extern "C"

@@ -18,8 +18,11 @@ int cuda_fail(cudaError_t e, const char* what);
     if (e_ != cudaSuccess) return ::jrg::cuda_fail(e_, #call); \
   } while (0)
 
+void count_launch();
+
 #define JRG_LAUNCH_CHECK(what)                           \
   do {                                                   \
+    ::jrg::count_launch();                               \
     cudaError_t e_ = cudaGetLastError();                 \
     if (e_ != cudaSuccess) return ::jrg::cuda_fail(e_, what); \
   } while (0)
@@ -40,6 +43,19 @@ struct PlanTables {
   void* vext = nullptr;       // [ngrid] complex V_ext(G) in precision R
   double* ginv = nullptr;     // [ngrid] 4 pi / |G|^2, 0 at G = 0
   double* gvec = nullptr;     // [ngrid][3] cartesian G vectors
+};
+
+// Per-phase CUDA-event timing of the fused entry points (optional).
+enum Phase {
+  PH_PACK = 0, PH_GRAM, PH_CHOL, PH_ROTATE, PH_KINETIC, PH_PLANE_INV, PH_LINE_DENSITY,
+  PH_REDUCE_DENSITY, PH_GRID_TERMS, PH_LINE_APPLY_V, PH_PLANE_FWD, PH_ADJ_GRAM, PH_ADJ_SMALL,
+  PH_ADJ_ROTATE, PH_COUNT
+};
+struct Profiler {
+  int max_calls = 0;
+  int calls = 0;                         // calls recorded so far
+  std::vector<cudaEvent_t> ev;           // [max_calls][PH_COUNT][2]
+  std::vector<unsigned char> used;       // [max_calls][PH_COUNT]
 };
 
 // Workspace offsets (bytes) of one plan.
@@ -70,4 +86,5 @@ struct jrg_plan {
   int* slot_begin = nullptr;  // energy slot boundaries [5]
   double* d_cell = nullptr;   // cell (9) then reciprocal vectors (9)
   double* d_atoms = nullptr;  // positions [natom][3] then charges [natom]
+  jrg::Profiler* prof = nullptr;
 };
