@@ -121,6 +121,19 @@ int jrg_fft3d_workspace_size(int precision, const int grid[3], int batch, size_t
 int jrg_fft3d(int precision, const int grid[3], int batch, int direction, const void* in,
               void* out, void* workspace, cudaStream_t stream);
 
+/* jrg_fft3d without a workspace, for callers that cannot allocate device
+ * memory (a runtime that owns the device memory, a fixed memory budget, or a
+ * path that must avoid cudaMalloc's implicit synchronisation).  No
+ * counterpart in the reference.  Scratch is a fixed 16 MiB device array
+ * inside the library, held on every GPU that loads it until exit: the
+ * twiddle tables (256-byte rounded) plus batch*nx*ny*nz complex elements
+ * must fit, else JRG_ERR_INVALID.  All calls share that array, so calls that
+ * overlap on the GPU race; nothing in it needs to start at zero.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress) and
+ * should come before any stream capture. */
+int jrg_fft3d_noalloc(int precision, const int grid[3], int batch, int direction,
+                      const void* in, void* out, cudaStream_t stream);
+
 /* One Adam step over n elements (optax.adam: eps outside the sqrt after bias
  * correction).  step is the 1-based count after this update.  scale, when not
  * NULL, multiplies each update element (learned preconditioner). */
