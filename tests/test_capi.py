@@ -1,0 +1,54 @@
+"""The C-ABI library loads without a GPU and exports every entry point that
+include/jrystal_gb300.h declares (no compute calls here)."""
+import ctypes as ct
+import os
+import re
+
+import pytest
+
+from jrystal_gb300 import _lib, build
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                      "jrystal_gb300.h")
+
+
+def declared_symbols():
+  src = open(HEADER).read()
+  src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+  return sorted(set(re.findall(r"\b(jrg_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+  names = declared_symbols()
+  for must in ("jrg_plan_create", "jrg_energy_grad", "jrg_coeff", "jrg_density", "jrg_fft3d",
+               "jrg_adam_update", "jrg_ewald", "jrg_potential"):
+    assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+  lib = _lib.load()
+  missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+  assert not missing, missing
+  # and the Python binding covers them
+  assert set(declared_symbols()) <= set(_lib.exported_symbols())
+
+
+def test_version_and_error_string_without_gpu():
+  lib = _lib.load()
+  assert lib.jrg_version() >= 1
+  assert isinstance(lib.jrg_last_error(), bytes)
+  assert lib.jrg_profile_num_phases() > 5
+
+
+def test_invalid_arguments_are_rejected_on_the_host():
+  lib = _lib.load()
+  out = ct.c_void_p()
+  assert lib.jrg_plan_create(None, ct.byref(out)) == _lib.JRG_ERR_INVALID
+  assert b"null" in lib.jrg_last_error()
+  assert lib.jrg_adam_update(16, 10, None, None, None, None, None, 1, 1e-2, 0.9, 0.99, 1e-8,
+                             None) == _lib.JRG_ERR_INVALID
+
+
+def test_build_recipe_targets_sm_103a():
+  assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
+  assert os.path.exists(build.LIB)
