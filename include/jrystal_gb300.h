@@ -147,6 +147,13 @@ int jrg_adam_update(int precision, int64_t n, void* param, const void* grad, voi
 int jrg_ewald(const jrg_plan* plan, double eta, double cutoff, double* result,
               void* workspace, cudaStream_t stream);
 
+/* Selects the register-resident slab kernels for cubic grids N^3 with
+ * N in {16, 24, 27, 32, 36, 48, 64, 96} (enable = 1, the default) or the
+ * generic shared-memory Stockham kernels for every grid (enable = 0);
+ * enable < 0 only queries.  Returns the previous setting.  Process-wide;
+ * no reference counterpart. */
+int jrg_fast_paths(int enable);
+
 /* Per-phase CUDA-event timing of jrg_energy_grad (no reference counterpart;
  * the reference only times whole steps, calc driver :207-211).  enable
  * creates events for up to max_calls calls (0 disables); read synchronises

@@ -43,6 +43,7 @@ _SIGS = {
   "jrg_adam_update": ([ct.c_int, ct.c_int64, _vp, _vp, _vp, _vp, _vp, ct.c_int,
                        ct.c_double, ct.c_double, ct.c_double, ct.c_double, _vp], ct.c_int),
   "jrg_ewald": ([_vp, ct.c_double, ct.c_double, _vp, _vp, _vp], ct.c_int),
+  "jrg_fast_paths": ([ct.c_int], ct.c_int),
   "jrg_profile_enable": ([_vp, ct.c_int], ct.c_int),
   "jrg_profile_read": ([_vp, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int), ct.c_int], ct.c_int),
   "jrg_profile_phase_name": ([ct.c_int], ct.c_char_p),

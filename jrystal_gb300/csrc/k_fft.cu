@@ -12,6 +12,7 @@
 // only y rows that hold sphere points are transformed where the data are
 // known to be zero.  The intermediate between the two kernels holds only the
 // active planes: [band][active plane][y][z].
+#include "fast_dispatch.h"
 #include "plan.h"
 
 namespace jrg {
@@ -296,6 +297,12 @@ template <typename R>
 int launch_plane_inv_sphere(const jrg_plan* P, const void* coef, void* planes, int nbands,
                             cudaStream_t st) {
   using C = C_t<R>;
+  {
+    fast::Args a{coef, planes, nullptr, nullptr, 0.0, 0, nbands, 1};
+    const int f = fast::dispatch<R>(P, fast::OP_PLANE_INV, a, st);
+    if (f < 0) return -f;
+    if (f > 0) return JRG_OK;
+  }
   const C* tw = reinterpret_cast<const C*>(P->d.tw);
   size_t sm = plane_smem<R>(P->ny, P->nz, P->max_rows);
   int rc = set_smem(k_plane_inv_sphere<R>, sm);
@@ -313,6 +320,12 @@ template <typename R>
 int launch_line_density(const jrg_plan* P, const void* planes, void* rho_part, const double* wband,
                         double wscale, int band0, int nbands, int bands_per_group, cudaStream_t st) {
   using C = C_t<R>;
+  {
+    fast::Args a{planes, rho_part, nullptr, wband, wscale, band0, nbands, bands_per_group};
+    const int f = fast::dispatch<R>(P, fast::OP_LINE_DENSITY, a, st);
+    if (f < 0) return -f;
+    if (f > 0) return JRG_OK;
+  }
   const C* tw = reinterpret_cast<const C*>(P->d.tw);
   size_t sm = line_smem<R>(P->nx, P->nz, 0, P->nx);
   int rc = set_smem(k_line_density<R>, sm);
@@ -330,6 +343,12 @@ template <typename R>
 int launch_line_apply_v(const jrg_plan* P, const void* planes_in, void* planes_out, const void* vr,
                         int nbands, int bands_per_group, cudaStream_t st) {
   using C = C_t<R>;
+  if (planes_in == planes_out) {   // the fast kernel works in place
+    fast::Args a{planes_in, planes_out, vr, nullptr, 0.0, 0, nbands, bands_per_group};
+    const int f = fast::dispatch<R>(P, fast::OP_LINE_APPLY_V, a, st);
+    if (f < 0) return -f;
+    if (f > 0) return JRG_OK;
+  }
   const C* tw = reinterpret_cast<const C*>(P->d.tw);
   size_t sm = line_smem<R>(P->nx, P->nz, P->nx * P->nz, P->nx + P->nact);
   int rc = set_smem(k_line_apply_v<R>, sm);
@@ -349,6 +368,12 @@ int launch_plane_fwd_sphere(const jrg_plan* P, const void* planes, const void* c
                             const double* wband, int band0, int nbands, double scale,
                             cudaStream_t st) {
   using C = C_t<R>;
+  {
+    fast::Args a{planes, gcoef, coef, wband, scale, band0, nbands, 1};
+    const int f = fast::dispatch<R>(P, fast::OP_PLANE_FWD, a, st);
+    if (f < 0) return -f;
+    if (f > 0) return JRG_OK;
+  }
   const C* tw = reinterpret_cast<const C*>(P->d.tw);
   size_t sm = plane_smem<R>(P->ny, P->nz, P->max_rows);
   int rc = set_smem(k_plane_fwd_sphere<R>, sm);

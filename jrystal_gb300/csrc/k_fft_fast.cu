@@ -1,0 +1,355 @@
+// Fast slab kernels for cubic grids N^3, N in {16, 24, 27, 32, 36, 48, 64, 96}.
+//
+// Same data flow as the generic kernels in k_fft.cu (plane pass over y and z
+// with the sphere scatter/gather fused in, line pass over x with the density
+// or V(r) product fused in), but every 1-D transform is register-resident:
+// a line of N points is held by N2 threads (N1 points each) and crosses
+// shared memory once (see fft_reg.cuh).  Global loads and stores feed the
+// first and leave the last register step directly.  Thread t of a CTA works
+// on line l = t % L as worker j2 = t / L, so the lanes of a warp walk
+// consecutive lines: consecutive z in global memory, consecutive addresses
+// in the exchange buffers, and an odd row pitch (N + 1) in the [z][y] plane
+// buffer keeps the column accesses free of bank conflicts.
+#include "fast_dispatch.h"
+#include "fft_reg.cuh"
+#include "plan.h"
+
+namespace jrg {
+namespace fast {
+
+using reg::Split;
+
+template <int N> constexpr int threads_for() { return N * Split<N>::N2; }
+
+// sphere -> y,z-transformed active planes
+template <typename R, int N>
+__global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere(
+    const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ planes, const int* __restrict__ plane_off,
+    const int* __restrict__ sph_yz, const int* __restrict__ row_off, const int* __restrict__ rows,
+    const C_t<R>* __restrict__ tw_g, int ng, int nact) {
+  using C = C_t<R>;
+  constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2, P = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* A = tw + N;              // [z][y], pitch P
+  C* ex = A + N * P;          // exchange, N*N
+  int* srows = reinterpret_cast<int*>(ex + N * N);
+  const int p = blockIdx.x, band = blockIdx.y, tid = threadIdx.x;
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = tw_g[i];
+  const C z0 = czero<C>();
+  for (int i = tid; i < N * P; i += blockDim.x) A[i] = z0;
+  const int r0 = row_off[p], nr = row_off[p + 1] - r0;
+  for (int i = tid; i < nr; i += blockDim.x) srows[i] = rows[r0 + i];
+  __syncthreads();
+  const C* cb = coef + (size_t)band * ng;
+  for (int e = plane_off[p] + tid; e < plane_off[p + 1]; e += blockDim.x) {
+    const int yz = sph_yz[e];
+    const int y = yz / N, z = yz - y * N;
+    A[z * P + y] = cb[e];
+  }
+  __syncthreads();
+  // z transforms of the active rows (L = nr lines)
+  C v[N1];
+  {
+    const bool act = tid < nr * N2;
+    const int l = act ? tid % nr : 0, j2 = act ? tid / nr : 0;
+    const int y = srows[l];
+    if (act) {
+#pragma unroll
+      for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[(N2 * j1 + j2) * P + y];
+      reg::line_step_a<N, +1>(v, tw, j2, ex, nr, l);
+    }
+    __syncthreads();
+    if (act) {
+      reg::line_step_b<N, +1>(v, j2, ex, nr, l);
+#pragma unroll
+      for (int j = 0; j < N1; ++j) A[(N2 * j + j2) * P + y] = v[j];
+    }
+    __syncthreads();
+  }
+  // y transforms of all z columns (L = N lines), straight to global memory
+  {
+    const int z = tid % N, j2 = tid / N;
+#pragma unroll
+    for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[z * P + N2 * j1 + j2];
+    reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
+    __syncthreads();
+    reg::line_step_b<N, +1>(v, j2, ex, N, z);
+    C* out = planes + ((size_t)band * nact + p) * (N * N);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) out[(N2 * j + j2) * N + z] = v[j];
+  }
+}
+
+// inverse x transform + occupation-weighted |psi|^2 of a band group
+template <typename R, int N>
+__global__ void __launch_bounds__(threads_for<N>()) k_line_density(
+    const C_t<R>* __restrict__ planes, R* __restrict__ rho_part, const double* __restrict__ wband,
+    double wscale, int band0, int nband, int bands_per_group, const int* __restrict__ xact,
+    const C_t<R>* __restrict__ tw_g, int nact) {
+  using C = C_t<R>;
+  constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* ex0 = tw + N;
+  C* ex1 = ex0 + N * N;
+  int* sxact = reinterpret_cast<int*>(ex1 + N * N);
+  const int y = blockIdx.x, grp = blockIdx.y, tid = threadIdx.x;
+  const int z = tid % N, j2 = tid / N;
+  for (int i = tid; i < N; i += blockDim.x) { tw[i] = tw_g[i]; sxact[i] = xact[i]; }
+  __syncthreads();
+  int slot[N1];
+#pragma unroll
+  for (int j1 = 0; j1 < N1; ++j1) slot[j1] = sxact[N2 * j1 + j2];
+  R acc[N1];
+#pragma unroll
+  for (int j = 0; j < N1; ++j) acc[j] = (R)0;
+  const int b_begin = grp * bands_per_group;
+  const int b_end = min(nband, b_begin + bands_per_group);
+  const C z0 = czero<C>();
+  C v[N1];
+  int parity = 0;
+  for (int b = b_begin; b < b_end; ++b, parity ^= 1) {
+    const R w = (R)(wband[band0 + b] * wscale);
+    const C* src = planes + (size_t)b * nact * (N * N) + y * N + z;
+#pragma unroll
+    for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : src[(size_t)slot[j1] * (N * N)];
+    C* ex = parity ? ex1 : ex0;
+    reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
+    __syncthreads();
+    reg::line_step_b<N, +1>(v, j2, ex, N, z);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) acc[j] += w * (v[j].x * v[j].x + v[j].y * v[j].y);
+  }
+  R* out = rho_part + (size_t)grp * (N * N * N) + y * N + z;
+#pragma unroll
+  for (int j = 0; j < N1; ++j) out[(size_t)(N2 * j + j2) * (N * N)] = acc[j];
+}
+
+// adjoint line pass: inverse x transform, times V(r), forward x transform,
+// active planes written back in place
+template <typename R, int N>
+__global__ void __launch_bounds__(threads_for<N>()) k_line_apply_v(
+    C_t<R>* __restrict__ planes, const R* __restrict__ vr, int nband, int bands_per_group,
+    const int* __restrict__ xact, const C_t<R>* __restrict__ tw_g, int nact) {
+  using C = C_t<R>;
+  constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* ex0 = tw + N;
+  C* ex1 = ex0 + N * N;
+  int* sxact = reinterpret_cast<int*>(ex1 + N * N);
+  const int y = blockIdx.x, grp = blockIdx.y, tid = threadIdx.x;
+  const int z = tid % N, j2 = tid / N;
+  for (int i = tid; i < N; i += blockDim.x) { tw[i] = tw_g[i]; sxact[i] = xact[i]; }
+  __syncthreads();
+  int slot[N1];
+  R vloc[N1];
+#pragma unroll
+  for (int j1 = 0; j1 < N1; ++j1) {
+    slot[j1] = sxact[N2 * j1 + j2];
+    vloc[j1] = vr[(size_t)(N2 * j1 + j2) * (N * N) + y * N + z];
+  }
+  const int b_begin = grp * bands_per_group;
+  const int b_end = min(nband, b_begin + bands_per_group);
+  const C z0 = czero<C>();
+  C v[N1];
+  for (int b = b_begin; b < b_end; ++b) {
+    C* base = planes + (size_t)b * nact * (N * N) + y * N + z;
+#pragma unroll
+    for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : base[(size_t)slot[j1] * (N * N)];
+    reg::line_step_a<N, +1>(v, tw, j2, ex0, N, z);
+    __syncthreads();
+    reg::line_step_b<N, +1>(v, j2, ex0, N, z);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) v[j] = cscale(v[j], vloc[j]);
+    reg::line_step_a<N, -1>(v, tw, j2, ex1, N, z);
+    __syncthreads();
+    reg::line_step_b<N, -1>(v, j2, ex1, N, z);
+#pragma unroll
+    for (int j = 0; j < N1; ++j)
+      if (slot[j] >= 0) base[(size_t)slot[j] * (N * N)] = v[j];
+  }
+}
+
+// forward: y, z transforms of an active plane, sphere gather and gradient
+//   g[b][e] = f_b * (tk[k][e] * c[b][e] + scale * FFT(V psi_b)[e])
+template <typename R, int N>
+__global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
+    const C_t<R>* __restrict__ planes, const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ gcoef,
+    const double* __restrict__ wband, const double* __restrict__ tk, int nb_per_k, int band0,
+    const int* __restrict__ plane_off, const int* __restrict__ sph_yz, const int* __restrict__ row_off,
+    const int* __restrict__ rows, const C_t<R>* __restrict__ tw_g, int ng, int nact, int nk,
+    double scale) {
+  using C = C_t<R>;
+  constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2, P = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* A = tw + N;
+  C* ex = A + N * P;
+  int* srows = reinterpret_cast<int*>(ex + N * N);
+  const int p = blockIdx.x, band = blockIdx.y, tid = threadIdx.x;
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = tw_g[i];
+  const int r0 = row_off[p], nr = row_off[p + 1] - r0;
+  for (int i = tid; i < nr; i += blockDim.x) srows[i] = rows[r0 + i];
+  __syncthreads();
+  C v[N1];
+  // y transforms of all z columns, from global memory
+  {
+    const int z = tid % N, j2 = tid / N;
+    const C* in = planes + ((size_t)band * nact + p) * (N * N) + z;
+#pragma unroll
+    for (int j1 = 0; j1 < N1; ++j1) v[j1] = in[(N2 * j1 + j2) * N];
+    reg::line_step_a<N, -1>(v, tw, j2, ex, N, z);
+    __syncthreads();
+    reg::line_step_b<N, -1>(v, j2, ex, N, z);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) A[z * P + N2 * j + j2] = v[j];
+    __syncthreads();
+  }
+  // z transforms of the active rows
+  {
+    const bool act = tid < nr * N2;
+    const int l = act ? tid % nr : 0, j2 = act ? tid / nr : 0;
+    const int y = srows[l];
+    if (act) {
+#pragma unroll
+      for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[(N2 * j1 + j2) * P + y];
+      reg::line_step_a<N, -1>(v, tw, j2, ex, nr, l);
+    }
+    __syncthreads();
+    if (act) {
+      reg::line_step_b<N, -1>(v, j2, ex, nr, l);
+#pragma unroll
+      for (int j = 0; j < N1; ++j) A[(N2 * j + j2) * P + y] = v[j];
+    }
+    __syncthreads();
+  }
+  const int gb = band0 + band;
+  const int kidx = (gb / nb_per_k) % nk;
+  const R w = (R)wband[gb];
+  const R sc = (R)scale;
+  const double* tkk = tk + (size_t)kidx * ng;
+  const C* cb = coef + (size_t)band * ng;
+  C* gout = gcoef + (size_t)band * ng;
+  for (int e = plane_off[p] + tid; e < plane_off[p + 1]; e += blockDim.x) {
+    const int yz = sph_yz[e];
+    const int y = yz / N, z = yz - y * N;
+    const C val = A[z * P + y];
+    const C c = cb[e];
+    const R t = (R)tkk[e];
+    C g;
+    g.x = w * (t * c.x + sc * val.x);
+    g.y = w * (t * c.y + sc * val.y);
+    gout[e] = g;
+  }
+}
+
+// ------------------------------------------------------------------------
+// dispatch: returns 1 when a fast kernel was launched, 0 when the grid is not
+// covered (the caller then uses the generic kernels), <0 on a launch error.
+// ------------------------------------------------------------------------
+template <typename R, int N> size_t plane_smem() {
+  return sizeof(C_t<R>) * (size_t)(N + N * (N + 1) + N * N) + sizeof(int) * (N + 1);
+}
+template <typename R, int N> size_t line_smem() {
+  return sizeof(C_t<R>) * (size_t)(N + 2 * N * N) + sizeof(int) * N;
+}
+
+static int optin_smem() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return v;
+}
+
+// 1: ready to launch, 0: does not fit (use the generic kernels), <0: -status
+template <typename K> static int prep(K kernel, size_t bytes) {
+  if ((long long)bytes > optin_smem()) return 0;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return -cuda_fail(e, "cudaFuncSetAttribute(fast slab kernel)");
+  return 1;
+}
+
+#define FAST_LAUNCHED(what)                                  \
+  do {                                                       \
+    ::jrg::count_launch();                                   \
+    cudaError_t e_ = cudaGetLastError();                     \
+    if (e_ != cudaSuccess) return -::jrg::cuda_fail(e_, what); \
+    return 1;                                                \
+  } while (0)
+
+template <typename R, int N>
+static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
+  using C = C_t<R>;
+  const C* tw = reinterpret_cast<const C*>(P->d.tw);   // x table first; all axes equal
+  constexpr int T = threads_for<N>();
+  int rc;
+  switch (op) {
+    case OP_PLANE_INV: {
+      const size_t sm = plane_smem<R, N>();
+      if ((rc = prep(k_plane_inv_sphere<R, N>, sm)) <= 0) return rc;
+      k_plane_inv_sphere<R, N><<<dim3(P->nact, a.nbands), T, sm, st>>>(
+          reinterpret_cast<const C*>(a.in), reinterpret_cast<C*>(a.out), P->d.plane_off, P->d.sph_yz,
+          P->d.row_off, P->d.rows, tw, P->ng, P->nact);
+      FAST_LAUNCHED("fast::k_plane_inv_sphere");
+    }
+    case OP_LINE_DENSITY: {
+      const size_t sm = line_smem<R, N>();
+      if ((rc = prep(k_line_density<R, N>, sm)) <= 0) return rc;
+      const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
+      k_line_density<R, N><<<dim3(N, ngroups), T, sm, st>>>(
+          reinterpret_cast<const C*>(a.in), reinterpret_cast<R*>(a.out), a.w, a.wscale, a.band0,
+          a.nbands, a.bands_per_group, P->d.xact, tw, P->nact);
+      FAST_LAUNCHED("fast::k_line_density");
+    }
+    case OP_LINE_APPLY_V: {
+      const size_t sm = line_smem<R, N>();
+      if ((rc = prep(k_line_apply_v<R, N>, sm)) <= 0) return rc;
+      const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
+      k_line_apply_v<R, N><<<dim3(N, ngroups), T, sm, st>>>(
+          reinterpret_cast<C*>(a.out), reinterpret_cast<const R*>(a.aux), a.nbands,
+          a.bands_per_group, P->d.xact, tw, P->nact);
+      FAST_LAUNCHED("fast::k_line_apply_v");
+    }
+    default: {
+      const size_t sm = plane_smem<R, N>();
+      if ((rc = prep(k_plane_fwd_sphere<R, N>, sm)) <= 0) return rc;
+      k_plane_fwd_sphere<R, N><<<dim3(P->nact, a.nbands), T, sm, st>>>(
+          reinterpret_cast<const C*>(a.in), reinterpret_cast<const C*>(a.aux),
+          reinterpret_cast<C*>(a.out), a.w, P->d.tk, P->nb, a.band0, P->d.plane_off, P->d.sph_yz,
+          P->d.row_off, P->d.rows, tw, P->ng, P->nact, P->nk, a.wscale);
+      FAST_LAUNCHED("fast::k_plane_fwd_sphere");
+    }
+  }
+}
+
+static bool g_fast_enabled = true;
+
+template <typename R>
+int dispatch(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
+  if (!g_fast_enabled || !(P->nx == P->ny && P->ny == P->nz)) return 0;
+  switch (P->nx) {
+    case 16: return run<R, 16>(P, op, a, st);
+    case 24: return run<R, 24>(P, op, a, st);
+    case 27: return run<R, 27>(P, op, a, st);
+    case 32: return run<R, 32>(P, op, a, st);
+    case 36: return run<R, 36>(P, op, a, st);
+    case 48: return run<R, 48>(P, op, a, st);
+    case 64: return run<R, 64>(P, op, a, st);
+    case 96: return run<R, 96>(P, op, a, st);
+    default: return 0;
+  }
+}
+
+template int dispatch<float>(const jrg_plan*, int, const Args&, cudaStream_t);
+template int dispatch<double>(const jrg_plan*, int, const Args&, cudaStream_t);
+
+}  // namespace fast
+}  // namespace jrg
+
+extern "C" int jrg_fast_paths(int enable) {
+  const int prev = jrg::fast::g_fast_enabled ? 1 : 0;
+  if (enable >= 0) jrg::fast::g_fast_enabled = enable != 0;
+  return prev;
+}

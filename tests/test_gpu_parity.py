@@ -29,6 +29,13 @@ CASES = [
   dict(kind="si2", grid=(16, 16, 16), kgrid=(2, 2, 2), nb=8, nocc=4),
   dict(kind="diamond", grid=(14, 15, 16), kgrid=(1, 1, 1), nb=3, nocc=3),
   dict(kind="si2", grid=(10, 12, 9), kgrid=(1, 2, 1), nb=5, nocc=2, mask="cubic"),
+  # cubic grids covered by the register-resident slab kernels
+  dict(kind="diamond", grid=(24, 24, 24), kgrid=(1, 1, 2), nb=4, nocc=2),
+  dict(kind="si2", grid=(27, 27, 27), kgrid=(1, 1, 1), nb=3, nocc=2),
+  dict(kind="si2", grid=(32, 32, 32), kgrid=(2, 1, 1), nb=4, nocc=2, mask="cubic"),
+  dict(kind="si8", grid=(36, 36, 36), kgrid=(1, 1, 1), nb=5, nocc=3),
+  dict(kind="si2", grid=(48, 48, 48), kgrid=(1, 1, 1), nb=3, nocc=2),
+  dict(kind="si8", grid=(64, 64, 64), kgrid=(1, 1, 1), nb=3, nocc=2),
 ]
 
 
@@ -137,3 +144,30 @@ def test_adam_matches_oracle(prec):
     p, m, v = R.adam_update(p, g * step, m, v, step, 1e-2)
   tol = 1e-14 if prec == 64 else 1e-6
   assert np.abs(tp.cpu().numpy() - p).max() < tol * 10
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_fast_and_generic_slab_kernels_agree(prec):
+  torch = _torch()
+  from jrystal_gb300 import _lib
+  lib = _lib.load()
+  sysm = make_system(kind="si2", grid=(32, 32, 32), kgrid=(2, 1, 1), nb=4, nocc=2)
+  wr, wi = random_params(sysm, seed=21)
+  plan = _plan(sysm, prec)
+  dt = torch.float64 if prec == 64 else torch.float32
+  twr = torch.tensor(wr, dtype=dt, device="cuda")
+  twi = torch.tensor(wi, dtype=dt, device="cuda")
+  out = {}
+  prev = lib.jrg_fast_paths(-1)
+  try:
+    for fast in (1, 0):
+      lib.jrg_fast_paths(fast)
+      e, gr, gi = plan.energy_and_grad(twr, twi, sysm.occupation)
+      out[fast] = (e.cpu().numpy().copy(), gr.cpu().numpy(), gi.cpu().numpy())
+  finally:
+    lib.jrg_fast_paths(prev)
+  tol = TOL[prec]
+  assert np.abs(out[1][0][:5] - out[0][0][:5]).max() <= tol["e_rel"] * np.abs(out[0][0][:5]).max()
+  scale = np.abs(out[0][1]).max()
+  assert np.abs(out[1][1] - out[0][1]).max() <= tol["g_rel"] * scale
+  assert np.abs(out[1][2] - out[0][2]).max() <= tol["g_rel"] * scale
