@@ -113,6 +113,13 @@ int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
 int jrg_potential(const jrg_plan* plan, const void* density, int kohn_sham, void* out,
                   void* workspace, cudaStream_t stream);
 
+/* Elementwise LDA on n real densities: the energy per particle eps_xc
+ * (kohn_sham = 0) or the potential v_xc = d(rho eps_xc)/d rho (kohn_sham =
+ * 1), summed over the JRG_XC_* terms; jrystal/_src/xc.py:54-64,109-124,222-253
+ * (jax_xc lda_x and lda_c_vwn, unpolarised). */
+int jrg_lda(int precision, int64_t n, int xc, int kohn_sham, const void* rho, void* out,
+            cudaStream_t stream);
+
 /* Batched complex 3-D FFT over the last three axes of [batch][nx][ny][nz].
  * direction -1: forward (unnormalised, jnp.fft.fftn); +1: inverse with the
  * 1/(nx ny nz) factor (jnp.fft.ifftn).  in and out may alias.  workspace

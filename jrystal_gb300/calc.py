@@ -1,0 +1,214 @@
+"""Direct-minimisation driver: jrystal's ground-state loop
+(calc/calc_ground_state_energy_all_electrons.py:63-247) on the fused GPU path.
+
+Each step runs the orthonormalisation, energy and hand-written gradient
+(jrg_energy_grad) and the Adam update (jrg_adam_update) on the device; the
+host reads back the energy for the windowed convergence check
+(calc/convergence.py:13-35), as the reference does after every update.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import grid as _grid
+from .crystal import Crystal
+from .engine import PlaneWavePlan, adam_update
+
+DEFAULT_CONFIG = {
+  "crystal": None,
+  "crystal_file_path_path": None,
+  "spin": 0,
+  "xc": "lda_x+lda_c_vwn",
+  "freq_mask_method": "spherical",
+  "cutoff_energy": 40.0,
+  "grid_sizes": 16,
+  "k_grid_sizes": [1, 1, 1],
+  "occupation": "uniform",
+  "smearing": 0.0,
+  "empty_bands": 0,
+  "spin_restricted": True,
+  "ewald_args": {"ewald_eta": 0.1, "ewald_cutoff": 2.0e4},
+  "epoch": 1000,
+  "optimizer": "adam",
+  "optimizer_args": {"learning_rate": 0.01, "b1": 0.9, "b2": 0.99},
+  "convergence_window_size": 20,
+  "convergence_condition": 1e-6,
+  "seed": 123,
+  "jax_enable_x64": True,
+  "verbose": False,
+}
+
+
+class ConvergenceChecker:
+  """Standard deviation of the last ``window_size`` energies below the
+  threshold (calc/convergence.py:13-35)."""
+
+  def __init__(self, window_size: int = 20, threshold: float = 1e-5):
+    self.window_size = window_size
+    self.threshold = threshold
+    self.history: List[float] = []
+
+  def check(self, value: float) -> bool:
+    self.history.append(float(value))
+    if len(self.history) > self.window_size:
+      self.history.pop(0)
+    if len(self.history) < self.window_size:
+      return False
+    return bool(np.std(self.history) < self.threshold)
+
+  def reset(self):
+    self.history = []
+
+
+class Minimizer:
+  """Adam on the raw plane-wave parameters with the fused device step.
+
+  params: tensor (2, S, K, G, B) holding w_re and w_im.  ``scale_fn``, when
+  given, is called as scale_fn(minimizer) before each update and returns a
+  float32 tensor of one positive scale per parameter element (the learned
+  diagonal preconditioner) or None for the plain update."""
+
+  def __init__(self, plan: PlaneWavePlan, occupation, params: torch.Tensor, lr: float = 1e-2,
+               b1: float = 0.9, b2: float = 0.99, eps: float = 1e-8, scale_fn=None,
+               total_steps: Optional[int] = None):
+    self.plan = plan
+    self.occ = torch.as_tensor(np.asarray(occupation), dtype=torch.float64, device=plan.device)
+    if tuple(params.shape) != (2,) + plan.param_shape:
+      raise ValueError(f"params shape {tuple(params.shape)} != {(2,) + plan.param_shape}")
+    self.params = params.contiguous()
+    self.grads = torch.empty_like(self.params)
+    self.m = torch.zeros_like(self.params)
+    self.v = torch.zeros_like(self.params)
+    self.lr, self.b1, self.b2, self.eps = lr, b1, b2, eps
+    self.t = 0
+    self.total_steps = total_steps
+    self.scale_fn = scale_fn
+    self.last_scale = None
+
+  def energy_and_grad(self):
+    e, _, _ = self.plan.energy_and_grad(self.params[0], self.params[1], self.occ, self.grads[0],
+                                        self.grads[1])
+    return e
+
+  def step(self) -> torch.Tensor:
+    """One update; returns the device energy vector of the parameters before it."""
+    e = self.energy_and_grad()
+    self.t += 1
+    scale = self.scale_fn(self) if self.scale_fn is not None else None
+    self.last_scale = scale
+    adam_update(self.params, self.grads, self.m, self.v, self.t, self.lr, self.b1, self.b2,
+                self.eps, scale=scale)
+    return e
+
+  def energy(self) -> float:
+    e, _, _ = self.plan.energy_and_grad(self.params[0], self.params[1], self.occ, with_grad=False)
+    return float(e[4].item())
+
+
+@dataclass
+class GroundStateEnergyOutput:
+  config: dict
+  crystal: Crystal
+  params_pw: dict
+  total_energy: float
+  total_energy_history: List[float]
+  energy_terms: dict = field(default_factory=dict)
+  ewald: float = 0.0
+  steps: int = 0
+  converged: bool = False
+  train_time: float = 0.0
+
+
+def _merge(config):
+  cfg = dict(DEFAULT_CONFIG)
+  cfg.update(config or {})
+  return cfg
+
+
+def create_crystal(cfg) -> Crystal:
+  if isinstance(cfg.get("crystal"), Crystal):
+    return cfg["crystal"]
+  path = cfg.get("crystal_file_path_path")
+  if cfg.get("crystal") is not None and path is None:
+    raise ValueError("pass the geometry as a Crystal object or through crystal_file_path_path")
+  return Crystal.create_from_file(path, spin=cfg.get("spin"))
+
+
+def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
+  """All-electron ground state by direct minimisation with fixed occupations
+  (calc/calc_ground_state_energy_all_electrons.py:63-247)."""
+  cfg = _merge(config)
+  if cfg["optimizer"] != "adam":
+    raise NotImplementedError("only the adam optimiser is implemented on the device")
+  if cfg["occupation"] not in ("uniform", "gamma"):
+    raise NotImplementedError("fixed occupations (uniform, gamma) only")
+  if not cfg["spin_restricted"]:
+    raise NotImplementedError("spin-polarised LDA is not implemented")
+  crystal = create_crystal(cfg)
+  precision = 64 if cfg["jax_enable_x64"] else 32
+  grid_sizes = tuple(int(g) for g in _grid.proper_grid_size(cfg["grid_sizes"]))
+  k_grid = tuple(int(k) for k in np.broadcast_to(cfg["k_grid_sizes"], 3))
+  kpts = _grid.k_vectors(crystal.cell_vectors, k_grid)
+  if cfg["freq_mask_method"] == "spherical":
+    mask = _grid.spherical_mask(crystal.cell_vectors, grid_sizes, cfg["cutoff_energy"])
+  elif cfg["freq_mask_method"] == "cubic":
+    mask = _grid.cubic_mask(grid_sizes)
+  else:
+    raise ValueError("freq_mask_method must be either cubic or spherical.")
+  nelec = crystal.num_electron
+  num_bands = math.ceil(nelec / 2) + cfg["empty_bands"]
+  K = kpts.shape[0]
+  if cfg["occupation"] == "uniform":
+    occ = np.zeros((2, K, num_bands))
+    occ[0, :, :(nelec + crystal.spin) // 2] = 1 / K
+    occ[1, :, :(nelec - crystal.spin) // 2] = 1 / K
+  else:
+    occ = np.zeros((2, K, num_bands))
+    occ[0, 0, :(nelec + crystal.spin) // 2] = 1
+    occ[1, 0, :(nelec - crystal.spin) // 2] = 1
+  occ = occ.sum(0, keepdims=True)
+  if "occupation_array" in cfg:
+    occ = np.asarray(cfg["occupation_array"], dtype=np.float64)
+    num_bands = occ.shape[-1]
+  plan = PlaneWavePlan(crystal.cell_vectors, crystal.positions, crystal.charges, grid_sizes, mask,
+                       kpts, num_bands, 1, precision, cfg["xc"])
+  ew = plan.ewald(cfg["ewald_args"]["ewald_eta"], cfg["ewald_args"]["ewald_cutoff"])
+  ng = int(mask.sum())
+  gen = torch.Generator(device=plan.device)
+  gen.manual_seed(int(cfg["seed"]))
+  if "init_params" in cfg:
+    w_re, w_im = cfg["init_params"]
+    params = torch.tensor(np.stack([w_re, w_im]), dtype=plan.rdtype, device=plan.device)
+  else:
+    params = torch.rand((2, 1, K, ng, num_bands), generator=gen, device=plan.device,
+                        dtype=plan.rdtype)
+  oa = cfg["optimizer_args"]
+  mini = Minimizer(plan, occ, params, lr=oa.get("learning_rate", 1e-2), b1=oa.get("b1", 0.9),
+                   b2=oa.get("b2", 0.999), eps=oa.get("eps", 1e-8),
+                   scale_fn=cfg.get("scale_fn"), total_steps=cfg["epoch"])
+  checker = ConvergenceChecker(cfg["convergence_window_size"], cfg["convergence_condition"])
+  history, converged, train_time = [], False, 0.0
+  i = 0
+  for i in range(cfg["epoch"]):
+    t0 = time.perf_counter()
+    e = mini.step()
+    etot = float(e[4].item())          # the reference blocks on the energy every step
+    train_time += time.perf_counter() - t0
+    history.append(etot)
+    if checker.check(etot):
+      converged = True
+      break
+  e, _, _ = plan.energy_and_grad(mini.params[0], mini.params[1], mini.occ, with_grad=False)
+  e = e.cpu().numpy()
+  terms = dict(kinetic=e[0], external=e[1], hartree=e[2], xc=e[3], total=e[4])
+  return GroundStateEnergyOutput(config=cfg, crystal=crystal,
+                                 params_pw={"w_re": mini.params[0], "w_im": mini.params[1]},
+                                 total_energy=float(e[4] + ew), total_energy_history=history,
+                                 energy_terms=terms, ewald=ew, steps=i + 1, converged=converged,
+                                 train_time=train_time)

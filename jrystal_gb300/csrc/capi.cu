@@ -19,10 +19,12 @@ template <typename R> int launch_plane_fwd_sphere(const jrg_plan*, const void*, 
 template <typename R> int launch_fft3d_dense(const FftAxis*, const C_t<R>*, int, int, bool, const void*, C_t<R>*, C_t<R>*, double, cudaStream_t);
 template <typename R> int launch_pack_params(const void*, const void*, void*, int, int, int, bool, cudaStream_t);
 template <typename R> int launch_unpack(const void*, void*, void*, void*, int, int, int, double, cudaStream_t);
-template <typename R> int launch_gram(const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t);
+template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t);
 int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, cudaStream_t);
 int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t);
-template <typename R> int launch_rotate(int, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, cudaStream_t);
+template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, cudaStream_t);
+constexpr int kSplit = 0, kBand = 1;           // tall-operand layouts (k_orth.cu)
+constexpr int kRotBand = 0, kRotGC = 1, kRotGSplit = 2;
 template <typename R> int launch_reduce_density(const void*, void*, int, int, long long, cudaStream_t);
 template <typename R> int launch_recip_terms(const void*, const double*, const void*, void*, double*, double*, int, long long, double, cudaStream_t);
 template <typename R> int launch_potential(const void*, const void*, double, void*, double*, int, long long, int, double, cudaStream_t);
@@ -35,6 +37,7 @@ template <typename R> int launch_geometry_tables(double*, double*, void*, const 
 int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
 template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t);
 int launch_twiddles(int n, int prec, void* out, cudaStream_t st);
+int launch_lda(int prec, long long n, int xc, int ks, const void* rho, void* out, cudaStream_t st);
 
 static thread_local std::string g_err;
 static std::atomic<long long> g_launches{0};
@@ -82,7 +85,7 @@ static void layout_workspace(jrg_plan* P) {
   if (w.nepart < 2 * kEwaldBlocks) w.nepart = 2 * kEwaldBlocks;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t r = o; o += align256(bytes); return r; };
-  w.wc = take(nbt * P->ng * C);
+  w.wc = 0;                             // parameters are read in place
   w.c = take(nbt * P->ng * C);
   w.gram_part = take(nsk * w.gram_splits * b2);
   w.gram = take(nsk * b2);
@@ -356,17 +359,13 @@ static void profile_call_done(const jrg_plan* P) {
 
 template <typename R>
 static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im, void* ws,
-                          cudaStream_t st) {
+                          cudaStream_t st, int out_kind = kRotBand, void* out = nullptr) {
   const Workspace& w = P->ws;
   const int nsk = P->ns * P->nk;
   int rc;
   {
-    PHASE(PH_PACK);
-    if ((rc = launch_pack_params<R>(w_re, w_im, wsp(ws, w.wc), nsk, P->ng, P->nb, false, st))) return rc;
-  }
-  {
     PHASE(PH_GRAM);
-    if ((rc = launch_gram<R>(wsp(ws, w.wc), wsp(ws, w.wc), (double2*)wsp(ws, w.gram_part),
+    if ((rc = launch_gram<R>(kSplit, w_re, w_im, kSplit, w_re, w_im, (double2*)wsp(ws, w.gram_part),
                              (double2*)wsp(ws, w.gram), nsk, P->ng, P->nb, w.gram_splits, st)))
       return rc;
   }
@@ -377,8 +376,8 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
       return rc;
   }
   PHASE(PH_ROTATE);
-  return launch_rotate<R>(0, wsp(ws, w.wc), (double2*)wsp(ws, w.rinv), nullptr, nullptr,
-                          wsp(ws, w.c), nullptr, nsk, P->ng, P->nb, 1.0, st);
+  return launch_rotate<R>(out_kind, kSplit, w_re, w_im, (double2*)wsp(ws, w.rinv), nullptr, nullptr,
+                          out ? out : wsp(ws, w.c), nullptr, nsk, P->ng, P->nb, 1.0, st);
 }
 
 // density of the band-major coefficients held in workspace slot c
@@ -457,8 +456,9 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
   // orthonormalisation adjoint
   {
     PHASE(PH_ADJ_GRAM);
-    if ((rc = launch_gram<R>(wsp(ws, w.c), wsp(ws, w.gc), (double2*)wsp(ws, w.adj_part),
-                             (double2*)wsp(ws, w.adj), nsk, P->ng, P->nb, w.gram_splits, st)))
+    if ((rc = launch_gram<R>(kBand, wsp(ws, w.c), nullptr, kBand, wsp(ws, w.gc), nullptr,
+                             (double2*)wsp(ws, w.adj_part), (double2*)wsp(ws, w.adj), nsk, P->ng,
+                             P->nb, w.gram_splits, st)))
       return rc;
   }
   double2* rh = (double2*)wsp(ws, w.kmat);
@@ -470,8 +470,8 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
       return rc;
   }
   PHASE(PH_ADJ_ROTATE);
-  return launch_rotate<R>(2, wsp(ws, w.gc), rh, wsp(ws, w.c), negm2, g_re, g_im, nsk, P->ng, P->nb,
-                          2.0, st);
+  return launch_rotate<R>(kRotGSplit, kBand, wsp(ws, w.gc), nullptr, rh, wsp(ws, w.c), negm2, g_re,
+                          g_im, nsk, P->ng, P->nb, 2.0, st);
 }
 
 template <typename R>
@@ -494,19 +494,8 @@ static int density_entry(const jrg_plan* P, const void* coeff, const double* occ
 template <typename R>
 static int coeff_entry(const jrg_plan* P, const void* w_re, const void* w_im, void* coeff, void* ws,
                        cudaStream_t st) {
-  const Workspace& w = P->ws;
-  const int nsk = P->ns * P->nk;
-  JRG_CUDA(cudaMemsetAsync(wsp(ws, w.flags), 0, 64, st));
-  int rc;
-  if ((rc = launch_pack_params<R>(w_re, w_im, wsp(ws, w.wc), nsk, P->ng, P->nb, false, st))) return rc;
-  if ((rc = launch_gram<R>(wsp(ws, w.wc), wsp(ws, w.wc), (double2*)wsp(ws, w.gram_part),
-                           (double2*)wsp(ws, w.gram), nsk, P->ng, P->nb, w.gram_splits, st)))
-    return rc;
-  if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram), (double2*)wsp(ws, w.rmat),
-                                (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags), st)))
-    return rc;
-  return launch_rotate<R>(1, wsp(ws, w.wc), (double2*)wsp(ws, w.rinv), nullptr, nullptr, coeff,
-                          nullptr, nsk, P->ng, P->nb, 1.0, st);
+  JRG_CUDA(cudaMemsetAsync(wsp(ws, P->ws.flags), 0, 64, st));
+  return orthonormalise<R>(P, w_re, w_im, ws, st, kRotGC, coeff);
 }
 
 template <typename R>
@@ -606,6 +595,12 @@ int jrg_fft3d(int prec, const int grid[3], int batch, int direction, const void*
                                       (double2*)scratch, (double2*)out, scale, st);
   return launch_fft3d_dense<float>(ax, (const float2*)tw, batch, direction, false, in,
                                    (float2*)scratch, (float2*)out, scale, st);
+}
+
+int jrg_lda(int prec, int64_t n, int xc, int kohn_sham, const void* rho, void* out, cudaStream_t st) {
+  if (!rho || !out || n < 0 || (prec != 32 && prec != 64) || (xc & ~3) || !xc)
+    return fail(JRG_ERR_INVALID, "jrg_lda: bad argument");
+  return launch_lda(prec, n, xc, kohn_sham ? 1 : 0, rho, out, st);
 }
 
 int jrg_adam_update(int prec, int64_t n, void* param, const void* grad, void* m, void* v,

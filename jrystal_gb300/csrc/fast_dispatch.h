@@ -15,5 +15,9 @@ struct Args {
 };
 // 1: launched, 0: grid not covered (use the generic kernels), <0: -status
 template <typename R> int dispatch(const jrg_plan* P, int op, const Args& a, cudaStream_t st);
+// dense batched 3-D transform of cubic grids (same return convention)
+template <typename R>
+int dispatch_dense(const FftAxis* ax, const C_t<R>* tw, int batch, int dir, bool real_in,
+                   const void* in, C_t<R>* scratch, C_t<R>* out, double scale, cudaStream_t st);
 }  // namespace fast
 }  // namespace jrg

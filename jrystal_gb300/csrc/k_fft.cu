@@ -396,6 +396,11 @@ int launch_fft3d_dense(const FftAxis* ax, const C_t<R>* tw, int batch, int dir, 
                        const void* in, C_t<R>* scratch, C_t<R>* out, double scale,
                        cudaStream_t st) {
   using C = C_t<R>;
+  {
+    const int f = fast::dispatch_dense<R>(ax, tw, batch, dir, real_in, in, scratch, out, scale, st);
+    if (f < 0) return -f;
+    if (f > 0) return JRG_OK;
+  }
   const int nx = ax[0].n, ny = ax[1].n, nz = ax[2].n;
   size_t smp = plane_smem<R>(ny, nz, 0);
   size_t sml = line_smem<R>(nx, nz, 0, 0);

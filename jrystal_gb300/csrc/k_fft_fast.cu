@@ -245,6 +245,80 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
   }
 }
 
+// dense plane pass of whole grids [batch][x][y][z]: z then y transforms of
+// plane x (input real or complex), result to `out` in the same layout
+template <typename R, int N, int DIR, bool REAL_IN>
+__global__ void __launch_bounds__(threads_for<N>()) k_plane_dense(const void* __restrict__ in_v,
+                                                                   C_t<R>* __restrict__ out,
+                                                                   const C_t<R>* __restrict__ tw_g) {
+  using C = C_t<R>;
+  constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2, P = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* A = tw + N;
+  C* ex = A + N * P;
+  const int tid = threadIdx.x;
+  const size_t base = ((size_t)blockIdx.y * N + blockIdx.x) * (N * N);
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = tw_g[i];
+  for (int i = tid; i < N * N; i += blockDim.x) {
+    const int y = i / N, z = i - y * N;
+    C v;
+    if constexpr (REAL_IN) { v.x = reinterpret_cast<const R*>(in_v)[base + i]; v.y = 0; }
+    else v = reinterpret_cast<const C*>(in_v)[base + i];
+    A[z * P + y] = v;
+  }
+  __syncthreads();
+  C v[N1];
+  {
+    const int y = tid % N, j2 = tid / N;
+#pragma unroll
+    for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[(N2 * j1 + j2) * P + y];
+    reg::line_step_a<N, DIR>(v, tw, j2, ex, N, y);
+    __syncthreads();
+    reg::line_step_b<N, DIR>(v, j2, ex, N, y);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) A[(N2 * j + j2) * P + y] = v[j];
+    __syncthreads();
+  }
+  {
+    const int z = tid % N, j2 = tid / N;
+#pragma unroll
+    for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[z * P + N2 * j1 + j2];
+    reg::line_step_a<N, DIR>(v, tw, j2, ex, N, z);
+    __syncthreads();
+    reg::line_step_b<N, DIR>(v, j2, ex, N, z);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) out[base + (N2 * j + j2) * N + z] = v[j];
+  }
+}
+
+// dense line pass: x transforms of row y of every (x, z) slab, times scale
+template <typename R, int N, int DIR>
+__global__ void __launch_bounds__(threads_for<N>()) k_line_dense(const C_t<R>* __restrict__ in,
+                                                                  C_t<R>* __restrict__ out,
+                                                                  const C_t<R>* __restrict__ tw_g,
+                                                                  double scale) {
+  using C = C_t<R>;
+  constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* ex = tw + N;
+  const int tid = threadIdx.x, y = blockIdx.x;
+  const int z = tid % N, j2 = tid / N;
+  const size_t base = (size_t)blockIdx.y * N * N * N + (size_t)y * N + z;
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = tw_g[i];
+  __syncthreads();
+  C v[N1];
+#pragma unroll
+  for (int j1 = 0; j1 < N1; ++j1) v[j1] = in[base + (size_t)(N2 * j1 + j2) * (N * N)];
+  reg::line_step_a<N, DIR>(v, tw, j2, ex, N, z);
+  __syncthreads();
+  reg::line_step_b<N, DIR>(v, j2, ex, N, z);
+  const R sc = (R)scale;
+#pragma unroll
+  for (int j = 0; j < N1; ++j) out[base + (size_t)(N2 * j + j2) * (N * N)] = cscale(v[j], sc);
+}
+
 // ------------------------------------------------------------------------
 // dispatch: returns 1 when a fast kernel was launched, 0 when the grid is not
 // covered (the caller then uses the generic kernels), <0 on a launch error.
@@ -344,6 +418,60 @@ int dispatch(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
 
 template int dispatch<float>(const jrg_plan*, int, const Args&, cudaStream_t);
 template int dispatch<double>(const jrg_plan*, int, const Args&, cudaStream_t);
+
+template <typename R, int N, int DIR>
+static int dense_run(const C_t<R>* tw, int batch, bool real_in, const void* in, C_t<R>* scratch,
+                     C_t<R>* out, double scale, cudaStream_t st) {
+  using C = C_t<R>;
+  constexpr int T = threads_for<N>();
+  const size_t smp = sizeof(C) * (size_t)(N + N * (N + 1) + N * N);
+  const size_t sml = sizeof(C) * (size_t)(N + N * N);
+  int rc;
+  if (real_in) {
+    if ((rc = prep(k_plane_dense<R, N, DIR, true>, smp)) <= 0) return rc;
+    k_plane_dense<R, N, DIR, true><<<dim3(N, batch), T, smp, st>>>(in, scratch, tw);
+  } else {
+    if ((rc = prep(k_plane_dense<R, N, DIR, false>, smp)) <= 0) return rc;
+    k_plane_dense<R, N, DIR, false><<<dim3(N, batch), T, smp, st>>>(in, scratch, tw);
+  }
+  {
+    ::jrg::count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return -::jrg::cuda_fail(e, "fast::k_plane_dense");
+  }
+  if ((rc = prep(k_line_dense<R, N, DIR>, sml)) <= 0) return rc;
+  k_line_dense<R, N, DIR><<<dim3(N, batch), T, sml, st>>>(scratch, out, tw, scale);
+  FAST_LAUNCHED("fast::k_line_dense");
+}
+
+template <typename R, int N>
+static int dense_dir(const C_t<R>* tw, int batch, int dir, bool real_in, const void* in,
+                     C_t<R>* scratch, C_t<R>* out, double scale, cudaStream_t st) {
+  return dir < 0 ? dense_run<R, N, -1>(tw, batch, real_in, in, scratch, out, scale, st)
+                 : dense_run<R, N, +1>(tw, batch, real_in, in, scratch, out, scale, st);
+}
+
+template <typename R>
+int dispatch_dense(const FftAxis* ax, const C_t<R>* tw, int batch, int dir, bool real_in,
+                   const void* in, C_t<R>* scratch, C_t<R>* out, double scale, cudaStream_t st) {
+  if (!g_fast_enabled || !(ax[0].n == ax[1].n && ax[1].n == ax[2].n)) return 0;
+  switch (ax[0].n) {
+    case 16: return dense_dir<R, 16>(tw, batch, dir, real_in, in, scratch, out, scale, st);
+    case 24: return dense_dir<R, 24>(tw, batch, dir, real_in, in, scratch, out, scale, st);
+    case 27: return dense_dir<R, 27>(tw, batch, dir, real_in, in, scratch, out, scale, st);
+    case 32: return dense_dir<R, 32>(tw, batch, dir, real_in, in, scratch, out, scale, st);
+    case 36: return dense_dir<R, 36>(tw, batch, dir, real_in, in, scratch, out, scale, st);
+    case 48: return dense_dir<R, 48>(tw, batch, dir, real_in, in, scratch, out, scale, st);
+    case 64: return dense_dir<R, 64>(tw, batch, dir, real_in, in, scratch, out, scale, st);
+    case 96: return dense_dir<R, 96>(tw, batch, dir, real_in, in, scratch, out, scale, st);
+    default: return 0;
+  }
+}
+
+template int dispatch_dense<float>(const FftAxis*, const C_t<float>*, int, int, bool, const void*,
+                                   C_t<float>*, C_t<float>*, double, cudaStream_t);
+template int dispatch_dense<double>(const FftAxis*, const C_t<double>*, int, int, bool, const void*,
+                                    C_t<double>*, C_t<double>*, double, cudaStream_t);
 
 }  // namespace fast
 }  // namespace jrg

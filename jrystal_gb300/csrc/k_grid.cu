@@ -82,6 +82,44 @@ __device__ __forceinline__ void lda_eps_v(double rho, int xc, double* eps, doubl
   *v = vv;
 }
 
+// FP32 path: rho^(1/3) from cbrtf refined by one Newton step in FP64 (the
+// exchange term dominates E_xc), the VWN correlation (about 1% of it) in FP32.
+__device__ __forceinline__ void lda_eps_v_f32(float rho, int xc, double* eps, double* v) {
+  double e = 0.0, vv = 0.0;
+  if (rho > 1e-15f) {
+    double y = (double)cbrtf(rho);
+    y -= (y * y * y - (double)rho) / (3.0 * y * y);
+    if (xc & JRG_XC_LDA_X) {
+      const double ex = -0.7385587663820224 * y;   // (3/4) (3/pi)^(1/3) rho^(1/3)
+      e += ex;
+      vv += 4.0 / 3.0 * ex;
+    }
+    if (xc & JRG_XC_LDA_C_VWN) {
+      const float A = 0.0310907f, b = 3.72744f, c = 12.9352f, x0 = -0.10498f;
+      const float q = 6.15199081975907951f;        // sqrt(4c - b^2)
+      const float xx0 = x0 * x0 + b * x0 + c;
+      const float rs = (float)(0.62035049089940001 / y);   // (3/(4 pi))^(1/3) / rho^(1/3)
+      const float x = sqrtf(rs);
+      const float xx = x * x + b * x + c;
+      const float at = atanf(q / (2.0f * x + b));
+      const float ec = A * (logf(x * x / xx) + 2.0f * b / q * at -
+                            b * x0 / xx0 * (logf((x - x0) * (x - x0) / xx) + 2.0f * (b + 2.0f * x0) / q * at));
+      const float den = (2.0f * x + b) * (2.0f * x + b) + q * q;
+      const float dec = A * (2.0f / x - (2.0f * x + b) / xx - 4.0f * b / den -
+                             b * x0 / xx0 * (2.0f / (x - x0) - (2.0f * x + b) / xx - 4.0f * (b + 2.0f * x0) / den));
+      e += ec;
+      vv += (double)(ec - x / 6.0f * dec);
+    }
+  }
+  *eps = e;
+  *v = vv;
+}
+
+template <typename R> __device__ __forceinline__ void lda_eps_v_t(R rho, int xc, double* eps, double* v) {
+  if constexpr (sizeof(R) == 4) lda_eps_v_f32(rho, xc, eps, v);
+  else lda_eps_v(rho, xc, eps, v);
+}
+
 // V(r) = Re(vri)*vscale + v_xc(rho) (when vr is given);  E_xc = vol/N * sum eps(rho) rho.
 template <typename R>
 __global__ void __launch_bounds__(256) k_potential(const R* __restrict__ rho,
@@ -92,9 +130,10 @@ __global__ void __launch_bounds__(256) k_potential(const R* __restrict__ rho,
   double ex = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
        i += (long long)gridDim.x * blockDim.x) {
-    const double r = rho[i];
+    const R rr = rho[i];
+    const double r = rr;
     double eps, v;
-    lda_eps_v(r, xc, &eps, &v);
+    lda_eps_v_t<R>(rr, xc, &eps, &v);
     ex += eps * r;
     if (vr) vr[i] = (R)((double)vri[i].x * vscale + v);
   }
@@ -109,7 +148,7 @@ __global__ void k_xc_field(const R* __restrict__ rho, R* __restrict__ out, long 
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
        i += (long long)gridDim.x * blockDim.x) {
     double eps, v;
-    lda_eps_v((double)rho[i], xc, &eps, &v);
+    lda_eps_v_t<R>(rho[i], xc, &eps, &v);
     out[i] = (R)(kohn_sham ? v : eps);
   }
 }
@@ -148,12 +187,12 @@ __global__ void __launch_bounds__(256) k_kinetic(const C_t<R>* __restrict__ coef
   const int k = (band / nb) % nk;
   const C_t<R>* c = coef + (size_t)band * ng;
   const double* t = tk + (size_t)k * ng;
-  double acc = 0.0;
+  R part = (R)0;
   for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-    const double x = c[g].x, y = c[g].y;
-    acc += t[g] * (x * x + y * y);
+    const R x = c[g].x, y = c[g].y;
+    part += (R)t[g] * (x * x + y * y);
   }
-  acc = block_sum(acc, red);
+  const double acc = block_sum((double)part, red);
   if (threadIdx.x == 0) slot[band] = acc * occ[band];
 }
 
@@ -433,6 +472,11 @@ int launch_adam(void* p, const void* g, void* m, void* v, const float* scale, lo
       reinterpret_cast<R*>(v), scale, n, (R)lr, (R)b1, (R)b2, (R)c1, (R)c2, (R)eps);
   JRG_LAUNCH_CHECK("k_adam");
   return JRG_OK;
+}
+
+int launch_lda(int prec, long long n, int xc, int ks, const void* rho, void* out, cudaStream_t st) {
+  if (prec == 64) return launch_xc_field<double>(rho, out, n, xc, ks, st);
+  return launch_xc_field<float>(rho, out, n, xc, ks, st);
 }
 
 int launch_twiddles(int n, int prec, void* out, cudaStream_t st) {

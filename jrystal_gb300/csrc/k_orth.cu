@@ -8,6 +8,7 @@
 // strict upper triangle of A with Re(diag A) on the diagonal,
 //   g_W = g_C R^{-H} - C (K R^{-H}),  dE/dw_re = 2 Re g_W, dE/dw_im = 2 Im g_W.
 // The internal coefficient layout is band-major: [sk][band][G] complex.
+#include <type_traits>
 #include "plan.h"
 
 namespace jrg {
@@ -69,66 +70,96 @@ __global__ void k_unpack(const C_t<R>* __restrict__ in, R* __restrict__ o_re, R*
   }
 }
 
-// Partial Gram S[i][j] = sum_g conj(X[i][g]) Y[j][g] over one G split, for a
-// 32x32 output tile.  Products and 64-term runs in precision R, runs summed
-// in FP64.
+// Input layouts of the tall [G x B] operands:
+//   LAYOUT_SPLIT: two real arrays (re, im) indexed [sk][g][b] (the parameter layout)
+//   LAYOUT_BAND:  one complex array indexed [sk][b][g] (internal coefficient layout)
+enum Layout { LAYOUT_SPLIT = 0, LAYOUT_BAND = 1 };
+
+template <typename R, int LAYOUT>
+__device__ __forceinline__ C_t<R> load_tall(const void* __restrict__ p0, const void* __restrict__ p1,
+                                            size_t sk, int i, int g, int ng, int nb) {
+  if constexpr (LAYOUT == LAYOUT_SPLIT) {
+    const size_t o = (sk * ng + g) * nb + i;
+    C_t<R> v;
+    v.x = reinterpret_cast<const R*>(p0)[o];
+    v.y = reinterpret_cast<const R*>(p1)[o];
+    return v;
+  } else {
+    return reinterpret_cast<const C_t<R>*>(p0)[(sk * nb + i) * ng + g];
+  }
+}
+
+// Partial Gram S[i][j] = sum_g conj(X[i][g]) Y[j][g] over one G split for a
+// 32x32 output tile; 16x16 threads, each a 2x2 block (rows ty, ty+16; columns
+// tx, tx+16).  Products and chunk-long runs in precision R, runs summed in FP64.
 constexpr int kGramTile = 32;
 template <typename R> struct GramChunk { static constexpr int value = 64; };
 template <> struct GramChunk<double> { static constexpr int value = 32; };  // 48 KB static smem
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_gram_partial(const C_t<R>* __restrict__ X,
-                                                      const C_t<R>* __restrict__ Y,
+template <typename R, int LX, int LY>
+__global__ void __launch_bounds__(256) k_gram_partial(const void* __restrict__ X0,
+                                                      const void* __restrict__ X1,
+                                                      const void* __restrict__ Y0,
+                                                      const void* __restrict__ Y1,
                                                       double2* __restrict__ part, int ng, int nb,
                                                       int split_len) {
   using C = C_t<R>;
-  constexpr int kGramChunk = GramChunk<R>::value;
-  __shared__ C xs[kGramTile][kGramChunk + 1];
-  __shared__ C ys[kGramTile][kGramChunk + 1];
+  constexpr int CH = GramChunk<R>::value;
+  __shared__ C xs[kGramTile][CH + 1];
+  __shared__ C ys[kGramTile][CH + 1];
   const int split = blockIdx.x;
   const int ntile = (nb + kGramTile - 1) / kGramTile;
   const int ti = blockIdx.y / ntile, tj = blockIdx.y % ntile;
-  const int sk = blockIdx.z;
+  const size_t sk = blockIdx.z;
   const int nsplit = gridDim.x;
-  const C* Xs = X + (size_t)sk * nb * ng;
-  const C* Ys = Y + (size_t)sk * nb * ng;
   const int g_begin = split * split_len;
   const int g_end = min(ng, g_begin + split_len);
-  // each thread owns 4 outputs: (i, j) = (ty + 8*q, tx) with tx < 32, ty < 8
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  double2 acc[4];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double2 acc[2][2];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) acc[q] = make_double2(0.0, 0.0);
-  for (int g0 = g_begin; g0 < g_end; g0 += kGramChunk) {
-    for (int idx = threadIdx.x; idx < kGramTile * kGramChunk; idx += blockDim.x) {
-      const int r = idx / kGramChunk, c = idx % kGramChunk;
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) acc[a][b] = make_double2(0.0, 0.0);
+  const C z0 = czero<C>();
+  for (int g0 = g_begin; g0 < g_end; g0 += CH) {
+    for (int idx = threadIdx.x; idx < kGramTile * CH; idx += blockDim.x) {
+      int r, c;
+      if (LX == LAYOUT_SPLIT) { r = idx % kGramTile; c = idx / kGramTile; }
+      else { c = idx % CH; r = idx / CH; }
       const int g = g0 + c;
       const int bi = ti * kGramTile + r, bj = tj * kGramTile + r;
-      xs[r][c] = (g < g_end && bi < nb) ? Xs[(size_t)bi * ng + g] : czero<C>();
-      ys[r][c] = (g < g_end && bj < nb) ? Ys[(size_t)bj * ng + g] : czero<C>();
+      xs[r][c] = (g < g_end && bi < nb) ? load_tall<R, LX>(X0, X1, sk, bi, g, ng, nb) : z0;
+      ys[r][c] = (g < g_end && bj < nb) ? load_tall<R, LY>(Y0, Y1, sk, bj, g, ng, nb) : z0;
     }
     __syncthreads();
+    C s[2][2];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int i = ty + 8 * q;
-      C s = czero<C>();
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) s[a][b] = z0;
 #pragma unroll 8
-      for (int c = 0; c < kGramChunk; ++c) {
-        const C a = xs[i][c], b = ys[tx][c];
-        // conj(a) * b
-        s.x += a.x * b.x + a.y * b.y;
-        s.y += a.x * b.y - a.y * b.x;
-      }
-      acc[q].x += (double)s.x;
-      acc[q].y += (double)s.y;
+    for (int c = 0; c < CH; ++c) {
+      const C x0 = xs[ty][c], x1 = xs[ty + 16][c];
+      const C y0 = ys[tx][c], y1 = ys[tx + 16][c];
+      // conj(x) * y
+      s[0][0].x += x0.x * y0.x + x0.y * y0.y; s[0][0].y += x0.x * y0.y - x0.y * y0.x;
+      s[0][1].x += x0.x * y1.x + x0.y * y1.y; s[0][1].y += x0.x * y1.y - x0.y * y1.x;
+      s[1][0].x += x1.x * y0.x + x1.y * y0.y; s[1][0].y += x1.x * y0.y - x1.y * y0.x;
+      s[1][1].x += x1.x * y1.x + x1.y * y1.y; s[1][1].y += x1.x * y1.y - x1.y * y1.x;
     }
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) { acc[a][b].x += (double)s[a][b].x; acc[a][b].y += (double)s[a][b].y; }
     __syncthreads();
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int i = ti * kGramTile + ty + 8 * q, j = tj * kGramTile + tx;
-    if (i < nb && j < nb) part[(((size_t)sk * nsplit + split) * nb + i) * nb + j] = acc[q];
-  }
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const int i = ti * kGramTile + ty + 16 * a, j = tj * kGramTile + tx + 16 * b;
+      if (i < nb && j < nb) part[((sk * nsplit + split) * nb + i) * nb + j] = acc[a][b];
+    }
 }
 
 __global__ void k_gram_reduce(const double2* __restrict__ part, double2* __restrict__ out,
@@ -146,25 +177,28 @@ __global__ void k_gram_reduce(const double2* __restrict__ part, double2* __restr
   }
 }
 
-// One CTA per (s,k): R = chol(S) (upper, S = R^H R) and Rinv = R^{-1}.
-// Works in global memory (B x B double2).  A non-positive or non-finite
-// pivot sets flags[0] |= 1 and continues with a unit pivot.
+// One CTA per (s,k): R = chol(S) (upper, S = R^H R) and Rinv = R^{-1}, in
+// FP64.  A non-positive or non-finite pivot sets flags[0] |= 1 and continues
+// with a unit pivot.  The matrices live in shared memory when SMEM (nb <= 64)
+// and in the output buffers otherwise.
+template <bool SMEM>
 __global__ void __launch_bounds__(256) k_cholesky_inv(const double2* __restrict__ S,
                                                       double2* __restrict__ Rm,
                                                       double2* __restrict__ Ri, int nb,
                                                       int* __restrict__ flags) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int sk = blockIdx.x;
   const size_t off = (size_t)sk * nb * nb;
   const double2* s = S + off;
-  double2* r = Rm + off;
-  double2* ri = Ri + off;
+  double2* r = SMEM ? reinterpret_cast<double2*>(smem_raw) : Rm + off;
+  double2* ri = SMEM ? r + nb * nb : Ri + off;
+  __shared__ double piv;
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int i = e / nb, j = e % nb;
     // Hermitian symmetrisation of the accumulated Gram
     const double2 a = s[i * nb + j], b = s[j * nb + i];
     r[e] = (j >= i) ? make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)) : make_double2(0.0, 0.0);
   }
-  __shared__ double piv;
   __syncthreads();
   for (int k = 0; k < nb; ++k) {
     if (threadIdx.x == 0) {
@@ -211,6 +245,87 @@ __global__ void __launch_bounds__(256) k_cholesky_inv(const double2* __restrict_
       ri[i * nb + j] = make_double2(-sx / dii, -sy / dii);
     }
   }
+  if (SMEM) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+      Rm[off + e] = r[e];
+      Ri[off + e] = ri[e];
+    }
+  }
+}
+
+// 1/sqrt(d) for d > 0 without the FP64 square-root/division sequences:
+// FP32 seed refined by three Newton steps in FP64 (multiplies and adds only).
+__device__ __forceinline__ double rsqrt_fp64(double d) {
+  double r = (double)rsqrtf((float)d);
+  r = r * (1.5 - 0.5 * d * r * r);
+  r = r * (1.5 - 0.5 * d * r * r);
+  r = r * (1.5 - 0.5 * d * r * r);
+  return r;
+}
+
+// nb <= 32: one warp per (s,k), lane j owns column j of R (in shared memory);
+// pivots broadcast with shuffles, no block barriers, no FP64 divisions.
+__global__ void __launch_bounds__(32) k_cholesky_inv_warp(const double2* __restrict__ S,
+                                                          double2* __restrict__ Rm,
+                                                          double2* __restrict__ Ri, int nb,
+                                                          int* __restrict__ flags) {
+  __shared__ double2 r[32][33];
+  __shared__ double2 ri[32][33];
+  __shared__ double dinv[32];
+  const int sk = blockIdx.x, j = threadIdx.x;
+  const size_t off = (size_t)sk * nb * nb;
+  const double2* s = S + off;
+  for (int i = 0; i < nb; ++i) {
+    if (j < nb) {
+      const double2 a = s[i * nb + j], b = s[j * nb + i];
+      r[i][j] = (j >= i) ? make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)) : make_double2(0.0, 0.0);
+    }
+  }
+  __syncwarp();
+  bool bad = false;
+  for (int k = 0; k < nb; ++k) {
+    double d = r[k][k].x;   // every lane reads the pivot
+    if (!(d > 0.0) || !isfinite(d)) { bad = true; d = 1.0; }
+    const double rs = rsqrt_fp64(d);
+    __syncwarp();
+    if (j == k) { r[k][k] = make_double2(d * rs, 0.0); dinv[k] = rs; }
+    if (j > k && j < nb) { const double2 v = r[k][j]; r[k][j] = make_double2(v.x * rs, v.y * rs); }
+    __syncwarp();
+    if (j > k && j < nb) {
+      const double2 b = r[k][j];
+      for (int i = k + 1; i <= j; ++i) {
+        const double2 a = r[k][i];
+        double2 v = r[i][j];
+        v.x -= a.x * b.x + a.y * b.y;
+        v.y -= a.x * b.y - a.y * b.x;
+        r[i][j] = v;
+      }
+    }
+    __syncwarp();
+  }
+  if (bad && j == 0) atomicOr(flags, 1);
+  // column j of R^{-1} by back substitution with the stored reciprocal pivots
+  if (j < nb) {
+    for (int i = 0; i < nb; ++i) ri[i][j] = make_double2(0.0, 0.0);
+    ri[j][j] = make_double2(dinv[j], 0.0);
+    for (int i = j - 1; i >= 0; --i) {
+      double sx = 0.0, sy = 0.0;
+      for (int l = i + 1; l <= j; ++l) {
+        const double2 a = r[i][l], b = ri[l][j];
+        sx += a.x * b.x - a.y * b.y;
+        sy += a.x * b.y + a.y * b.x;
+      }
+      ri[i][j] = make_double2(-sx * dinv[i], -sy * dinv[i]);
+    }
+  }
+  __syncwarp();
+  for (int i = 0; i < nb; ++i) {
+    if (j < nb) {
+      Rm[off + i * nb + j] = r[i][j];
+      Ri[off + i * nb + j] = ri[i][j];
+    }
+  }
 }
 
 // Adjoint small matrices per (s,k), one CTA each:
@@ -245,28 +360,29 @@ __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict
   }
 }
 
-// out[sk][j][g] (band-major) or (S,K,G,B) layouts of sum_t X_t[sk][i][g] M_t[sk][i][j].
-// Thread per g, 16-wide j tile; M tile staged in shared memory in precision R.
-constexpr int kRotJ = 16;
+// out = sum_t X_t M_t with X_t [G x B] tall (layout LX0 / LX1) and M_t
+// [B x B] FP64; output band-major complex, (S,K,G,B) complex, or (S,K,G,B)
+// split real/imag times fac.  Thread per g, J-wide column tile; the M tile is
+// staged in shared memory in precision R.
 enum RotOut { ROT_BANDMAJOR = 0, ROT_GMAJOR_C = 1, ROT_GMAJOR_SPLIT = 2 };
 
-template <typename R, int OUT>
-__global__ void __launch_bounds__(256) k_rotate(const C_t<R>* __restrict__ X0,
+template <typename R, int OUT, int J, int LX0, int LX1>
+__global__ void __launch_bounds__(256) k_rotate(const void* __restrict__ X0a, const void* __restrict__ X0b,
                                                 const double2* __restrict__ M0,
-                                                const C_t<R>* __restrict__ X1,
+                                                const void* __restrict__ X1a, const void* __restrict__ X1b,
                                                 const double2* __restrict__ M1, void* out0,
                                                 void* out1, int ng, int nb, R fac) {
   using C = C_t<R>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* ms = reinterpret_cast<C*>(smem_raw);   // [nterms][nb][kRotJ]
-  const int sk = blockIdx.z;
-  const int j0 = blockIdx.y * kRotJ;
-  const int nj = min(kRotJ, nb - j0);
-  const int nterms = X1 ? 2 : 1;
-  const size_t moff = (size_t)sk * nb * nb;
-  for (int e = threadIdx.x; e < nterms * nb * kRotJ; e += blockDim.x) {
-    const int t = e / (nb * kRotJ), rem = e % (nb * kRotJ);
-    const int i = rem / kRotJ, jj = rem % kRotJ;
+  C* ms = reinterpret_cast<C*>(smem_raw);   // [nterms][nb][J]
+  const size_t sk = blockIdx.z;
+  const int j0 = blockIdx.y * J;
+  const int nj = min(J, nb - j0);
+  const int nterms = X1a ? 2 : 1;
+  const size_t moff = sk * nb * nb;
+  for (int e = threadIdx.x; e < nterms * nb * J; e += blockDim.x) {
+    const int t = e / (nb * J), rem = e % (nb * J);
+    const int i = rem / J, jj = rem % J;
     const double2* M = t ? M1 : M0;
     double2 v = (jj < nj) ? M[moff + (size_t)i * nb + j0 + jj] : make_double2(0.0, 0.0);
     ms[e] = cmk<C>(v.x, v.y);
@@ -274,38 +390,40 @@ __global__ void __launch_bounds__(256) k_rotate(const C_t<R>* __restrict__ X0,
   __syncthreads();
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ng) return;
-  C acc[kRotJ];
+  C acc[J];
 #pragma unroll
-  for (int jj = 0; jj < kRotJ; ++jj) acc[jj] = czero<C>();
-  for (int t = 0; t < nterms; ++t) {
-    const C* X = (t ? X1 : X0) + (size_t)sk * nb * ng;
-    const C* mt = ms + (size_t)t * nb * kRotJ;
+  for (int jj = 0; jj < J; ++jj) acc[jj] = czero<C>();
+  auto term = [&](auto lx, const void* xa, const void* xb, const C* mt) {
+    constexpr int L = decltype(lx)::value;
+#pragma unroll 4
     for (int i = 0; i < nb; ++i) {
-      const C x = X[(size_t)i * ng + g];
+      const C x = load_tall<R, L>(xa, xb, sk, i, g, ng, nb);
 #pragma unroll
-      for (int jj = 0; jj < kRotJ; ++jj) {
-        const C m = mt[i * kRotJ + jj];
+      for (int jj = 0; jj < J; ++jj) {
+        const C m = mt[i * J + jj];
         acc[jj].x = fma(x.x, m.x, fma(-x.y, m.y, acc[jj].x));
         acc[jj].y = fma(x.x, m.y, fma(x.y, m.x, acc[jj].y));
       }
     }
-  }
-  const size_t base = (size_t)sk * nb * ng;
+  };
+  term(std::integral_constant<int, LX0>{}, X0a, X0b, ms);
+  if (nterms > 1) term(std::integral_constant<int, LX1>{}, X1a, X1b, ms + (size_t)nb * J);
+  const size_t base = sk * nb * ng;
   if (OUT == ROT_BANDMAJOR) {
     C* o = reinterpret_cast<C*>(out0) + base;
 #pragma unroll
-    for (int jj = 0; jj < kRotJ; ++jj)
+    for (int jj = 0; jj < J; ++jj)
       if (jj < nj) o[(size_t)(j0 + jj) * ng + g] = acc[jj];
   } else if (OUT == ROT_GMAJOR_C) {
     C* o = reinterpret_cast<C*>(out0) + base + (size_t)g * nb + j0;
 #pragma unroll
-    for (int jj = 0; jj < kRotJ; ++jj)
+    for (int jj = 0; jj < J; ++jj)
       if (jj < nj) o[jj] = acc[jj];
   } else {
     R* ore = reinterpret_cast<R*>(out0) + base + (size_t)g * nb + j0;
     R* oim = reinterpret_cast<R*>(out1) + base + (size_t)g * nb + j0;
 #pragma unroll
-    for (int jj = 0; jj < kRotJ; ++jj)
+    for (int jj = 0; jj < J; ++jj)
       if (jj < nj) { ore[jj] = fac * acc[jj].x; oim[jj] = fac * acc[jj].y; }
   }
 }
@@ -345,14 +463,17 @@ int launch_unpack(const void* in, void* o_re, void* o_im, void* o_c, int nsk, in
 }
 
 template <typename R>
-int launch_gram(const void* X, const void* Y, double2* part, double2* out, int nsk, int ng, int nb,
-                int nsplit, cudaStream_t st) {
+int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, const void* Y1,
+                double2* part, double2* out, int nsk, int ng, int nb, int nsplit, cudaStream_t st) {
   const int split_len = (ng + nsplit - 1) / nsplit;
   const int ntile = (nb + kGramTile - 1) / kGramTile;
   dim3 grid(nsplit, ntile * ntile, nsk);
-  k_gram_partial<R><<<grid, 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(X),
-                                          reinterpret_cast<const C_t<R>*>(Y), part, ng, nb,
-                                          split_len);
+  if (lx == LAYOUT_SPLIT && ly == LAYOUT_SPLIT)
+    k_gram_partial<R, LAYOUT_SPLIT, LAYOUT_SPLIT><<<grid, 256, 0, st>>>(X0, X1, Y0, Y1, part, ng, nb, split_len);
+  else if (lx == LAYOUT_BAND && ly == LAYOUT_BAND)
+    k_gram_partial<R, LAYOUT_BAND, LAYOUT_BAND><<<grid, 256, 0, st>>>(X0, X1, Y0, Y1, part, ng, nb, split_len);
+  else
+    return fail(JRG_ERR_INVALID, "launch_gram: unsupported layout pair");
   JRG_LAUNCH_CHECK("k_gram_partial");
   const size_t n = (size_t)nsk * nb * nb;
   k_gram_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, out, nsplit, nb, nsk);
@@ -362,7 +483,18 @@ int launch_gram(const void* X, const void* Y, double2* part, double2* out, int n
 
 int launch_cholesky_inv(const double2* S, double2* Rm, double2* Ri, int nsk, int nb, int* flags,
                         cudaStream_t st) {
-  k_cholesky_inv<<<nsk, 256, 0, st>>>(S, Rm, Ri, nb, flags);
+  if (nb <= 32) {
+    k_cholesky_inv_warp<<<nsk, 32, 0, st>>>(S, Rm, Ri, nb, flags);
+  } else if (nb <= 64) {
+    const size_t sm = 2 * sizeof(double2) * (size_t)nb * nb;
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k_cholesky_inv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(cholesky)");
+    }
+    k_cholesky_inv<true><<<nsk, 256, sm, st>>>(S, Rm, Ri, nb, flags);
+  } else {
+    k_cholesky_inv<false><<<nsk, 256, 0, st>>>(S, Rm, Ri, nb, flags);
+  }
   JRG_LAUNCH_CHECK("k_cholesky_inv");
   return JRG_OK;
 }
@@ -374,27 +506,48 @@ int launch_adjoint_small(const double2* A, const double2* Ri, double2* Rh, doubl
   return JRG_OK;
 }
 
-template <typename R>
-int launch_rotate(int out_kind, const void* X0, const double2* M0, const void* X1,
-                  const double2* M1, void* out0, void* out1, int nsk, int ng, int nb, double fac,
-                  cudaStream_t st) {
+template <typename R, int OUT, int J>
+static int rotate_j(int lx0, const void* X0a, const void* X0b, const double2* M0, int lx1,
+                    const void* X1a, const void* X1b, const double2* M1, void* out0, void* out1,
+                    int nsk, int ng, int nb, double fac, cudaStream_t st) {
   using C = C_t<R>;
-  const int nterms = X1 ? 2 : 1;
-  const size_t sm = sizeof(C) * (size_t)nterms * nb * kRotJ;
-  dim3 grid((ng + 255) / 256, (nb + kRotJ - 1) / kRotJ, nsk);
+  const int nterms = X1a ? 2 : 1;
+  const size_t sm = sizeof(C) * (size_t)nterms * nb * J;
+  dim3 grid((ng + 255) / 256, (nb + J - 1) / J, nsk);
   auto go = [&](auto kern) -> int {
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate)");
     }
-    kern<<<grid, 256, sm, st>>>(reinterpret_cast<const C*>(X0), M0, reinterpret_cast<const C*>(X1),
-                                M1, out0, out1, ng, nb, (R)fac);
+    kern<<<grid, 256, sm, st>>>(X0a, X0b, M0, X1a, X1b, M1, out0, out1, ng, nb, (R)fac);
     JRG_LAUNCH_CHECK("k_rotate");
     return JRG_OK;
   };
-  if (out_kind == ROT_BANDMAJOR) return go(k_rotate<R, ROT_BANDMAJOR>);
-  if (out_kind == ROT_GMAJOR_C) return go(k_rotate<R, ROT_GMAJOR_C>);
-  return go(k_rotate<R, ROT_GMAJOR_SPLIT>);
+  if (lx0 == LAYOUT_SPLIT) return go(k_rotate<R, OUT, J, LAYOUT_SPLIT, LAYOUT_BAND>);
+  return go(k_rotate<R, OUT, J, LAYOUT_BAND, LAYOUT_BAND>);
+}
+
+template <typename R, int OUT>
+static int rotate_out(int lx0, const void* X0a, const void* X0b, const double2* M0, int lx1,
+                      const void* X1a, const void* X1b, const double2* M1, void* out0, void* out1,
+                      int nsk, int ng, int nb, double fac, cudaStream_t st) {
+  if (nb <= 8) return rotate_j<R, OUT, 8>(lx0, X0a, X0b, M0, lx1, X1a, X1b, M1, out0, out1, nsk, ng, nb, fac, st);
+  if (nb <= 16) return rotate_j<R, OUT, 16>(lx0, X0a, X0b, M0, lx1, X1a, X1b, M1, out0, out1, nsk, ng, nb, fac, st);
+  if (nb <= 24) return rotate_j<R, OUT, 24>(lx0, X0a, X0b, M0, lx1, X1a, X1b, M1, out0, out1, nsk, ng, nb, fac, st);
+  return rotate_j<R, OUT, 32>(lx0, X0a, X0b, M0, lx1, X1a, X1b, M1, out0, out1, nsk, ng, nb, fac, st);
+}
+
+// out_kind: ROT_*; lx0: layout of X0 (split: X0a=re, X0b=im; band: X0a); X1 is band-major
+template <typename R>
+int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const double2* M0,
+                  const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng, int nb,
+                  double fac, cudaStream_t st) {
+  if (X1 && lx0 != LAYOUT_BAND) return fail(JRG_ERR_INVALID, "launch_rotate: two-term form needs band-major inputs");
+  if (out_kind == ROT_BANDMAJOR)
+    return rotate_out<R, ROT_BANDMAJOR>(lx0, X0a, X0b, M0, LAYOUT_BAND, X1, nullptr, M1, out0, out1, nsk, ng, nb, fac, st);
+  if (out_kind == ROT_GMAJOR_C)
+    return rotate_out<R, ROT_GMAJOR_C>(lx0, X0a, X0b, M0, LAYOUT_BAND, X1, nullptr, M1, out0, out1, nsk, ng, nb, fac, st);
+  return rotate_out<R, ROT_GMAJOR_SPLIT>(lx0, X0a, X0b, M0, LAYOUT_BAND, X1, nullptr, M1, out0, out1, nsk, ng, nb, fac, st);
 }
 
 #define JRG_INST_ORTH(R)                                                                        \
@@ -402,10 +555,10 @@ int launch_rotate(int out_kind, const void* X0, const double2* M0, const void* X
                                      cudaStream_t);                                             \
   template int launch_unpack<R>(const void*, void*, void*, void*, int, int, int, double,          \
                                 cudaStream_t);                                                  \
-  template int launch_gram<R>(const void*, const void*, double2*, double2*, int, int, int, int,   \
-                              cudaStream_t);                                                    \
-  template int launch_rotate<R>(int, const void*, const double2*, const void*, const double2*,    \
-                                void*, void*, int, int, int, double, cudaStream_t);
+  template int launch_gram<R>(int, const void*, const void*, int, const void*, const void*,       \
+                              double2*, double2*, int, int, int, int, cudaStream_t);            \
+  template int launch_rotate<R>(int, int, const void*, const void*, const double2*, const void*,  \
+                                const double2*, void*, void*, int, int, int, double, cudaStream_t);
 JRG_INST_ORTH(float)
 JRG_INST_ORTH(double)
 

@@ -1,0 +1,150 @@
+"""jrystal-compatible modules (pw, energy, potential, hamiltonian, braket,
+ewald, occupation, autograd binding, driver) against the oracle."""
+import numpy as np
+import pytest
+
+from oracle import restatement as R
+from tests.systems import make_system, random_params
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case():
+  import torch
+  import jrystal_gb300 as jr
+  jr.set_precision(64)
+  sysm = make_system(kind="si2", grid=(16, 16, 16), kgrid=(2, 1, 1), nb=4, nocc=2)
+  wr, wi = random_params(sysm, seed=3)
+  params = {"w_re": torch.tensor(wr, device="cuda"), "w_im": torch.tensor(wi, device="cuda")}
+  return sysm, wr, wi, params
+
+
+def _np(t):
+  return t.detach().cpu().numpy()
+
+
+def test_pw_coeff_wave_and_density(case):
+  import jrystal_gb300 as jr
+  sysm, wr, wi, params = case
+  c = jr.pw.coeff(params, sysm.mask)
+  dense = R.coeff(wr, wi, sysm.mask)
+  # columns agree up to a unit phase per band
+  ph = np.einsum("skbxyz,skbxyz->skb", dense.conj(), _np(c))
+  np.testing.assert_allclose(np.abs(ph), 1.0, atol=1e-10)
+  rho = jr.pw.density_grid(c, sysm.vol, sysm.occupation)
+  np.testing.assert_allclose(_np(rho), R.density_grid(dense, sysm.vol, sysm.occupation), atol=1e-12)
+  rho_g = jr.pw.density_grid_reciprocal(c, sysm.vol, sysm.occupation)
+  np.testing.assert_allclose(_np(rho_g), R.density_grid_reciprocal(dense, sysm.vol, sysm.occupation),
+                             atol=1e-10)
+  w = jr.pw.wave_grid(c, sysm.vol)
+  np.testing.assert_allclose(np.abs(_np(w)), np.abs(R.wave_grid(dense, sysm.vol)), atol=1e-10)
+  # fused sphere density equals the dense path at vol = 1
+  cs = jr.pw.coeff_sphere(params, sysm.mask)
+  rs = jr.pw.density_from_sphere(cs, sysm.mask, sysm.occupation)
+  np.testing.assert_allclose(_np(rs), R.density_grid(dense, 1.0, sysm.occupation), atol=1e-11)
+
+
+def test_energy_terms_and_total(case):
+  import jrystal_gb300 as jr
+  sysm, wr, wi, params = case
+  c = jr.pw.coeff(params, sysm.mask)
+  g = sysm.g_vector_grid
+  terms = jr.energy.total_energy(c, sysm.positions, sysm.charges, g, sysm.kpts, sysm.vol,
+                                 sysm.occupation, xc=sysm.xc, split=True)
+  ref = R.energy_terms(wr, wi, sysm, with_grad=False)
+  for got, name in zip(terms, ["kinetic", "external", "hartree", "xc"]):
+    assert abs(float(got) - ref[name]) < 1e-9 * max(1, abs(ref[name])), name
+  rho = jr.pw.density_grid(c, sysm.vol, sysm.occupation)
+  e_xc = jr.energy.xc_energy(rho, g, sysm.vol, sysm.xc)
+  assert abs(float(e_xc) - ref["xc"]) < 1e-9 * abs(ref["xc"])
+
+
+def test_effective_potential_and_ks_trace(case):
+  import jrystal_gb300 as jr
+  sysm, wr, wi, params = case
+  c = jr.pw.coeff(params, sysm.mask)
+  g = sysm.g_vector_grid
+  occ = np.ones(sysm.occupation.shape)
+  rho = jr.pw.density_grid(c, sysm.vol, occ)
+  vh, ve, vx = jr.potential.effective(rho, sysm.positions, sysm.charges, g, sysm.vol, split=True,
+                                      xc_type=sysm.xc, kohn_sham=True)
+  rh, re, rx = R.effective(_np(rho), sysm.positions, sysm.charges, g, sysm.vol, split=True,
+                           xc_type=sysm.xc, kohn_sham=True)
+  np.testing.assert_allclose(_np(vh), rh, atol=1e-10)
+  np.testing.assert_allclose(_np(ve), re, atol=1e-8)
+  np.testing.assert_allclose(_np(vx), rx, atol=1e-10)
+  # hamiltonian_test.py:78-102: KS trace == total_energy(kohn_sham=True)
+  e1 = jr.hamiltonian.hamiltonian_matrix_trace(c, sysm.positions, sysm.charges, rho, g, sysm.kpts,
+                                               sysm.vol, xc=sysm.xc, kohn_sham=True)
+  e2 = jr.energy.total_energy(c, sysm.positions, sysm.charges, g, sysm.kpts, sysm.vol,
+                              kohn_sham=True, xc=sysm.xc)
+  assert abs(float(e1) - float(e2)) < 1e-7
+  h = jr.hamiltonian.hamiltonian_matrix(c, sysm.positions, sysm.charges, rho, g, sysm.kpts,
+                                        sysm.vol, xc=sysm.xc, kohn_sham=True)
+  hn = _np(h)
+  np.testing.assert_allclose(hn, np.conj(np.swapaxes(hn, -1, -2)), atol=1e-9)   # Hermitian
+  np.testing.assert_allclose(np.einsum("skii->", hn).real, float(e1), atol=1e-9)
+
+
+def test_ewald_api(case):
+  import jrystal_gb300 as jr
+  sysm = case[0]
+  g = sysm.g_vector_grid
+  got = jr.energy.nuclear_repulsion(sysm.positions, sysm.charges, sysm.cell_vectors, g, sysm.vol,
+                                    0.1, 2e3)
+  ref = R.nuclear_repulsion(sysm.positions, sysm.charges, sysm.cell_vectors, g, sysm.vol, 0.1, 2e3)
+  assert abs(got - ref) < 1e-10 * abs(ref)
+
+
+def test_occupation_and_entropy():
+  import jrystal_gb300 as jr
+  u = jr.occupation.uniform(3, 8, num_bands=6)
+  np.testing.assert_allclose(_np(u), R.uniform_occupation(3, 8, num_bands=6))
+  gm = jr.occupation.gamma(3, 8, num_bands=6)
+  np.testing.assert_allclose(_np(gm), R.gamma_occupation(3, 8, num_bands=6))
+  s = jr.entropy.fermi_dirac(u)
+  assert abs(float(s) - R.fermi_dirac_entropy(_np(u))) < 1e-12
+  with pytest.raises(NotImplementedError):
+    jr.occupation.param_init(0, 4, 8, 1, method="idempotent")
+
+
+def test_autograd_binding_matches_oracle(case):
+  import torch
+  from jrystal_gb300.autograd import total_energy
+  from jrystal_gb300.engine import PlaneWavePlan
+  sysm, wr, wi, _ = case
+  plan = PlaneWavePlan(sysm.cell_vectors, sysm.positions, sysm.charges, sysm.grid, sysm.mask,
+                       sysm.kpts, 4, 1, 64, sysm.xc)
+  a = torch.tensor(wr, device="cuda", requires_grad=True)
+  b = torch.tensor(wi, device="cuda", requires_grad=True)
+  e = total_energy(a, b, plan, sysm.occupation)
+  e.backward()
+  terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+  assert abs(float(e) - terms["total"]) < 1e-9 * abs(terms["total"])
+  np.testing.assert_allclose(_np(a.grad), gr, atol=1e-9 * np.abs(gr).max())
+  np.testing.assert_allclose(_np(b.grad), gi, atol=1e-9 * np.abs(gi).max())
+
+
+def test_driver_decreases_energy_and_matches_oracle_at_the_end(tmp_path):
+  import jrystal_gb300 as jr
+  xyz = tmp_path / "si.xyz"
+  a = 10.26 * 0.529177249
+  xyz.write_text("2\nLattice=\"0 {0} {0} {0} 0 {0} {0} {0} 0\" Properties=species:S:1:pos:R:3\n"
+                 "Si 0 0 0\nSi {1} {1} {1}\n".format(a / 2, a / 4))
+  out = jr.calc.energy_all_electrons({
+    "crystal_file_path_path": str(xyz), "grid_sizes": 16, "k_grid_sizes": [1, 1, 1],
+    "cutoff_energy": 10.0, "epoch": 60, "convergence_condition": 1e-12, "empty_bands": 0,
+    "optimizer_args": {"learning_rate": 0.01, "b1": 0.9, "b2": 0.99}})
+  h = out.total_energy_history
+  assert h[-1] < h[0]
+  p = out.params_pw
+  c = out.crystal
+  mask = jr.grid.spherical_mask(c.cell_vectors, (16, 16, 16), 10.0)
+  kpts = jr.grid.k_vectors(c.cell_vectors, (1, 1, 1))
+  occ = np.zeros((1, 1, 14))
+  occ[..., :14] = 2.0
+  sysm = R.System(c.cell_vectors, c.positions, np.asarray(c.charges, float), (16, 16, 16), mask,
+                  kpts, occ, "lda_x+lda_c_vwn")
+  ref = R.energy_terms(_np(p["w_re"]), _np(p["w_im"]), sysm, with_grad=False)
+  assert abs(out.energy_terms["total"] - ref["total"]) < 1e-8 * abs(ref["total"])

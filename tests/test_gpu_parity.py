@@ -85,7 +85,7 @@ def test_coeff_orthonormal_and_density(prec):
 
 
 @pytest.mark.parametrize("prec", [64, 32])
-@pytest.mark.parametrize("grid", [(12, 12, 12), (7, 10, 12), (16, 9, 20), (24, 27, 32)])
+@pytest.mark.parametrize("grid", [(12, 12, 12), (7, 10, 12), (16, 9, 20), (24, 27, 32), (27, 27, 27), (64, 64, 64)])
 def test_fft3d(prec, grid):
   torch = _torch()
   from jrystal_gb300.engine import fft3d
