@@ -154,6 +154,32 @@ int jrg_adam_update(int precision, int64_t n, void* param, const void* grad, voi
 int jrg_ewald(const jrg_plan* plan, double eta, double cutoff, double* result,
               void* workspace, cudaStream_t stream);
 
+/* Learned diagonal preconditioner (no counterpart in the reference): an MLP
+ * 3-64-64-64-1 (GELU, softplus) of x1 = |G+k|^2/E_kin,band, x2 = band/B,
+ * x3 = step fraction, scaling each Adam update element.  Parameters: FP32
+ * master copy (w32) and BF16 copy (wb) of jrg_mlp_num_params() values in the
+ * order W1[64][3] b1 W2[64][64] b2 W3[64][64] b3 W4[64] b4.
+ * jrg_precond_scale writes scale[2][S][K][G][B] (the same scale for w_re and
+ * w_im of a coefficient, 1 for unoccupied bands, capped at smax) from the
+ * per-band kinetic energies of the last jrg_energy_grad on this workspace.
+ * jrg_mlp_train_eval runs the BF16/FP32 training forward over n records
+ * x[n][3] -> s[n] and, given the one-step model terms a[n], c[n] (weights wt
+ * optional), the summed loss sum wt (s a + s^2 c/2) and the gradient of its
+ * mean with respect to the FP32 parameters. */
+int jrg_mlp_num_params(void);
+int jrg_mlp_to_bf16(const float* w32, void* wb, cudaStream_t stream);
+int jrg_mlp_workspace_size(int n, size_t* bytes);
+int jrg_mlp_train_eval(int n, const float* x, const float* w32, const void* wb, const float* a,
+                       const float* c, const float* wt, float* s_out, double* loss, float* grad,
+                       void* workspace, cudaStream_t stream);
+int jrg_precond_scale(const jrg_plan* plan, const float* w32, const void* wb, float t_frac,
+                      float smax, const double* occupation, float* scale, void* workspace,
+                      cudaStream_t stream);
+/* Per-band kinetic energies sum_G |G+k|^2/2 |c|^2 of the last jrg_energy_grad
+ * (device double[S*K*B]) and the plan's |G+k|^2/2 table (double[K*G]). */
+int jrg_band_kinetic(const jrg_plan* plan, const void* workspace, double* out, cudaStream_t stream);
+int jrg_kinetic_table(const jrg_plan* plan, double* out, cudaStream_t stream);
+
 /* Selects the register-resident slab kernels for cubic grids N^3 with
  * N in {16, 24, 27, 32, 36, 48, 64, 96} (enable = 1, the default) or the
  * generic shared-memory Stockham kernels for every grid (enable = 0);

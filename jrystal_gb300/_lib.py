@@ -45,6 +45,14 @@ _SIGS = {
                        ct.c_double, ct.c_double, ct.c_double, ct.c_double, _vp], ct.c_int),
   "jrg_ewald": ([_vp, ct.c_double, ct.c_double, _vp, _vp, _vp], ct.c_int),
   "jrg_fast_paths": ([ct.c_int], ct.c_int),
+  "jrg_mlp_num_params": ([], ct.c_int),
+  "jrg_mlp_to_bf16": ([_vp, _vp, _vp], ct.c_int),
+  "jrg_mlp_workspace_size": ([ct.c_int, ct.POINTER(ct.c_size_t)], ct.c_int),
+  "jrg_mlp_train_eval": ([ct.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+                         ct.c_int),
+  "jrg_precond_scale": ([_vp, _vp, _vp, ct.c_float, ct.c_float, _vp, _vp, _vp, _vp], ct.c_int),
+  "jrg_band_kinetic": ([_vp, _vp, _vp, _vp], ct.c_int),
+  "jrg_kinetic_table": ([_vp, _vp, _vp], ct.c_int),
   "jrg_profile_enable": ([_vp, ct.c_int], ct.c_int),
   "jrg_profile_read": ([_vp, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int), ct.c_int], ct.c_int),
   "jrg_profile_phase_name": ([ct.c_int], ct.c_char_p),

@@ -31,7 +31,8 @@ template <typename R> int launch_potential(const void*, const void*, double, voi
 template <typename R> int launch_xc_field(const void*, void*, long long, int, int, cudaStream_t);
 template <typename R> int launch_real_part(const void*, void*, long long, double, cudaStream_t);
 template <typename R> int launch_hartree_g(const void*, const double*, void*, long long, double, cudaStream_t);
-template <typename R> int launch_kinetic(const void*, const double*, const double*, double*, int, int, int, int, cudaStream_t);
+template <typename R> int launch_kinetic(const void*, const double*, const double*, double*, double*, int, int, int, int, cudaStream_t);
+int launch_precond_scale(const float*, const void*, const double*, const double*, const double*, int, int, int, long long, float, float, float*, cudaStream_t);
 int launch_sum_slots(const double*, const int*, double*, int, const int*, cudaStream_t);
 template <typename R> int launch_geometry_tables(double*, double*, void*, const double*, const double*, const double*, int, int, int, int, double, cudaStream_t);
 int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
@@ -104,6 +105,7 @@ static void layout_workspace(jrg_plan* P) {
   w.adj_part = w.gram_part;
   w.epart = take((size_t)w.nepart * sizeof(double));
   w.flags = take(64);
+  w.ekin = take(nbt * sizeof(double));
   w.total = o;
 }
 
@@ -415,7 +417,8 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
   double* slots = (double*)wsp(ws, w.epart);
   {
     PHASE(PH_KINETIC);
-    if ((rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, occ, slots, nbt, P->ng, P->nb, P->nk, st)))
+    if ((rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, occ, slots, (double*)wsp(ws, w.ekin), nbt,
+                                P->ng, P->nb, P->nk, st)))
       return rc;
   }
   void* rho = wsp(ws, w.rho);
@@ -595,6 +598,29 @@ int jrg_fft3d(int prec, const int grid[3], int batch, int direction, const void*
                                       (double2*)scratch, (double2*)out, scale, st);
   return launch_fft3d_dense<float>(ax, (const float2*)tw, batch, direction, false, in,
                                    (float2*)scratch, (float2*)out, scale, st);
+}
+
+int jrg_precond_scale(const jrg_plan* P, const float* w32, const void* wb, float t_frac, float smax,
+                      const double* occ, float* scale, void* ws, cudaStream_t st) {
+  if (!P || !w32 || !wb || !occ || !scale || !ws)
+    return fail(JRG_ERR_INVALID, "jrg_precond_scale: null argument");
+  const long long total = (long long)P->ns * P->nk * P->ng * P->nb;
+  return launch_precond_scale(w32, wb, P->d.tk, (const double*)wsp(ws, P->ws.ekin), occ, P->nk, P->ng,
+                              P->nb, total, t_frac, smax, scale, st);
+}
+
+int jrg_band_kinetic(const jrg_plan* P, const void* ws, double* out, cudaStream_t st) {
+  if (!P || !ws || !out) return fail(JRG_ERR_INVALID, "jrg_band_kinetic: null argument");
+  JRG_CUDA(cudaMemcpyAsync(out, (const char*)ws + P->ws.ekin,
+                           sizeof(double) * (size_t)P->ns * P->nk * P->nb, cudaMemcpyDeviceToDevice, st));
+  return JRG_OK;
+}
+
+int jrg_kinetic_table(const jrg_plan* P, double* out, cudaStream_t st) {
+  if (!P || !out) return fail(JRG_ERR_INVALID, "jrg_kinetic_table: null argument");
+  JRG_CUDA(cudaMemcpyAsync(out, P->d.tk, sizeof(double) * (size_t)P->nk * P->ng,
+                           cudaMemcpyDeviceToDevice, st));
+  return JRG_OK;
 }
 
 int jrg_lda(int prec, int64_t n, int xc, int kohn_sham, const void* rho, void* out, cudaStream_t st) {

@@ -181,7 +181,8 @@ template <typename R>
 __global__ void __launch_bounds__(256) k_kinetic(const C_t<R>* __restrict__ coef,
                                                  const double* __restrict__ tk,
                                                  const double* __restrict__ occ,
-                                                 double* __restrict__ slot, int ng, int nb, int nk) {
+                                                 double* __restrict__ slot, double* __restrict__ ekin,
+                                                 int ng, int nb, int nk) {
   __shared__ double red[32];
   const int band = blockIdx.x;           // global (s, k, b)
   const int k = (band / nb) % nk;
@@ -193,7 +194,10 @@ __global__ void __launch_bounds__(256) k_kinetic(const C_t<R>* __restrict__ coef
     part += (R)t[g] * (x * x + y * y);
   }
   const double acc = block_sum((double)part, red);
-  if (threadIdx.x == 0) slot[band] = acc * occ[band];
+  if (threadIdx.x == 0) {
+    slot[band] = acc * occ[band];
+    if (ekin) ekin[band] = acc;
+  }
 }
 
 // energies[t] = sum of its slots, t = 0..3; energies[4] = total
@@ -426,10 +430,10 @@ int launch_hartree_g(const void* rhog, const double* ginv, void* out, long long 
 }
 
 template <typename R>
-int launch_kinetic(const void* coef, const double* tk, const double* occ, double* slot, int nbands,
-                   int ng, int nb, int nk, cudaStream_t st) {
-  k_kinetic<R><<<nbands, 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(coef), tk, occ, slot, ng, nb,
-                                       nk);
+int launch_kinetic(const void* coef, const double* tk, const double* occ, double* slot, double* ekin,
+                   int nbands, int ng, int nb, int nk, cudaStream_t st) {
+  k_kinetic<R><<<nbands, 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(coef), tk, occ, slot, ekin, ng,
+                                       nb, nk);
   JRG_LAUNCH_CHECK("k_kinetic");
   return JRG_OK;
 }
@@ -496,8 +500,8 @@ int launch_twiddles(int n, int prec, void* out, cudaStream_t st) {
   template int launch_real_part<R>(const void*, void*, long long, double, cudaStream_t);          \
   template int launch_hartree_g<R>(const void*, const double*, void*, long long, double,          \
                                    cudaStream_t);                                               \
-  template int launch_kinetic<R>(const void*, const double*, const double*, double*, int, int,    \
-                                 int, int, cudaStream_t);                                       \
+  template int launch_kinetic<R>(const void*, const double*, const double*, double*, double*, int, \
+                                 int, int, int, cudaStream_t);                                  \
   template int launch_geometry_tables<R>(double*, double*, void*, const double*, const double*,   \
                                          const double*, int, int, int, int, double, cudaStream_t); \
   template int launch_adam<R>(void*, const void*, void*, void*, const float*, long long, double,  \

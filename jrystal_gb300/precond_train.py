@@ -1,0 +1,143 @@
+"""Trains and evaluates the learned preconditioner on trajectories this
+implementation generates.
+
+  python -m jrystal_gb300.precond_train --out weights.npz [--eval-json eval.json]
+
+1. Trajectories: 64 strained cells (Si, C, Al; seed 2; grids from
+   {24, 27, 32, 36, 48}; 2x2x2 k-grid; 8-16 bands, the lower half doubly
+   occupied), 300 plain Adam steps each (lr 1e-2), ~6 sampled coefficient
+   records per step (~1.2e5 records).
+2. Training: Adam lr 1e-3, 2000 steps, seed 3, with the library's BF16/FP32
+   training kernels; then ``rounds - 1`` refinement rounds whose records
+   come from trajectories run under the current network (the one-step model
+   is re-expressed for the absolute scale, see collect_records).
+3. Evaluation on 16 held-out strained cells: plain and learned (with the
+   plain fallback) optimisers from the same start; steps and wall time until
+   |E - E_ref| < 1e-5 Ha/atom, with E_ref the lower of the two final energies.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+import torch
+
+from . import cells, precond
+from .calc import Minimizer
+from .engine import PlaneWavePlan
+
+
+def _plan(wl):
+  return PlaneWavePlan(wl.cell, wl.positions, wl.charges, wl.grid_sizes, wl.mask, wl.kpts,
+                       wl.num_band, 1, wl.precision, wl.xc)
+
+
+def _params(wl, plan):
+  wr, wi = wl.init_params()
+  return torch.tensor(np.stack([wr, wi]), dtype=plan.rdtype, device=plan.device)
+
+
+def generate(ncells=64, steps=300, per_step=6, seed=2, grids=(24, 27, 32, 36, 48), mlp=None,
+             smax=4.0, lr=1e-2):
+  rng = np.random.default_rng(seed)
+  recs = []
+  for i in range(ncells):
+    wl = cells.strained_cell(rng, grids=grids)
+    plan = _plan(wl)
+    fn = precond.GuardedScale(mlp, steps, smax, rise_tol=1e9) if mlp is not None else None
+    recs.append(precond.collect_records(plan, wl.occupation, _params(wl, plan), steps, lr,
+                                        precond.RecordSpec(per_step=per_step), seed=seed * 1000 + i,
+                                        scale_fn=fn))
+    plan.close()
+  return {k: torch.cat([r[k] for r in recs]) for k in recs[0]}
+
+
+def fit(rounds=3, ncells=64, steps=300, per_step=6, smax=4.0, grids=(24, 27, 32, 36, 48),
+        refine_steps=1500, log=print):
+  """Round 1 on plain trajectories of ``steps`` steps; refinement rounds on
+  trajectories of ``refine_steps`` steps run under the current network (the
+  horizon of the step feature x3 is refine_steps from round 2 on)."""
+  mlp = precond.MLP(seed=3)
+  t0 = time.time()
+  R = generate(ncells, steps, per_step, 2, grids)
+  log(f"round 1: {R['x'].shape[0]} records from plain trajectories ({time.time() - t0:.1f} s)")
+  precond.train(mlp, R, steps=2000, lr=1e-3, seed=3)
+  for r in range(2, rounds + 1):
+    R2 = generate(ncells // 4, refine_steps, max(1, per_step * steps // refine_steps * 2),
+                  2 + 10 * r, grids, mlp=mlp, smax=smax)
+    R = {k: torch.cat([R[k], R2[k]]) for k in R}
+    precond.train(mlp, R, steps=2000, lr=1e-3, seed=3 + r)
+    log(f"round {r}: {R['x'].shape[0]} records, loss {precond.evaluate_loss(mlp, R):.4f}")
+  return mlp
+
+
+def run_pair(wl, mlp, nsteps, smax=4.0, total=1500, lr=1e-2):
+  """Plain and learned histories (energy per step) and ms per step of each."""
+  plan = _plan(wl)
+  out = {}
+  for mode in ("plain", "learned"):
+    g = precond.GuardedScale(mlp, total, smax) if mode == "learned" else None
+    mini = Minimizer(plan, wl.occupation, _params(wl, plan), lr=lr, scale_fn=g, total_steps=total)
+    hist = torch.empty(nsteps, dtype=torch.float64, device=plan.device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for t in range(nsteps):
+      e = mini.step()
+      hist[t] = e[4]
+      if g is not None and t % 20 == 0 and g.fallback_at is None:
+        g.observe(float(e[4]), t)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / nsteps * 1e3
+    out[mode] = (hist.cpu().numpy(), ms, None if g is None else g.fallback_at)
+  plan.close()
+  return out
+
+
+def evaluate(mlp, ncells=16, nsteps=8000, seed=99, grids=(24, 27, 32), smax=4.0, tol=1e-5,
+             total=1500):
+  rng = np.random.default_rng(seed)
+  rows = []
+  for j in range(ncells):
+    wl = cells.strained_cell(rng, grids=grids)
+    res = run_pair(wl, mlp, nsteps, smax, total)
+    nat = wl.positions.shape[0]
+    eref = min(res["plain"][0][-1], res["learned"][0][-1])
+    row = {"cell": wl.name}
+    for mode, (h, ms, fb) in res.items():
+      t = precond.time_to_tolerance(h, eref, tol * nat)
+      row[mode] = {"steps": t, "ms_per_step": ms, "seconds": None if t is None else t * ms / 1e3,
+                   "fallback_at": fb, "E_end": float(h[-1])}
+    p, l = row["plain"]["seconds"], row["learned"]["seconds"]
+    # a plain run that never reached the tolerance counts as its full length
+    p_eff = p if p is not None else nsteps * row["plain"]["ms_per_step"] / 1e3
+    row["speedup_wall"] = None if l is None else p_eff / l
+    row["plain_reached"] = p is not None
+    rows.append(row)
+  sp = [r["speedup_wall"] for r in rows if r["speedup_wall"] is not None]
+  return {"cells": rows, "median_speedup_wall": float(np.median(sp)) if sp else None,
+          "learned_reached": sum(r["learned"]["steps"] is not None for r in rows),
+          "plain_reached": sum(r["plain_reached"] for r in rows), "nsteps": nsteps, "tol": tol}
+
+
+def main():
+  ap = argparse.ArgumentParser()
+  ap.add_argument("--out", required=True)
+  ap.add_argument("--eval-json", default=None)
+  ap.add_argument("--rounds", type=int, default=3)
+  ap.add_argument("--eval-cells", type=int, default=16)
+  ap.add_argument("--eval-steps", type=int, default=8000)
+  ap.add_argument("--refine-steps", type=int, default=1500)
+  args = ap.parse_args()
+  mlp = fit(rounds=args.rounds, refine_steps=args.refine_steps)
+  mlp.save(args.out)
+  if args.eval_json:
+    res = evaluate(mlp, ncells=args.eval_cells, nsteps=args.eval_steps, total=args.refine_steps)
+    with open(args.eval_json, "w") as f:
+      json.dump(res, f, indent=1)
+    print(json.dumps({k: v for k, v in res.items() if k != "cells"}))
+
+
+if __name__ == "__main__":
+  main()
