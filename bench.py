@@ -41,6 +41,8 @@ def _args():
   p.add_argument("--workload", default="si8_cubic_64")
   p.add_argument("--no-cpu-baseline", action="store_true")
   p.add_argument("--cpu-sample-kpts", type=int, default=1)
+  p.add_argument("--kgrid", type=int, nargs=3, default=None,
+                 help="override the workload's k-grid (smaller cases for profiling)")
   return p.parse_args()
 
 
@@ -322,6 +324,9 @@ def main():
   args = _args()
   from jrystal_gb300 import workloads
   wl = workloads.WORKLOADS[args.workload]()
+  if args.kgrid:
+    wl.kgrid = tuple(args.kgrid)
+    wl.name += "_k" + "x".join(map(str, args.kgrid))
   if args.impl == "reference":
     run_reference(args, wl)
   else:

@@ -187,6 +187,12 @@ int jrg_kinetic_table(const jrg_plan* plan, double* out, cudaStream_t stream);
  * no reference counterpart. */
 int jrg_fast_paths(int enable);
 
+/* Selects tensor-core (mma.sync TF32, three-product hi/lo split) Gram and
+ * rotation contractions for the FP32 path with num_band <= 32 (enable = 1,
+ * the default) or the CUDA-core kernels (0); < 0 only queries.  Returns the
+ * previous setting.  No reference counterpart. */
+int jrg_tensor_core_paths(int enable);
+
 /* Per-phase CUDA-event timing of jrg_energy_grad (no reference counterpart;
  * the reference only times whole steps, calc driver :207-211).  enable
  * creates events for up to max_calls calls (0 disables); read synchronises

@@ -45,6 +45,7 @@ _SIGS = {
                        ct.c_double, ct.c_double, ct.c_double, ct.c_double, _vp], ct.c_int),
   "jrg_ewald": ([_vp, ct.c_double, ct.c_double, _vp, _vp, _vp], ct.c_int),
   "jrg_fast_paths": ([ct.c_int], ct.c_int),
+  "jrg_tensor_core_paths": ([ct.c_int], ct.c_int),
   "jrg_mlp_num_params": ([], ct.c_int),
   "jrg_mlp_to_bf16": ([_vp, _vp, _vp], ct.c_int),
   "jrg_mlp_workspace_size": ([ct.c_int, ct.POINTER(ct.c_size_t)], ct.c_int),

@@ -80,7 +80,8 @@ static void layout_workspace(jrg_plan* P) {
   const size_t C = csize(P->prec), Rz = rsize(P->prec);
   const size_t nsk = (size_t)P->ns * P->nk, nbt = nsk * P->nb;
   const size_t b2 = (size_t)P->nb * P->nb * sizeof(double2);
-  w.gram_splits = std::max(1, std::min(64, (int)((P->ng + 1023) / 1024)));
+  // enough (s,k,split) CTAs to fill the GPU several times over: ~256 G rows each
+  w.gram_splits = std::max(1, std::min(512, (int)((P->ng + 255) / 256)));
   w.ngroups = (int)nsk;
   w.nepart = (int)nbt + 2 * kRecipBlocks + kXcBlocks;
   if (w.nepart < 2 * kEwaldBlocks) w.nepart = 2 * kEwaldBlocks;
@@ -88,7 +89,11 @@ static void layout_workspace(jrg_plan* P) {
   auto take = [&](size_t bytes) { size_t r = o; o += align256(bytes); return r; };
   w.wc = 0;                             // parameters are read in place
   w.c = take(nbt * P->ng * C);
-  w.gram_part = take(nsk * w.gram_splits * b2);
+  {
+    // CUDA-core partials: nb^2 complex; tensor-core partials: (2nb rounded to 16)^2 real
+    const size_t mp = (size_t)((2 * P->nb + 15) / 16 * 16);
+    w.gram_part = take(nsk * w.gram_splits * std::max(b2, mp * mp * sizeof(double)));
+  }
   w.gram = take(nsk * b2);
   w.rmat = take(nsk * b2);
   w.rinv = take(nsk * b2);

@@ -20,6 +20,11 @@ namespace fast {
 using reg::Split;
 
 template <int N> constexpr int threads_for() { return N * Split<N>::N2; }
+// two resident CTAs per SM where the register file allows it (<= 64 registers
+// per thread at 512 threads): hides the global-load latency of the band loop
+template <typename R, int N> constexpr int min_blocks_for() {
+  return (sizeof(R) == 4 && N <= 64) ? 2 : 1;
+}
 
 // sphere -> y,z-transformed active planes
 template <typename R, int N>
@@ -83,7 +88,7 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere(
 
 // inverse x transform + occupation-weighted |psi|^2 of a band group
 template <typename R, int N>
-__global__ void __launch_bounds__(threads_for<N>()) k_line_density(
+__global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_density(
     const C_t<R>* __restrict__ planes, R* __restrict__ rho_part, const double* __restrict__ wband,
     double wscale, int band0, int nband, int bands_per_group, const int* __restrict__ xact,
     const C_t<R>* __restrict__ tw_g, int nact) {
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(threads_for<N>()) k_line_density(
 // adjoint line pass: inverse x transform, times V(r), forward x transform,
 // active planes written back in place
 template <typename R, int N>
-__global__ void __launch_bounds__(threads_for<N>()) k_line_apply_v(
+__global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_apply_v(
     C_t<R>* __restrict__ planes, const R* __restrict__ vr, int nband, int bands_per_group,
     const int* __restrict__ xact, const C_t<R>* __restrict__ tw_g, int nact) {
   using C = C_t<R>;
@@ -341,6 +346,9 @@ static int optin_smem() {
 template <typename K> static int prep(K kernel, size_t bytes) {
   if ((long long)bytes > optin_smem()) return 0;
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return -cuda_fail(e, "cudaFuncSetAttribute(fast slab kernel)");
   return 1;
 }

@@ -338,19 +338,57 @@ __global__ void k_ewald_finish(const double* __restrict__ slots, int nslots, con
 // Adam (optax placement of eps) with optional elementwise update scale
 // ------------------------------------------------------------------------
 template <typename R>
+__device__ __forceinline__ R adam_one(R& p, R g, R& m, R& v, R lr, R b1, R b2, R c1, R c2, R eps) {
+  m = b1 * m + (1 - b1) * g;
+  v = b2 * v + (1 - b2) * g * g;
+  return -lr * (m / c1) / (sqrt(v / c2) + eps);
+}
+
+template <typename R>
 __global__ void k_adam(R* __restrict__ p, const R* __restrict__ g, R* __restrict__ m,
                        R* __restrict__ v, const float* __restrict__ scale, long long n, R lr, R b1,
                        R b2, R c1, R c2, R eps) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const R gi = g[i];
-    const R mi = b1 * m[i] + (1 - b1) * gi;
-    const R vi = b2 * v[i] + (1 - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    R u = -lr * (mi / c1) / (sqrt(vi / c2) + eps);
-    if (scale) u *= (R)scale[i];
-    p[i] += u;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if constexpr (sizeof(R) == 4) {
+    // four elements per thread with 16-byte accesses when the buffers are aligned
+    const bool vec = (((uintptr_t)p | (uintptr_t)g | (uintptr_t)m | (uintptr_t)v |
+                       (uintptr_t)scale) & 15) == 0;
+    const long long n4 = vec ? n / 4 : 0;
+    for (long long q = tid; q < n4; q += stride) {
+      float4 pp = reinterpret_cast<float4*>(p)[q];
+      const float4 gg = reinterpret_cast<const float4*>(g)[q];
+      float4 mm = reinterpret_cast<float4*>(m)[q];
+      float4 vv = reinterpret_cast<float4*>(v)[q];
+      float4 u;
+      u.x = adam_one<float>(pp.x, gg.x, mm.x, vv.x, lr, b1, b2, c1, c2, eps);
+      u.y = adam_one<float>(pp.y, gg.y, mm.y, vv.y, lr, b1, b2, c1, c2, eps);
+      u.z = adam_one<float>(pp.z, gg.z, mm.z, vv.z, lr, b1, b2, c1, c2, eps);
+      u.w = adam_one<float>(pp.w, gg.w, mm.w, vv.w, lr, b1, b2, c1, c2, eps);
+      if (scale) {
+        const float4 s = reinterpret_cast<const float4*>(scale)[q];
+        u.x *= s.x; u.y *= s.y; u.z *= s.z; u.w *= s.w;
+      }
+      pp.x += u.x; pp.y += u.y; pp.z += u.z; pp.w += u.w;
+      reinterpret_cast<float4*>(p)[q] = pp;
+      reinterpret_cast<float4*>(m)[q] = mm;
+      reinterpret_cast<float4*>(v)[q] = vv;
+    }
+    for (long long i = 4 * n4 + tid; i < n; i += stride) {
+      R mi = m[i], vi = v[i];
+      R u = adam_one<R>(p[i], g[i], mi, vi, lr, b1, b2, c1, c2, eps);
+      m[i] = mi; v[i] = vi;
+      if (scale) u *= (R)scale[i];
+      p[i] += u;
+    }
+  } else {
+    for (long long i = tid; i < n; i += stride) {
+      R mi = m[i], vi = v[i];
+      R u = adam_one<R>(p[i], g[i], mi, vi, lr, b1, b2, c1, c2, eps);
+      m[i] = mi; v[i] = vi;
+      if (scale) u *= (R)scale[i];
+      p[i] += u;
+    }
   }
 }
 
@@ -471,7 +509,7 @@ int launch_ewald(const double* cell, const double* gvec, const double* pos, cons
 template <typename R>
 int launch_adam(void* p, const void* g, void* m, void* v, const float* scale, long long n, double lr,
                 double b1, double b2, double c1, double c2, double eps, cudaStream_t st) {
-  k_adam<R><<<grid_for(n, 256, 8192), 256, 0, st>>>(
+  k_adam<R><<<grid_for((n + 3) / 4, 256, 152 * 16), 256, 0, st>>>(
       reinterpret_cast<R*>(p), reinterpret_cast<const R*>(g), reinterpret_cast<R*>(m),
       reinterpret_cast<R*>(v), scale, n, (R)lr, (R)b1, (R)b2, (R)c1, (R)c2, (R)eps);
   JRG_LAUNCH_CHECK("k_adam");

@@ -328,6 +328,73 @@ __global__ void __launch_bounds__(32) k_cholesky_inv_warp(const double2* __restr
   }
 }
 
+// nb <= 32: one CTA of nb*nb threads per (s,k), thread (i, j) owns element
+// (i, j).  Right-looking Cholesky and a right-looking inverse, so each pivot
+// step is two or three dependent FP64 operations per thread (FP64 latency is
+// long on this part; the work is spread instead of chained).
+__global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __restrict__ S,
+                                                            double2* __restrict__ Rm,
+                                                            double2* __restrict__ Ri, int nb,
+                                                            int* __restrict__ flags) {
+  __shared__ double2 r[32][33];
+  __shared__ double2 x[32][33];
+  __shared__ double dinv[32];
+  const int sk = blockIdx.x;
+  const int i = threadIdx.x / nb, j = threadIdx.x % nb;
+  const bool live = threadIdx.x < nb * nb;
+  const size_t off = (size_t)sk * nb * nb;
+  if (live) {
+    const double2 a = S[off + i * nb + j], b = S[off + j * nb + i];
+    r[i][j] = (j >= i) ? make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)) : make_double2(0.0, 0.0);
+    x[i][j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (live && i == k && j == k) {
+      double d = r[k][k].x;
+      if (!(d > 0.0) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
+      const double rs = rsqrt_fp64(d);
+      r[k][k] = make_double2(d * rs, 0.0);
+      dinv[k] = rs;
+    }
+    __syncthreads();
+    if (live && i == k && j > k) {
+      const double rs = dinv[k];
+      const double2 v = r[k][j];
+      r[k][j] = make_double2(v.x * rs, v.y * rs);
+    }
+    __syncthreads();
+    if (live && i > k && j >= i) {
+      const double2 a = r[k][i], b = r[k][j];
+      double2 v = r[i][j];
+      v.x -= a.x * b.x + a.y * b.y;
+      v.y -= a.x * b.y - a.y * b.x;
+      r[i][j] = v;
+    }
+    __syncthreads();
+  }
+  // X = R^{-1}: rows finalised bottom-up, each subtracted from the rows above
+  for (int k = nb - 1; k >= 0; --k) {
+    if (live && i == k && j >= k) {
+      const double2 v = x[k][j];
+      x[k][j] = make_double2(v.x * dinv[k], v.y * dinv[k]);
+    }
+    __syncthreads();
+    if (live && i < k && j >= k) {
+      const double2 a = r[i][k], b = x[k][j];
+      double2 v = x[i][j];
+      v.x -= a.x * b.x - a.y * b.y;
+      v.y -= a.x * b.y + a.y * b.x;
+      x[i][j] = v;
+    }
+    __syncthreads();
+  }
+  if (live) {
+    Rm[off + i * nb + j] = r[i][j];
+    Ri[off + i * nb + j] = x[i][j];
+  }
+}
+
 // Adjoint small matrices per (s,k), one CTA each:
 //   Rh = R^{-H};  K from A;  M2 = K R^{-H}  (stored negated: -M2)
 __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict__ A,
@@ -462,9 +529,22 @@ int launch_unpack(const void* in, void* o_re, void* o_im, void* o_c, int nsk, in
   return JRG_OK;
 }
 
+int launch_gram_tc(int lx, const void* X0, const void* X1, int ly, const void* Y0, const void* Y1,
+                   double* part, double2* out, int nsk, int ng, int nb, int nsplit, cudaStream_t st);
+int launch_rotate_tc(int out_kind, int lx0, const void* X0a, const void* X0b, const double2* M0,
+                     const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng,
+                     int nb, double fac, cudaStream_t st);
+static bool g_tc_enabled = true;
+
 template <typename R>
 int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, const void* Y1,
                 double2* part, double2* out, int nsk, int ng, int nb, int nsplit, cudaStream_t st) {
+  if (sizeof(R) == 4 && g_tc_enabled) {   // FP32 path: tensor cores (TF32 x3)
+    const int t = launch_gram_tc(lx, X0, X1, ly, Y0, Y1, reinterpret_cast<double*>(part), out, nsk,
+                                 ng, nb, nsplit, st);
+    if (t < 0) return -t;
+    if (t > 0) return JRG_OK;
+  }
   const int split_len = (ng + nsplit - 1) / nsplit;
   const int ntile = (nb + kGramTile - 1) / kGramTile;
   dim3 grid(nsplit, ntile * ntile, nsk);
@@ -484,7 +564,7 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
 int launch_cholesky_inv(const double2* S, double2* Rm, double2* Ri, int nsk, int nb, int* flags,
                         cudaStream_t st) {
   if (nb <= 32) {
-    k_cholesky_inv_warp<<<nsk, 32, 0, st>>>(S, Rm, Ri, nb, flags);
+    k_cholesky_inv_elem<<<nsk, ((nb * nb + 31) / 32) * 32, 0, st>>>(S, Rm, Ri, nb, flags);
   } else if (nb <= 64) {
     const size_t sm = 2 * sizeof(double2) * (size_t)nb * nb;
     if (sm > 48 * 1024) {
@@ -543,6 +623,11 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
                   const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng, int nb,
                   double fac, cudaStream_t st) {
   if (X1 && lx0 != LAYOUT_BAND) return fail(JRG_ERR_INVALID, "launch_rotate: two-term form needs band-major inputs");
+  if (sizeof(R) == 4 && g_tc_enabled) {
+    const int t = launch_rotate_tc(out_kind, lx0, X0a, X0b, M0, X1, M1, out0, out1, nsk, ng, nb, fac, st);
+    if (t < 0) return -t;
+    if (t > 0) return JRG_OK;
+  }
   if (out_kind == ROT_BANDMAJOR)
     return rotate_out<R, ROT_BANDMAJOR>(lx0, X0a, X0b, M0, LAYOUT_BAND, X1, nullptr, M1, out0, out1, nsk, ng, nb, fac, st);
   if (out_kind == ROT_GMAJOR_C)
@@ -563,3 +648,9 @@ JRG_INST_ORTH(float)
 JRG_INST_ORTH(double)
 
 }  // namespace jrg
+
+extern "C" int jrg_tensor_core_paths(int enable) {
+  const int prev = jrg::g_tc_enabled ? 1 : 0;
+  if (enable >= 0) jrg::g_tc_enabled = enable != 0;
+  return prev;
+}
