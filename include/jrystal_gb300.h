@@ -188,9 +188,9 @@ int jrg_kinetic_table(const jrg_plan* plan, double* out, cudaStream_t stream);
 int jrg_fast_paths(int enable);
 
 /* Selects tensor-core (mma.sync TF32, three-product hi/lo split) Gram and
- * rotation contractions for the FP32 path with num_band <= 32 (enable = 1,
- * the default) or the CUDA-core kernels (0); < 0 only queries.  Returns the
- * previous setting.  No reference counterpart. */
+ * rotation contractions for the FP32 path with num_band <= 32 (enable = 1)
+ * or the CUDA-core kernels (0, the default: faster at these band counts);
+ * < 0 only queries.  Returns the previous setting.  No reference counterpart. */
 int jrg_tensor_core_paths(int enable);
 
 /* Per-phase CUDA-event timing of jrg_energy_grad (no reference counterpart;

@@ -22,7 +22,7 @@ template <typename R> int launch_unpack(const void*, void*, void*, void*, int, i
 template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t);
 int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, cudaStream_t);
 int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t);
-template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, cudaStream_t);
+template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t);
 constexpr int kSplit = 0, kBand = 1;           // tall-operand layouts (k_orth.cu)
 constexpr int kRotBand = 0, kRotGC = 1, kRotGSplit = 2;
 template <typename R> int launch_reduce_density(const void*, void*, int, int, long long, cudaStream_t);
@@ -111,6 +111,7 @@ static void layout_workspace(jrg_plan* P) {
   w.epart = take((size_t)w.nepart * sizeof(double));
   w.flags = take(64);
   w.ekin = take(nbt * sizeof(double));
+  w.rot_scratch = take(nsk * 2 * 128 * 64 * sizeof(uint32_t));   // split B of the TF32 rotations
   w.total = o;
 }
 
@@ -384,7 +385,8 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
   }
   PHASE(PH_ROTATE);
   return launch_rotate<R>(out_kind, kSplit, w_re, w_im, (double2*)wsp(ws, w.rinv), nullptr, nullptr,
-                          out ? out : wsp(ws, w.c), nullptr, nsk, P->ng, P->nb, 1.0, st);
+                          out ? out : wsp(ws, w.c), nullptr, nsk, P->ng, P->nb, 1.0,
+                          wsp(ws, w.rot_scratch), st);
 }
 
 // density of the band-major coefficients held in workspace slot c
@@ -479,7 +481,7 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
   }
   PHASE(PH_ADJ_ROTATE);
   return launch_rotate<R>(kRotGSplit, kBand, wsp(ws, w.gc), nullptr, rh, wsp(ws, w.c), negm2, g_re,
-                          g_im, nsk, P->ng, P->nb, 2.0, st);
+                          g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st);
 }
 
 template <typename R>

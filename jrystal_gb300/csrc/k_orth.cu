@@ -533,8 +533,8 @@ int launch_gram_tc(int lx, const void* X0, const void* X1, int ly, const void* Y
                    double* part, double2* out, int nsk, int ng, int nb, int nsplit, cudaStream_t st);
 int launch_rotate_tc(int out_kind, int lx0, const void* X0a, const void* X0b, const double2* M0,
                      const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng,
-                     int nb, double fac, cudaStream_t st);
-static bool g_tc_enabled = true;
+                     int nb, double fac, uint32_t* bscratch, cudaStream_t st);
+static bool g_tc_enabled = false;   // measured slower than the CUDA-core kernels at B <= 32
 
 template <typename R>
 int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, const void* Y1,
@@ -621,10 +621,11 @@ static int rotate_out(int lx0, const void* X0a, const void* X0b, const double2* 
 template <typename R>
 int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const double2* M0,
                   const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng, int nb,
-                  double fac, cudaStream_t st) {
+                  double fac, void* scratch, cudaStream_t st) {
   if (X1 && lx0 != LAYOUT_BAND) return fail(JRG_ERR_INVALID, "launch_rotate: two-term form needs band-major inputs");
   if (sizeof(R) == 4 && g_tc_enabled) {
-    const int t = launch_rotate_tc(out_kind, lx0, X0a, X0b, M0, X1, M1, out0, out1, nsk, ng, nb, fac, st);
+    const int t = launch_rotate_tc(out_kind, lx0, X0a, X0b, M0, X1, M1, out0, out1, nsk, ng, nb, fac,
+                                   reinterpret_cast<uint32_t*>(scratch), st);
     if (t < 0) return -t;
     if (t > 0) return JRG_OK;
   }
@@ -643,7 +644,8 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
   template int launch_gram<R>(int, const void*, const void*, int, const void*, const void*,       \
                               double2*, double2*, int, int, int, int, cudaStream_t);            \
   template int launch_rotate<R>(int, int, const void*, const void*, const double2*, const void*,  \
-                                const double2*, void*, void*, int, int, int, double, cudaStream_t);
+                                const double2*, void*, void*, int, int, int, double, void*,     \
+                                cudaStream_t);
 JRG_INST_ORTH(float)
 JRG_INST_ORTH(double)
 

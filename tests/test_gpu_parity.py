@@ -171,3 +171,31 @@ def test_fast_and_generic_slab_kernels_agree(prec):
   scale = np.abs(out[0][1]).max()
   assert np.abs(out[1][1] - out[0][1]).max() <= tol["g_rel"] * scale
   assert np.abs(out[1][2] - out[0][2]).max() <= tol["g_rel"] * scale
+
+
+def test_tensor_core_and_cuda_core_contractions_agree():
+  torch = _torch()
+  from jrystal_gb300 import _lib
+  lib = _lib.load()
+  sysm = make_system(kind="si8", grid=(36, 36, 36), kgrid=(2, 1, 1), nb=24, nocc=12)
+  wr, wi = random_params(sysm, seed=31)
+  terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+  plan = _plan(sysm, 32)
+  twr = torch.tensor(wr, dtype=torch.float32, device="cuda")
+  twi = torch.tensor(wi, dtype=torch.float32, device="cuda")
+  out = {}
+  prev = lib.jrg_tensor_core_paths(-1)
+  try:
+    for tc in (1, 0):
+      lib.jrg_tensor_core_paths(tc)
+      e, g1, g2 = plan.energy_and_grad(twr, twi, sysm.occupation)
+      out[tc] = (e.cpu().numpy().copy(), g1.cpu().numpy(), g2.cpu().numpy())
+  finally:
+    lib.jrg_tensor_core_paths(prev)
+  tol = TOL[32]
+  scale = max(np.abs(gr).max(), np.abs(gi).max())
+  for tc in (1, 0):
+    e, g1, g2 = out[tc]
+    for i, name in enumerate(["kinetic", "external", "hartree", "xc", "total"]):
+      assert abs(e[i] - terms[name]) <= tol["e_rel"] * max(1.0, abs(terms[name])), (tc, name)
+    assert max(np.abs(g1 - gr).max(), np.abs(g2 - gi).max()) <= tol["g_rel"] * scale, tc
