@@ -40,6 +40,8 @@ def _args():
   p.add_argument("--impl", default="ours", choices=["ours", "reference"])
   p.add_argument("--workload", default="si8_cubic_64")
   p.add_argument("--no-cpu-baseline", action="store_true")
+  p.add_argument("--no-time-to-tol", action="store_true",
+                 help="skip the learned-vs-plain time-to-tolerance runs")
   p.add_argument("--cpu-sample-kpts", type=int, default=1)
   p.add_argument("--kgrid", type=int, nargs=3, default=None,
                  help="override the workload's k-grid (smaller cases for profiling)")
@@ -202,6 +204,28 @@ def phase_bytes(plan):
   }
 
 
+def time_to_tolerance(nsteps=8000, cell_index=1):
+  """Learned vs plain optimiser on a held-out strained cell (the evaluation
+  sequence of the preconditioner, seed 99): wall time until |E - E_ref| <
+  1e-5 Ha/atom, E_ref the lower of the two final energies."""
+  from jrystal_gb300 import cells, precond, precond_train
+  mlp = precond.MLP.load(precond.DEFAULT_WEIGHTS)
+  rng = np.random.default_rng(99)
+  for _ in range(cell_index + 1):
+    wl = cells.strained_cell(rng, grids=(24, 27, 32))
+  res = precond_train.run_pair(wl, mlp, nsteps)
+  nat = wl.positions.shape[0]
+  eref = min(res["plain"][0][-1], res["learned"][0][-1])
+  out = {"cell": wl.name, "tol_ha_per_atom": 1e-5, "max_steps": nsteps}
+  for mode, (h, ms, fb) in res.items():
+    t = precond.time_to_tolerance(h, eref, 1e-5 * nat)
+    out[mode] = {"steps": t, "ms_per_step": round(ms, 4),
+                 "seconds": None if t is None else round(t * ms / 1e3, 4)}
+  p, l = out["plain"]["seconds"], out["learned"]["seconds"]
+  out["speedup_wall"] = None if (p is None or l is None) else round(p / l, 3)
+  return out
+
+
 def run_ours(args, wl):
   import torch
   import torch.distributed as dist
@@ -307,6 +331,8 @@ def run_ours(args, wl):
                    "d2h_bytes_per_step": 64},
            "gpu_launches": int(launches), "roofline": roof,
            "energies_last_step": energies[:5]}
+    if not args.no_time_to_tol:
+      out["time_to_1e-5_Ha_per_atom"] = time_to_tolerance()
     if not args.no_cpu_baseline:
       workers = len(os.sched_getaffinity(0))
       nks = max(1, min(args.cpu_sample_kpts, wl.num_kpt))

@@ -20,7 +20,7 @@ template <typename R> int launch_fft3d_dense(const FftAxis*, const C_t<R>*, int,
 template <typename R> int launch_pack_params(const void*, const void*, void*, int, int, int, bool, cudaStream_t);
 template <typename R> int launch_unpack(const void*, void*, void*, void*, int, int, int, double, cudaStream_t);
 template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t);
-int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, cudaStream_t);
+int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t);
 int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t);
 template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t);
 constexpr int kSplit = 0, kBand = 1;           // tall-operand layouts (k_orth.cu)
@@ -111,6 +111,7 @@ static void layout_workspace(jrg_plan* P) {
   w.epart = take((size_t)w.nepart * sizeof(double));
   w.flags = take(64);
   w.ekin = take(nbt * sizeof(double));
+  w.dinv = take(nbt * sizeof(double));
   w.rot_scratch = take(nsk * 2 * 128 * 64 * sizeof(uint32_t));   // split B of the TF32 rotations
   w.total = o;
 }
@@ -380,7 +381,8 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
   {
     PHASE(PH_CHOL);
     if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram), (double2*)wsp(ws, w.rmat),
-                                  (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags), st)))
+                                  (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags),
+                                  (double*)wsp(ws, w.dinv), st)))
       return rc;
   }
   PHASE(PH_ROTATE);

@@ -177,83 +177,6 @@ __global__ void k_gram_reduce(const double2* __restrict__ part, double2* __restr
   }
 }
 
-// One CTA per (s,k): R = chol(S) (upper, S = R^H R) and Rinv = R^{-1}, in
-// FP64.  A non-positive or non-finite pivot sets flags[0] |= 1 and continues
-// with a unit pivot.  The matrices live in shared memory when SMEM (nb <= 64)
-// and in the output buffers otherwise.
-template <bool SMEM>
-__global__ void __launch_bounds__(256) k_cholesky_inv(const double2* __restrict__ S,
-                                                      double2* __restrict__ Rm,
-                                                      double2* __restrict__ Ri, int nb,
-                                                      int* __restrict__ flags) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int sk = blockIdx.x;
-  const size_t off = (size_t)sk * nb * nb;
-  const double2* s = S + off;
-  double2* r = SMEM ? reinterpret_cast<double2*>(smem_raw) : Rm + off;
-  double2* ri = SMEM ? r + nb * nb : Ri + off;
-  __shared__ double piv;
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int i = e / nb, j = e % nb;
-    // Hermitian symmetrisation of the accumulated Gram
-    const double2 a = s[i * nb + j], b = s[j * nb + i];
-    r[e] = (j >= i) ? make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)) : make_double2(0.0, 0.0);
-  }
-  __syncthreads();
-  for (int k = 0; k < nb; ++k) {
-    if (threadIdx.x == 0) {
-      double d = r[k * nb + k].x;
-      if (!(d > 0.0) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
-      d = sqrt(d);
-      r[k * nb + k] = make_double2(d, 0.0);
-      piv = d;
-    }
-    __syncthreads();
-    const double inv = 1.0 / piv;
-    for (int j = k + 1 + threadIdx.x; j < nb; j += blockDim.x) {
-      double2 v = r[k * nb + j];
-      r[k * nb + j] = make_double2(v.x * inv, v.y * inv);
-    }
-    __syncthreads();
-    const int m = nb - k - 1;
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int i = k + 1 + e / m, j = k + 1 + e % m;
-      if (j >= i) {
-        const double2 a = r[k * nb + i], b = r[k * nb + j];
-        double2 v = r[i * nb + j];
-        // v -= conj(a) * b
-        v.x -= a.x * b.x + a.y * b.y;
-        v.y -= a.x * b.y - a.y * b.x;
-        r[i * nb + j] = v;
-      }
-    }
-    __syncthreads();
-  }
-  // Rinv: back substitution, one column per thread
-  for (int j = threadIdx.x; j < nb; j += blockDim.x) {
-    for (int i = 0; i < nb; ++i) ri[i * nb + j] = make_double2(0.0, 0.0);
-    const double djj = r[j * nb + j].x;
-    ri[j * nb + j] = make_double2(1.0 / djj, 0.0);
-    for (int i = j - 1; i >= 0; --i) {
-      double sx = 0.0, sy = 0.0;
-      for (int l = i + 1; l <= j; ++l) {
-        const double2 a = r[i * nb + l], b = ri[l * nb + j];
-        sx += a.x * b.x - a.y * b.y;
-        sy += a.x * b.y + a.y * b.x;
-      }
-      const double dii = r[i * nb + i].x;
-      ri[i * nb + j] = make_double2(-sx / dii, -sy / dii);
-    }
-  }
-  if (SMEM) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-      Rm[off + e] = r[e];
-      Ri[off + e] = ri[e];
-    }
-  }
-}
-
 // 1/sqrt(d) for d > 0 without the FP64 square-root/division sequences:
 // FP32 seed refined by three Newton steps in FP64 (multiplies and adds only).
 __device__ __forceinline__ double rsqrt_fp64(double d) {
@@ -262,70 +185,6 @@ __device__ __forceinline__ double rsqrt_fp64(double d) {
   r = r * (1.5 - 0.5 * d * r * r);
   r = r * (1.5 - 0.5 * d * r * r);
   return r;
-}
-
-// nb <= 32: one warp per (s,k), lane j owns column j of R (in shared memory);
-// pivots broadcast with shuffles, no block barriers, no FP64 divisions.
-__global__ void __launch_bounds__(32) k_cholesky_inv_warp(const double2* __restrict__ S,
-                                                          double2* __restrict__ Rm,
-                                                          double2* __restrict__ Ri, int nb,
-                                                          int* __restrict__ flags) {
-  __shared__ double2 r[32][33];
-  __shared__ double2 ri[32][33];
-  __shared__ double dinv[32];
-  const int sk = blockIdx.x, j = threadIdx.x;
-  const size_t off = (size_t)sk * nb * nb;
-  const double2* s = S + off;
-  for (int i = 0; i < nb; ++i) {
-    if (j < nb) {
-      const double2 a = s[i * nb + j], b = s[j * nb + i];
-      r[i][j] = (j >= i) ? make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)) : make_double2(0.0, 0.0);
-    }
-  }
-  __syncwarp();
-  bool bad = false;
-  for (int k = 0; k < nb; ++k) {
-    double d = r[k][k].x;   // every lane reads the pivot
-    if (!(d > 0.0) || !isfinite(d)) { bad = true; d = 1.0; }
-    const double rs = rsqrt_fp64(d);
-    __syncwarp();
-    if (j == k) { r[k][k] = make_double2(d * rs, 0.0); dinv[k] = rs; }
-    if (j > k && j < nb) { const double2 v = r[k][j]; r[k][j] = make_double2(v.x * rs, v.y * rs); }
-    __syncwarp();
-    if (j > k && j < nb) {
-      const double2 b = r[k][j];
-      for (int i = k + 1; i <= j; ++i) {
-        const double2 a = r[k][i];
-        double2 v = r[i][j];
-        v.x -= a.x * b.x + a.y * b.y;
-        v.y -= a.x * b.y - a.y * b.x;
-        r[i][j] = v;
-      }
-    }
-    __syncwarp();
-  }
-  if (bad && j == 0) atomicOr(flags, 1);
-  // column j of R^{-1} by back substitution with the stored reciprocal pivots
-  if (j < nb) {
-    for (int i = 0; i < nb; ++i) ri[i][j] = make_double2(0.0, 0.0);
-    ri[j][j] = make_double2(dinv[j], 0.0);
-    for (int i = j - 1; i >= 0; --i) {
-      double sx = 0.0, sy = 0.0;
-      for (int l = i + 1; l <= j; ++l) {
-        const double2 a = r[i][l], b = ri[l][j];
-        sx += a.x * b.x - a.y * b.y;
-        sy += a.x * b.y + a.y * b.x;
-      }
-      ri[i][j] = make_double2(-sx * dinv[i], -sy * dinv[i]);
-    }
-  }
-  __syncwarp();
-  for (int i = 0; i < nb; ++i) {
-    if (j < nb) {
-      Rm[off + i * nb + j] = r[i][j];
-      Ri[off + i * nb + j] = ri[i][j];
-    }
-  }
 }
 
 // nb <= 32: one CTA of nb*nb threads per (s,k), thread (i, j) owns element
@@ -392,6 +251,74 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __res
   if (live) {
     Rm[off + i * nb + j] = r[i][j];
     Ri[off + i * nb + j] = x[i][j];
+  }
+}
+
+// nb > 32: the same element-parallel algorithm with the matrices in the
+// output buffers (global memory, L1/L2 resident) and 1024 threads looping
+// over the elements of each phase.
+__global__ void __launch_bounds__(1024) k_cholesky_inv_big(const double2* __restrict__ S,
+                                                           double2* __restrict__ Rm,
+                                                           double2* __restrict__ Ri, double* dinv_g,
+                                                           int nb, int* __restrict__ flags) {
+  const int sk = blockIdx.x;
+  const size_t off = (size_t)sk * nb * nb;
+  double2* r = Rm + off;
+  double2* x = Ri + off;
+  double* dinv = dinv_g + (size_t)sk * nb;
+  const int n2 = nb * nb;
+  for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+    const int i = e / nb, j = e % nb;
+    const double2 a = S[off + e], b = S[off + (size_t)j * nb + i];
+    r[e] = (j >= i) ? make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)) : make_double2(0.0, 0.0);
+    x[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (threadIdx.x == 0) {
+      double d = r[(size_t)k * nb + k].x;
+      if (!(d > 0.0) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
+      const double rs = rsqrt_fp64(d);
+      r[(size_t)k * nb + k] = make_double2(d * rs, 0.0);
+      dinv[k] = rs;
+    }
+    __syncthreads();
+    const double rs = dinv[k];
+    for (int j = k + 1 + threadIdx.x; j < nb; j += blockDim.x) {
+      const double2 v = r[(size_t)k * nb + j];
+      r[(size_t)k * nb + j] = make_double2(v.x * rs, v.y * rs);
+    }
+    __syncthreads();
+    const int m = nb - k - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = k + 1 + e / m, j = k + 1 + e % m;
+      if (j >= i) {
+        const double2 a = r[(size_t)k * nb + i], b = r[(size_t)k * nb + j];
+        double2 v = r[(size_t)i * nb + j];
+        v.x -= a.x * b.x + a.y * b.y;
+        v.y -= a.x * b.y - a.y * b.x;
+        r[(size_t)i * nb + j] = v;
+      }
+    }
+    __syncthreads();
+  }
+  for (int k = nb - 1; k >= 0; --k) {
+    const double dk = dinv[k];
+    for (int j = k + threadIdx.x; j < nb; j += blockDim.x) {
+      const double2 v = x[(size_t)k * nb + j];
+      x[(size_t)k * nb + j] = make_double2(v.x * dk, v.y * dk);
+    }
+    __syncthreads();
+    const int w = nb - k;
+    for (int e = threadIdx.x; e < k * w; e += blockDim.x) {
+      const int i = e / w, j = k + e % w;
+      const double2 a = r[(size_t)i * nb + k], b = x[(size_t)k * nb + j];
+      double2 v = x[(size_t)i * nb + j];
+      v.x -= a.x * b.x - a.y * b.y;
+      v.y -= a.x * b.y + a.y * b.x;
+      x[(size_t)i * nb + j] = v;
+    }
+    __syncthreads();
   }
 }
 
@@ -562,18 +489,11 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
 }
 
 int launch_cholesky_inv(const double2* S, double2* Rm, double2* Ri, int nsk, int nb, int* flags,
-                        cudaStream_t st) {
+                        double* dinv_scratch, cudaStream_t st) {
   if (nb <= 32) {
     k_cholesky_inv_elem<<<nsk, ((nb * nb + 31) / 32) * 32, 0, st>>>(S, Rm, Ri, nb, flags);
-  } else if (nb <= 64) {
-    const size_t sm = 2 * sizeof(double2) * (size_t)nb * nb;
-    if (sm > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(k_cholesky_inv<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(cholesky)");
-    }
-    k_cholesky_inv<true><<<nsk, 256, sm, st>>>(S, Rm, Ri, nb, flags);
   } else {
-    k_cholesky_inv<false><<<nsk, 256, 0, st>>>(S, Rm, Ri, nb, flags);
+    k_cholesky_inv_big<<<nsk, 1024, 0, st>>>(S, Rm, Ri, dinv_scratch, nb, flags);
   }
   JRG_LAUNCH_CHECK("k_cholesky_inv");
   return JRG_OK;

@@ -56,6 +56,7 @@ class MLP:
     w[-1] = 0.5413248546129181        # softplus(b4) = 1: start at the plain update
     self.w32 = torch.tensor(w, device=self.device)
     self.wb = torch.empty(NUM_PARAMS, dtype=torch.bfloat16, device=self.device)
+    self.horizon = 300          # total_steps the step feature x3 was trained with
     self.sync()
 
   def sync(self):
@@ -63,10 +64,12 @@ class MLP:
     _lib.check(_lib.load().jrg_mlp_to_bf16(_p(self.w32), _p(self.wb), _st()), "jrg_mlp_to_bf16")
 
   def state_dict(self):
-    return {"w32": self.w32.detach().cpu().numpy()}
+    return {"w32": self.w32.detach().cpu().numpy(), "horizon": np.array(self.horizon)}
 
   def load_state_dict(self, d):
     self.w32.copy_(torch.as_tensor(d["w32"], device=self.device))
+    if "horizon" in d:
+      self.horizon = int(np.asarray(d["horizon"]))
     self.sync()
 
   def save(self, path):
@@ -147,11 +150,18 @@ def evaluate_loss(mlp: MLP, records: dict) -> float:
   return float(loss.item()) / records["x"].shape[0]
 
 
+DEFAULT_WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__file__), "data",
+                                             "precond_si_c_al.npz")
+
+
 class GuardedScale:
   """scale_fn for calc.Minimizer: learned scales, plain fallback after the
-  energy rises above its best value by more than ``rise_tol``."""
+  energy rises above its best value by more than ``rise_tol``.  The step
+  feature is step / total_steps (the network's training horizon by default)."""
 
-  def __init__(self, mlp: MLP, total_steps: int, smax: float = 8.0, rise_tol: float = 0.0):
+  def __init__(self, mlp: MLP, total_steps: Optional[int] = None, smax: float = 4.0,
+               rise_tol: float = 0.0):
+    total_steps = total_steps or mlp.horizon
     self.mlp, self.total, self.smax, self.rise_tol = mlp, total_steps, smax, rise_tol
     self.best = None
     self.fallback_at = None

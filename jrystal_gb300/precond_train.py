@@ -60,6 +60,7 @@ def fit(rounds=3, ncells=64, steps=300, per_step=6, smax=4.0, grids=(24, 27, 32,
   trajectories of ``refine_steps`` steps run under the current network (the
   horizon of the step feature x3 is refine_steps from round 2 on)."""
   mlp = precond.MLP(seed=3)
+  mlp.horizon = steps if rounds == 1 else refine_steps
   t0 = time.time()
   R = generate(ncells, steps, per_step, 2, grids)
   log(f"round 1: {R['x'].shape[0]} records from plain trajectories ({time.time() - t0:.1f} s)")
@@ -73,7 +74,7 @@ def fit(rounds=3, ncells=64, steps=300, per_step=6, smax=4.0, grids=(24, 27, 32,
   return mlp
 
 
-def run_pair(wl, mlp, nsteps, smax=4.0, total=1500, lr=1e-2):
+def run_pair(wl, mlp, nsteps, smax=4.0, total=None, lr=1e-2):
   """Plain and learned histories (energy per step) and ms per step of each."""
   plan = _plan(wl)
   out = {}
@@ -96,7 +97,7 @@ def run_pair(wl, mlp, nsteps, smax=4.0, total=1500, lr=1e-2):
 
 
 def evaluate(mlp, ncells=16, nsteps=8000, seed=99, grids=(24, 27, 32), smax=4.0, tol=1e-5,
-             total=1500):
+             total=None):
   rng = np.random.default_rng(seed)
   rows = []
   for j in range(ncells):
@@ -125,7 +126,7 @@ def main():
   ap = argparse.ArgumentParser()
   ap.add_argument("--out", required=True)
   ap.add_argument("--eval-json", default=None)
-  ap.add_argument("--rounds", type=int, default=3)
+  ap.add_argument("--rounds", type=int, default=1)
   ap.add_argument("--eval-cells", type=int, default=16)
   ap.add_argument("--eval-steps", type=int, default=8000)
   ap.add_argument("--refine-steps", type=int, default=1500)
@@ -133,7 +134,7 @@ def main():
   mlp = fit(rounds=args.rounds, refine_steps=args.refine_steps)
   mlp.save(args.out)
   if args.eval_json:
-    res = evaluate(mlp, ncells=args.eval_cells, nsteps=args.eval_steps, total=args.refine_steps)
+    res = evaluate(mlp, ncells=args.eval_cells, nsteps=args.eval_steps)
     with open(args.eval_json, "w") as f:
       json.dump(res, f, indent=1)
     print(json.dumps({k: v for k, v in res.items() if k != "cells"}))
