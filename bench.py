@@ -43,6 +43,8 @@ def _args():
   p.add_argument("--no-time-to-tol", action="store_true",
                  help="skip the learned-vs-plain time-to-tolerance runs")
   p.add_argument("--cpu-sample-kpts", type=int, default=1)
+  p.add_argument("--step", default="split", choices=["split", "fused"],
+                 help="split: jrg_energy_grad then jrg_adam_update; fused: jrg_energy_grad_adam")
   p.add_argument("--kgrid", type=int, nargs=3, default=None,
                  help="override the workload's k-grid (smaller cases for profiling)")
   return p.parse_args()
@@ -178,8 +180,9 @@ def _config(wl, n):
           "l2": "no explicit flush: each step streams >0.7 GB of plane buffers, >5x the 129 MB L2"}
 
 
-# algorithmic bytes per call of each phase of jrg_energy_grad
-def phase_bytes(plan):
+# algorithmic bytes per call of each phase of jrg_energy_grad (fused: the
+# adjoint rotation also reads and writes the parameters and both moments)
+def phase_bytes(plan, fused=False):
   c = 8 if plan.precision == 32 else 16
   r = c // 2
   nbt = plan.num_spin * plan.num_kpt * plan.num_band
@@ -200,7 +203,7 @@ def phase_bytes(plan):
     "line_apply_v": nbt * 2 * planes + nsk * ngrid * r,
     "plane_fwd_sphere": nbt * (planes + 2 * sph) + plan.num_kpt * plan.num_g * 8,
     "adj_gram": 2 * nbt * sph,
-    "adj_rotate": 2 * nbt * sph + nbt * sph,
+    "adj_rotate": 2 * nbt * sph + (6 if fused else 1) * nbt * sph,
   }
 
 
@@ -249,9 +252,13 @@ def run_ours(args, wl):
   occ = torch.tensor(wl.occupation, dtype=torch.float64, device=dev)
   state = {"t": 0}
 
+  fused = args.step == "fused" and wl.num_band <= 32
+
   def step(p):
-    e, _, _ = plan.energy_and_grad(p[0], p[1], occ, grads[0], grads[1])
     state["t"] += 1
+    if fused:   # Adam in the epilogue of the gradient kernel
+      return plan.energy_grad_adam(p, m, v, occ, state["t"], wl.lr)
+    e, _, _ = plan.energy_and_grad(p[0], p[1], occ, grads[0], grads[1])
     adam_update(p, grads, m, v, state["t"], wl.lr)
     return e
 
@@ -314,7 +321,7 @@ def run_ours(args, wl):
 
   if rank == 0:
     peak, peak_kind = _peaks()
-    pb = phase_bytes(plan)
+    pb = phase_bytes(plan, fused)
     top = max((k for k in phases if k in pb), key=lambda k: phases[k])
     achieved = pb[top] / (phases[top] * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -106,6 +106,31 @@ int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
                     const double* occupation, double* energies, void* grad_re,
                     void* grad_im, void* workspace, cudaStream_t stream);
 
+/* One optimiser step (no counterpart in the reference as one call: it
+ * fuses value_and_grad(total_energy) and optax.adam's update of
+ * jrystal/calc/calc_ground_state_energy_all_electrons.py:175-190).
+ * The energies (as jrg_energy_grad) are those of the parameters before the
+ * update; the Adam update of jrg_adam_update runs in the epilogue of the
+ * kernel that forms the gradient, so the gradient is written only when grad
+ * is given.  params, m, v, grad: [2][S][K][G][B] (real parts, then
+ * imaginary parts), updated in place.  scale, when given, multiplies each
+ * update element ([2][S][K][G][B] FP32); with mlp_w32/mlp_wb given it is
+ * first overwritten with the learned preconditioner's scales
+ * (jrg_precond_scale at step fraction t_frac, cap smax) computed inside the
+ * step from this step's band kinetic energies.  num_spin 1, num_band <= 32. */
+typedef struct {
+  int step;                 /* 1-based Adam step */
+  double lr, b1, b2, eps;
+  float* scale;             /* optional */
+  const float* mlp_w32;     /* optional learned preconditioner (FP32 and BF16 copies) */
+  const void* mlp_wb;
+  float t_frac, smax;
+} jrg_adam_step;
+
+int jrg_energy_grad_adam(const jrg_plan* plan, void* params, void* m, void* v,
+                         const double* occupation, const jrg_adam_step* opt, double* energies,
+                         void* grad, void* workspace, cudaStream_t stream);
+
 /* Effective potential from a density [S][nx][ny][nz] (S must be 1):
  * out [3][nx][ny][nz] real = Hartree, external, xc parts (split form) with
  * jrystal's conventions: kohn_sham=0 halves Hartree and gives the xc energy
@@ -180,11 +205,12 @@ int jrg_precond_scale(const jrg_plan* plan, const float* w32, const void* wb, fl
 int jrg_band_kinetic(const jrg_plan* plan, const void* workspace, double* out, cudaStream_t stream);
 int jrg_kinetic_table(const jrg_plan* plan, double* out, cudaStream_t stream);
 
-/* Selects the register-resident slab kernels for cubic grids N^3 with
- * N in {16, 24, 27, 32, 36, 48, 64, 96} (enable = 1, the default) or the
- * generic shared-memory Stockham kernels for every grid (enable = 0);
- * enable < 0 only queries.  Returns the previous setting.  Process-wide;
- * no reference counterpart. */
+/* Selects the specialised kernels (enable = 1, the default): register-
+ * resident slab FFTs for cubic grids N^3 with N in {16, 24, 27, 32, 36, 48,
+ * 64, 96} and register-blocked Gram contractions for num_band <= 32; or the
+ * generic ones (enable = 0): shared-memory Stockham FFTs for every grid and
+ * 32x32-tiled Gram contractions.  enable < 0 only queries.  Returns the
+ * previous setting.  Process-wide; no reference counterpart. */
 int jrg_fast_paths(int enable);
 
 /* Selects tensor-core (mma.sync TF32, three-product hi/lo split) Gram and

@@ -23,6 +23,24 @@ XC_FLAGS = {"lda_x": 1, "lda_c_vwn": 2}
 
 # exported entry points and their argument types
 _vp = ct.c_void_p
+
+
+class AdamStep(ct.Structure):
+  """jrg_adam_step."""
+  _fields_ = [
+    ("step", ct.c_int),
+    ("lr", ct.c_double),
+    ("b1", ct.c_double),
+    ("b2", ct.c_double),
+    ("eps", ct.c_double),
+    ("scale", ct.c_void_p),
+    ("mlp_w32", ct.c_void_p),
+    ("mlp_wb", ct.c_void_p),
+    ("t_frac", ct.c_float),
+    ("smax", ct.c_float),
+  ]
+
+
 _SIGS = {
   "jrg_version": ([], ct.c_int),
   "jrg_last_error": ([], ct.c_char_p),
@@ -33,6 +51,8 @@ _SIGS = {
   "jrg_coeff": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
   "jrg_density": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
   "jrg_energy_grad": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
+  "jrg_energy_grad_adam": ([_vp, _vp, _vp, _vp, _vp, ct.POINTER(AdamStep), _vp, _vp, _vp, _vp],
+                           ct.c_int),
   "jrg_potential": ([_vp, _vp, ct.c_int, _vp, _vp, _vp], ct.c_int),
   "jrg_fft3d_workspace_size": ([ct.c_int, ct.POINTER(ct.c_int), ct.c_int,
                                 ct.POINTER(ct.c_size_t)], ct.c_int),

@@ -72,11 +72,19 @@ class Minimizer:
   params: tensor (2, S, K, G, B) holding w_re and w_im.  ``scale_fn``, when
   given, is called as scale_fn(minimizer) before each update and returns a
   float32 tensor of one positive scale per parameter element (the learned
-  diagonal preconditioner) or None for the plain update."""
+  diagonal preconditioner) or None for the plain update.  A scale_fn with an
+  ``in_step(minimizer)`` method (precond.GuardedScale) instead hands the
+  network to the device step, which evaluates it between the kinetic and the
+  density phases.  With ``fused`` (one spin channel, at most 32 bands) the
+  Adam update runs in the epilogue of the gradient kernel and ``grads`` is
+  only filled when ``keep_grad`` is set; the split path (gradient kernel,
+  then a separate Adam kernel) is the default because it is the faster of
+  the two on the 64^3 Si8 cell (2.23 vs 2.32 ms per step)."""
 
   def __init__(self, plan: PlaneWavePlan, occupation, params: torch.Tensor, lr: float = 1e-2,
                b1: float = 0.9, b2: float = 0.99, eps: float = 1e-8, scale_fn=None,
-               total_steps: Optional[int] = None):
+               total_steps: Optional[int] = None, fused: bool = False,
+               keep_grad: bool = False):
     self.plan = plan
     self.occ = torch.as_tensor(np.asarray(occupation), dtype=torch.float64, device=plan.device)
     if tuple(params.shape) != (2,) + plan.param_shape:
@@ -90,6 +98,9 @@ class Minimizer:
     self.total_steps = total_steps
     self.scale_fn = scale_fn
     self.last_scale = None
+    supported = plan.num_spin == 1 and plan.num_band <= 32
+    self.fused = fused and supported
+    self.keep_grad = keep_grad
 
   def energy_and_grad(self):
     e, _, _ = self.plan.energy_and_grad(self.params[0], self.params[1], self.occ, self.grads[0],
@@ -98,6 +109,15 @@ class Minimizer:
 
   def step(self) -> torch.Tensor:
     """One update; returns the device energy vector of the parameters before it."""
+    in_step = getattr(self.scale_fn, "in_step", None)
+    if self.fused and (self.scale_fn is None or in_step is not None):
+      self.t += 1
+      spec = in_step(self) if in_step is not None else None
+      kw = {} if spec is None else dict(mlp=spec[0], t_frac=spec[1], smax=spec[2], scale=spec[3])
+      self.last_scale = None if spec is None else spec[3]
+      return self.plan.energy_grad_adam(self.params, self.m, self.v, self.occ, self.t, self.lr,
+                                        self.b1, self.b2, self.eps,
+                                        grad=self.grads if self.keep_grad else None, **kw)
     e = self.energy_and_grad()
     self.t += 1
     scale = self.scale_fn(self) if self.scale_fn is not None else None

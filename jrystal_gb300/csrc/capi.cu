@@ -38,6 +38,7 @@ template <typename R> int launch_geometry_tables(double*, double*, void*, const 
 int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
 template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t);
 int launch_twiddles(int n, int prec, void* out, cudaStream_t st);
+template <typename R> int launch_rotate_adam(const void*, const double2*, const void*, const double2*, const AdamArgs&, int, int, int, double, cudaStream_t);
 int launch_lda(int prec, long long n, int xc, int ks, const void* rho, void* out, cudaStream_t st);
 
 static thread_local std::string g_err;
@@ -414,7 +415,8 @@ static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* 
 
 template <typename R>
 static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
-                            double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
+                            double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st,
+                            const AdamArgs* adam = nullptr) {
   using C = C_t<R>;
   const Workspace& w = P->ws;
   const int nsk = P->ns * P->nk;
@@ -428,6 +430,14 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
     PHASE(PH_KINETIC);
     if ((rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, occ, slots, (double*)wsp(ws, w.ekin), nbt,
                                 P->ng, P->nb, P->nk, st)))
+      return rc;
+  }
+  if (adam && adam->mlp_w32) {
+    // learned update scales from this step's band kinetic energies
+    PHASE(PH_PRECOND);
+    if ((rc = launch_precond_scale(adam->mlp_w32, adam->mlp_wb, P->d.tk, (const double*)wsp(ws, w.ekin),
+                                   occ, P->nk, P->ng, P->nb, (long long)nbt * P->ng, adam->t_frac,
+                                   adam->smax, adam->scale[0], st)))
       return rc;
   }
   void* rho = wsp(ws, w.rho);
@@ -451,8 +461,8 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
     if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st)))
       return rc;
   }
-  if (!g_re && !g_im) return JRG_OK;
-  if (!g_re || !g_im) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
+  if (!adam && !g_re && !g_im) return JRG_OK;
+  if (!adam && (!g_re || !g_im)) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
   // adjoint: planes -> x lines (x V) -> planes -> sphere gradient
   {
     PHASE(PH_LINE_APPLY_V);
@@ -482,6 +492,9 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
       return rc;
   }
   PHASE(PH_ADJ_ROTATE);
+  if (adam)
+    return launch_rotate_adam<R>(wsp(ws, w.gc), rh, wsp(ws, w.c), negm2, *adam, nsk, P->ng, P->nb,
+                                 2.0, st);
   return launch_rotate<R>(kRotGSplit, kBand, wsp(ws, w.gc), nullptr, rh, wsp(ws, w.c), negm2, g_re,
                           g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st);
 }
@@ -555,6 +568,35 @@ int jrg_energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const
   if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad: spin-polarised LDA is not implemented");
   return P->prec == 64 ? energy_grad<double>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st)
                        : energy_grad<float>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st);
+}
+
+int jrg_energy_grad_adam(const jrg_plan* P, void* params, void* m, void* v, const double* occ,
+                         const jrg_adam_step* opt, double* energies, void* grad, void* ws,
+                         cudaStream_t st) {
+  if (!P || !params || !m || !v || !occ || !opt || !energies || !ws || opt->step < 1)
+    return fail(JRG_ERR_INVALID, "jrg_energy_grad_adam: bad argument");
+  if (opt->mlp_w32 && (!opt->mlp_wb || !opt->scale))
+    return fail(JRG_ERR_INVALID, "jrg_energy_grad_adam: the learned scale needs mlp_wb and a scale buffer");
+  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_adam: spin-polarised LDA is not implemented");
+  if (P->nb > 32) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_adam: num_band > 32");
+  const size_t n = (size_t)P->ns * P->nk * P->ng * P->nb;
+  const size_t half = n * (P->prec == 64 ? 8 : 4);
+  auto hi = [&](void* b) { return b ? (void*)((char*)b + half) : nullptr; };
+  AdamArgs a;
+  a.p[0] = params; a.p[1] = hi(params);
+  a.m[0] = m; a.m[1] = hi(m);
+  a.v[0] = v; a.v[1] = hi(v);
+  a.scale[0] = opt->scale; a.scale[1] = opt->scale ? opt->scale + n : nullptr;
+  a.grad[0] = grad; a.grad[1] = hi(grad);
+  a.lr = opt->lr; a.b1 = opt->b1; a.b2 = opt->b2; a.eps = opt->eps;
+  a.c1 = 1.0 - std::pow(opt->b1, opt->step);
+  a.c2 = 1.0 - std::pow(opt->b2, opt->step);
+  a.mlp_w32 = opt->mlp_w32; a.mlp_wb = opt->mlp_wb;
+  a.t_frac = opt->t_frac; a.smax = opt->smax;
+  int rc = P->prec == 64 ? energy_grad_impl<double>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a)
+                         : energy_grad_impl<float>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a);
+  profile_call_done(P);
+  return rc;
 }
 
 int jrg_potential(const jrg_plan* P, const void* rho, int ks, void* out, void* ws, cudaStream_t st) {
@@ -668,7 +710,7 @@ namespace {
 const char* kPhaseNames[jrg::PH_COUNT] = {
   "pack_params", "gram", "cholesky_inv", "rotate", "kinetic", "plane_inv_sphere", "line_density",
   "reduce_density", "grid_terms", "line_apply_v", "plane_fwd_sphere", "adj_gram", "adj_small",
-  "adj_rotate"};
+  "adj_rotate", "precond_scale"};
 }
 
 extern "C" {

@@ -50,4 +50,13 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return t;
 }
 
+// optax.adam (scale_by_adam + scale(-lr)) for one element: updates the
+// moments in place and returns the parameter increment.
+template <typename R>
+__device__ __forceinline__ R adam_one(R g, R& m, R& v, R lr, R b1, R b2, R c1, R c2, R eps) {
+  m = b1 * m + (1 - b1) * g;
+  v = b2 * v + (1 - b2) * g * g;
+  return -lr * (m / c1) / (sqrt(v / c2) + eps);
+}
+
 }  // namespace jrg

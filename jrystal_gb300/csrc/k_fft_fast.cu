@@ -484,8 +484,13 @@ template int dispatch_dense<double>(const FftAxis*, const C_t<double>*, int, int
 }  // namespace fast
 }  // namespace jrg
 
+namespace jrg { void set_gram_rb(bool on); }
+
 extern "C" int jrg_fast_paths(int enable) {
   const int prev = jrg::fast::g_fast_enabled ? 1 : 0;
-  if (enable >= 0) jrg::fast::g_fast_enabled = enable != 0;
+  if (enable >= 0) {
+    jrg::fast::g_fast_enabled = enable != 0;
+    jrg::set_gram_rb(enable != 0);
+  }
   return prev;
 }

@@ -337,12 +337,6 @@ __global__ void k_ewald_finish(const double* __restrict__ slots, int nslots, con
 // ------------------------------------------------------------------------
 // Adam (optax placement of eps) with optional elementwise update scale
 // ------------------------------------------------------------------------
-template <typename R>
-__device__ __forceinline__ R adam_one(R& p, R g, R& m, R& v, R lr, R b1, R b2, R c1, R c2, R eps) {
-  m = b1 * m + (1 - b1) * g;
-  v = b2 * v + (1 - b2) * g * g;
-  return -lr * (m / c1) / (sqrt(v / c2) + eps);
-}
 
 template <typename R>
 __global__ void k_adam(R* __restrict__ p, const R* __restrict__ g, R* __restrict__ m,
@@ -361,10 +355,10 @@ __global__ void k_adam(R* __restrict__ p, const R* __restrict__ g, R* __restrict
       float4 mm = reinterpret_cast<float4*>(m)[q];
       float4 vv = reinterpret_cast<float4*>(v)[q];
       float4 u;
-      u.x = adam_one<float>(pp.x, gg.x, mm.x, vv.x, lr, b1, b2, c1, c2, eps);
-      u.y = adam_one<float>(pp.y, gg.y, mm.y, vv.y, lr, b1, b2, c1, c2, eps);
-      u.z = adam_one<float>(pp.z, gg.z, mm.z, vv.z, lr, b1, b2, c1, c2, eps);
-      u.w = adam_one<float>(pp.w, gg.w, mm.w, vv.w, lr, b1, b2, c1, c2, eps);
+      u.x = adam_one<float>(gg.x, mm.x, vv.x, lr, b1, b2, c1, c2, eps);
+      u.y = adam_one<float>(gg.y, mm.y, vv.y, lr, b1, b2, c1, c2, eps);
+      u.z = adam_one<float>(gg.z, mm.z, vv.z, lr, b1, b2, c1, c2, eps);
+      u.w = adam_one<float>(gg.w, mm.w, vv.w, lr, b1, b2, c1, c2, eps);
       if (scale) {
         const float4 s = reinterpret_cast<const float4*>(scale)[q];
         u.x *= s.x; u.y *= s.y; u.z *= s.z; u.w *= s.w;
@@ -376,7 +370,7 @@ __global__ void k_adam(R* __restrict__ p, const R* __restrict__ g, R* __restrict
     }
     for (long long i = 4 * n4 + tid; i < n; i += stride) {
       R mi = m[i], vi = v[i];
-      R u = adam_one<R>(p[i], g[i], mi, vi, lr, b1, b2, c1, c2, eps);
+      R u = adam_one<R>(g[i], mi, vi, lr, b1, b2, c1, c2, eps);
       m[i] = mi; v[i] = vi;
       if (scale) u *= (R)scale[i];
       p[i] += u;
@@ -384,7 +378,7 @@ __global__ void k_adam(R* __restrict__ p, const R* __restrict__ g, R* __restrict
   } else {
     for (long long i = tid; i < n; i += stride) {
       R mi = m[i], vi = v[i];
-      R u = adam_one<R>(p[i], g[i], mi, vi, lr, b1, b2, c1, c2, eps);
+      R u = adam_one<R>(g[i], mi, vi, lr, b1, b2, c1, c2, eps);
       m[i] = mi; v[i] = vi;
       if (scale) u *= (R)scale[i];
       p[i] += u;

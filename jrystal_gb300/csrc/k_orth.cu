@@ -8,6 +8,7 @@
 // strict upper triangle of A with Re(diag A) on the diagonal,
 //   g_W = g_C R^{-H} - C (K R^{-H}),  dE/dw_re = 2 Re g_W, dE/dw_im = 2 Im g_W.
 // The internal coefficient layout is band-major: [sk][band][G] complex.
+#include <algorithm>
 #include <type_traits>
 #include "plan.h"
 
@@ -160,6 +161,138 @@ __global__ void __launch_bounds__(256) k_gram_partial(const void* __restrict__ X
       const int i = ti * kGramTile + ty + 16 * a, j = tj * kGramTile + tx + 16 * b;
       if (i < nb && j < nb) part[((sk * nsplit + split) * nb + i) * nb + j] = acc[a][b];
     }
+}
+
+// cp.async (sm_80+) copies of 4, 8 or 16 bytes into shared memory
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(sa), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// num_band <= 32: warp-tiled partial Gram.  A block walks its G range in
+// chunks of 64 G vectors staged in shared memory as [g][band] (cp.async,
+// double-buffered); each of the 8 warps takes 8 G vectors of a chunk and
+// every lane accumulates rows li + 4a (a < NBP/4) by columns lj + 8b
+// (b < NBP/8) of its warp's partial, lane = 8 li + lj: per G vector NBP/4 +
+// NBP/8 shared loads (broadcast within lane groups, conflict-free) feed
+// NBP^2/32 complex multiply-adds.  The warps' partials (FP32 sums of at most
+// split_len / 8 terms on the FP32 path) are reduced in FP64.
+constexpr int kGwCG = 64;   // G vectors per chunk
+
+template <typename R>
+size_t gram_w_smem(int NBP) {
+  const size_t stage = 2 * 2 * (size_t)kGwCG * (NBP + 1) * sizeof(C_t<R>);
+  const size_t red = 8 * (size_t)NBP * NBP * sizeof(double2);
+  return stage > red ? stage : red;
+}
+
+template <typename R, int LX, int LY, int NBP>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
+k_gram_w(const void* __restrict__ X0, const void* __restrict__ X1, const void* __restrict__ Y0,
+         const void* __restrict__ Y1, double2* __restrict__ part, int ng, int nb, int split_len) {
+  using C = C_t<R>;
+  constexpr int CG = kGwCG, LD = NBP + 1, TI = NBP / 4, TJ = NBP / 8;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* xs = reinterpret_cast<C*>(smem_raw);   // [2][CG][LD]
+  C* ys = xs + 2 * CG * LD;                 // [2][CG][LD]
+  const int split = blockIdx.x;
+  const size_t sk = blockIdx.z;
+  const int nsplit = gridDim.x;
+  const int g_begin = split * split_len;
+  const int g_end = min(ng, g_begin + split_len);
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int li = lane >> 3, lj = lane & 7;
+  // zero the padding bands once (rows nb..NBP-1 are never staged)
+  for (int e = t; e < 2 * CG * LD; e += 256) {
+    if (e % LD >= nb) { xs[e] = czero<C>(); ys[e] = czero<C>(); }
+  }
+  auto stage = [&](int buf, int g0) {
+    C* xd = xs + buf * CG * LD;
+    C* yd = ys + buf * CG * LD;
+    for (int e = t; e < CG * nb; e += 256) {
+      int r, c;   // band, chunk column
+      if (LX == LAYOUT_SPLIT) { r = e % nb; c = e / nb; }
+      else { c = e % CG; r = e / CG; }
+      const int g = g0 + c;
+      C* dx = xd + c * LD + r;
+      C* dy = yd + c * LD + r;
+      if (g >= g_end) {
+        *dx = czero<C>();
+        *dy = czero<C>();
+      } else if (LX == LAYOUT_SPLIT) {
+        const size_t o = (sk * ng + g) * nb + r;
+        cp_async<sizeof(R)>(&dx->x, reinterpret_cast<const R*>(X0) + o);
+        cp_async<sizeof(R)>(&dx->y, reinterpret_cast<const R*>(X1) + o);
+        cp_async<sizeof(R)>(&dy->x, reinterpret_cast<const R*>(Y0) + o);
+        cp_async<sizeof(R)>(&dy->y, reinterpret_cast<const R*>(Y1) + o);
+      } else {
+        const size_t o = (sk * nb + r) * ng + g;
+        cp_async<sizeof(C)>(dx, reinterpret_cast<const C*>(X0) + o);
+        cp_async<sizeof(C)>(dy, reinterpret_cast<const C*>(Y0) + o);
+      }
+    }
+    cp_async_commit();
+  };
+  C acc[TI][TJ];
+#pragma unroll
+  for (int a = 0; a < TI; ++a)
+#pragma unroll
+    for (int b = 0; b < TJ; ++b) acc[a][b] = czero<C>();
+  const int nchunk = (g_end - g_begin + CG - 1) / CG;
+  __syncthreads();
+  if (nchunk > 0) stage(0, g_begin);
+  for (int c = 0; c < nchunk; ++c) {
+    if (c + 1 < nchunk) {
+      stage((c + 1) & 1, g_begin + (c + 1) * CG);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const C* xb = xs + (c & 1) * CG * LD + w * (CG / 8) * LD;
+    const C* yb = ys + (c & 1) * CG * LD + w * (CG / 8) * LD;
+    constexpr int QU = (NBP >= 32 && sizeof(R) == 4) ? 1 : 2;
+#pragma unroll QU
+    for (int q = 0; q < CG / 8; ++q) {
+      C x[TI], y[TJ];
+#pragma unroll
+      for (int a = 0; a < TI; ++a) x[a] = xb[q * LD + li + 4 * a];
+#pragma unroll
+      for (int b = 0; b < TJ; ++b) y[b] = yb[q * LD + lj + 8 * b];
+#pragma unroll
+      for (int a = 0; a < TI; ++a)
+#pragma unroll
+        for (int b = 0; b < TJ; ++b) {   // conj(x) * y
+          acc[a][b].x = fma(x[a].x, y[b].x, fma(x[a].y, y[b].y, acc[a][b].x));
+          acc[a][b].y = fma(x[a].x, y[b].y, fma(-x[a].y, y[b].x, acc[a][b].y));
+        }
+    }
+    __syncthreads();
+  }
+  double2* red = reinterpret_cast<double2*>(smem_raw);   // [8][NBP][NBP]
+#pragma unroll
+  for (int a = 0; a < TI; ++a)
+#pragma unroll
+    for (int b = 0; b < TJ; ++b)
+      red[((size_t)w * NBP + li + 4 * a) * NBP + lj + 8 * b] =
+          make_double2((double)acc[a][b].x, (double)acc[a][b].y);
+  __syncthreads();
+  const int nn = nb * nb;
+  for (int e = t; e < nn; e += 256) {
+    const int i = e / nb, j = e - i * nb;
+    double2 v = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const double2 u = red[((size_t)q * NBP + i) * NBP + j];
+      v.x += u.x;
+      v.y += u.y;
+    }
+    part[(sk * nsplit + split) * nn + e] = v;
+  }
 }
 
 __global__ void k_gram_reduce(const double2* __restrict__ part, double2* __restrict__ out,
@@ -361,7 +494,7 @@ __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict
 enum RotOut { ROT_BANDMAJOR = 0, ROT_GMAJOR_C = 1, ROT_GMAJOR_SPLIT = 2 };
 
 template <typename R, int OUT, int J, int LX0, int LX1>
-__global__ void __launch_bounds__(256) k_rotate(const void* __restrict__ X0a, const void* __restrict__ X0b,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_rotate(const void* __restrict__ X0a, const void* __restrict__ X0b,
                                                 const double2* __restrict__ M0,
                                                 const void* __restrict__ X1a, const void* __restrict__ X1b,
                                                 const double2* __restrict__ M1, void* out0,
@@ -387,21 +520,37 @@ __global__ void __launch_bounds__(256) k_rotate(const void* __restrict__ X0a, co
   C acc[J];
 #pragma unroll
   for (int jj = 0; jj < J; ++jj) acc[jj] = czero<C>();
-  auto term = [&](auto lx, const void* xa, const void* xb, const C* mt) {
-    constexpr int L = decltype(lx)::value;
-#pragma unroll 4
-    for (int i = 0; i < nb; ++i) {
-      const C x = load_tall<R, L>(xa, xb, sk, i, g, ng, nb);
+  // rows k < nb come from X0, nb <= k < 2 nb from X1; the loads of the next
+  // P rows are issued before the current P rows are consumed
+  const int K = nterms * nb;
+  auto ld = [&](int k) -> C {
+    if (k >= K) return czero<C>();
+    return k < nb ? load_tall<R, LX0>(X0a, X0b, sk, k, g, ng, nb)
+                  : load_tall<R, LX1>(X1a, X1b, sk, k - nb, g, ng, nb);
+  };
+  constexpr int P = sizeof(R) == 4 ? 8 : 4;
+  C cur[P], nxt[P];
 #pragma unroll
-      for (int jj = 0; jj < J; ++jj) {
-        const C m = mt[i * J + jj];
-        acc[jj].x = fma(x.x, m.x, fma(-x.y, m.y, acc[jj].x));
-        acc[jj].y = fma(x.x, m.y, fma(x.y, m.x, acc[jj].y));
+  for (int q = 0; q < P; ++q) cur[q] = ld(q);
+  for (int k0 = 0; k0 < K; k0 += P) {
+#pragma unroll
+    for (int q = 0; q < P; ++q) nxt[q] = ld(k0 + P + q);
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      if (k0 + q < K) {
+        const C x = cur[q];
+        const C* mt = ms + (size_t)(k0 + q) * J;
+#pragma unroll
+        for (int jj = 0; jj < J; ++jj) {
+          const C m = mt[jj];
+          acc[jj].x = fma(x.x, m.x, fma(-x.y, m.y, acc[jj].x));
+          acc[jj].y = fma(x.x, m.y, fma(x.y, m.x, acc[jj].y));
+        }
       }
     }
-  };
-  term(std::integral_constant<int, LX0>{}, X0a, X0b, ms);
-  if (nterms > 1) term(std::integral_constant<int, LX1>{}, X1a, X1b, ms + (size_t)nb * J);
+#pragma unroll
+    for (int q = 0; q < P; ++q) cur[q] = nxt[q];
+  }
   const size_t base = sk * nb * ng;
   if (OUT == ROT_BANDMAJOR) {
     C* o = reinterpret_cast<C*>(out0) + base;
@@ -419,6 +568,275 @@ __global__ void __launch_bounds__(256) k_rotate(const void* __restrict__ X0a, co
 #pragma unroll
     for (int jj = 0; jj < J; ++jj)
       if (jj < nj) { ore[jj] = fac * acc[jj].x; oim[jj] = fac * acc[jj].y; }
+  }
+}
+
+// ------------------------------------------------------------------------
+// Register-blocked rotation for num_band <= 32 (BANDMAJOR and GMAJOR_SPLIT
+// outputs).  A block owns 256 G vectors of one (s, k): the stacked rows of X
+// (X0 then X1, K = nterms * nb rows) stream through shared memory in chunks of
+// 8 rows with cp.async double buffering, the stacked M (K x NBP, NBP = nb
+// rounded up to 8) sits in shared memory, and each thread accumulates a
+// 4 (G) x NBP/4 (band) block: per row, two 128-bit x loads and NBP/8 128-bit
+// broadcast M loads feed 4 * NBP/4 complex multiply-adds.  G-major outputs
+// are transposed through shared memory and written as coalesced runs.
+constexpr int kRbKC = 8;     // rows per chunk
+constexpr int kRbGT = 256;   // G vectors per block
+
+template <typename R>
+size_t rotate_rb_smem(int K, int NBP) {
+  const size_t KP = (size_t)(K + kRbKC - 1) / kRbKC * kRbKC;
+  const size_t ms = KP * NBP * sizeof(C_t<R>);
+  const size_t xs = 2 * (size_t)kRbKC * kRbGT * sizeof(C_t<R>);
+  const size_t tile = (size_t)kRbGT * (NBP + 1) * sizeof(R);
+  return ms + (xs > tile ? xs : tile);
+}
+
+template <typename R, int LX0, int OUT, int NBP>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
+k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const double2* __restrict__ M0,
+            const void* __restrict__ X1, const double2* __restrict__ M1, void* out0, void* out1,
+            int ng, int nb, R fac) {
+  using C = C_t<R>;
+  constexpr int KC = kRbKC, GT = kRbGT, TG = 4, TJ = NBP / 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nterms = X1 ? 2 : 1;
+  const int K = nterms * nb;
+  const int KP = (K + KC - 1) / KC * KC;
+  C* ms = reinterpret_cast<C*>(smem_raw);        // [KP][NBP]
+  C* xs = ms + (size_t)KP * NBP;                  // [2][KC][GT], then the output tile
+  const size_t sk = blockIdx.y;
+  const int g0 = blockIdx.x * GT;
+  const int t = threadIdx.x;
+  const size_t moff = sk * nb * nb;
+  for (int e = t; e < KP * NBP; e += 256) {
+    const int k = e / NBP, j = e % NBP;
+    double2 v = make_double2(0.0, 0.0);
+    if (k < K && j < nb) v = (k < nb ? M0 : M1)[moff + (size_t)(k < nb ? k : k - nb) * nb + j];
+    ms[e] = cmk<C>(v.x, v.y);
+  }
+  const int gs = g0 + t;            // staging column of this thread
+  const bool gv = gs < ng;
+  auto stage = [&](int buf, int k0) {
+    C* dst = xs + (size_t)buf * KC * GT + t;
+#pragma unroll
+    for (int q = 0; q < KC; ++q) {
+      const int k = k0 + q;
+      C* d = dst + q * GT;
+      if (!gv || k >= K) {
+        *d = czero<C>();
+      } else if (k < nb && LX0 == LAYOUT_SPLIT) {
+        const size_t o = (sk * ng + gs) * nb + k;
+        cp_async<sizeof(R)>(&d->x, reinterpret_cast<const R*>(X0a) + o);
+        cp_async<sizeof(R)>(&d->y, reinterpret_cast<const R*>(X0b) + o);
+      } else {
+        const C* src = k < nb ? reinterpret_cast<const C*>(X0a) : reinterpret_cast<const C*>(X1);
+        const int i = k < nb ? k : k - nb;
+        cp_async<sizeof(C)>(d, src + (sk * nb + i) * ng + gs);
+      }
+    }
+    cp_async_commit();
+  };
+  const int lane = t & 31, w = t >> 5, wj = w & 3, wg = w >> 2;
+  // G columns of this thread: wg * 128 + (a / 2) * 64 + 2 * lane + (a % 2)
+  C acc[TG][TJ];
+#pragma unroll
+  for (int a = 0; a < TG; ++a)
+#pragma unroll
+    for (int b = 0; b < TJ; ++b) acc[a][b] = czero<C>();
+  const int nchunk = KP / KC;
+  stage(0, 0);
+  for (int c = 0; c < nchunk; ++c) {
+    if (c + 1 < nchunk) {
+      stage((c + 1) & 1, (c + 1) * KC);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const C* xb = xs + (size_t)(c & 1) * KC * GT + wg * 128 + 2 * lane;
+#pragma unroll
+    for (int q = 0; q < KC; ++q) {
+      C x[TG], m[TJ];
+#pragma unroll
+      for (int a = 0; a < TG; a += 2) {
+        const C* px = xb + q * GT + (a / 2) * 64;
+        x[a] = px[0];
+        x[a + 1] = px[1];
+      }
+      const C* mr = ms + (size_t)(c * KC + q) * NBP + wj * TJ;
+      if constexpr (sizeof(R) == 4) {
+#pragma unroll
+        for (int b = 0; b < TJ; b += 2) {
+          const float4 v = *reinterpret_cast<const float4*>(mr + b);
+          m[b] = cmk<C>(v.x, v.y);
+          m[b + 1] = cmk<C>(v.z, v.w);
+        }
+      } else {
+#pragma unroll
+        for (int b = 0; b < TJ; ++b) m[b] = mr[b];
+      }
+#pragma unroll
+      for (int a = 0; a < TG; ++a)
+#pragma unroll
+        for (int b = 0; b < TJ; ++b) {
+          acc[a][b].x = fma(x[a].x, m[b].x, fma(-x[a].y, m[b].y, acc[a][b].x));
+          acc[a][b].y = fma(x[a].x, m[b].y, fma(x[a].y, m[b].x, acc[a][b].y));
+        }
+    }
+    __syncthreads();
+  }
+  if constexpr (OUT == ROT_BANDMAJOR) {
+    C* o = reinterpret_cast<C*>(out0) + sk * nb * ng;
+#pragma unroll
+    for (int a = 0; a < TG; ++a) {
+      const int g = g0 + wg * 128 + (a / 2) * 64 + 2 * lane + (a % 2);
+#pragma unroll
+      for (int b = 0; b < TJ; ++b) {
+        const int j = wj * TJ + b;
+        if (g < ng && j < nb) o[(size_t)j * ng + g] = acc[a][b];
+      }
+    }
+  } else {
+    // (S,K,G,B) split real/imag times fac, one part at a time through shared
+    // memory: tile[g_local][band], row stride NBP + 1
+    R* tile = reinterpret_cast<R*>(xs);
+    const size_t base = (sk * ng + g0) * nb;
+    const int len = min(GT, ng - g0) * nb;
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      if (part) __syncthreads();
+#pragma unroll
+      for (int a = 0; a < TG; ++a) {
+        const int gl = wg * 128 + (a / 2) * 64 + 2 * lane + (a % 2);
+#pragma unroll
+        for (int b = 0; b < TJ; ++b)
+          tile[gl * (NBP + 1) + wj * TJ + b] = fac * (part ? acc[a][b].y : acc[a][b].x);
+      }
+      __syncthreads();
+      R* o = reinterpret_cast<R*>(part ? out1 : out0) + base;
+      for (int e = t; e < len; e += 256) {
+        const int r = e / nb;
+        o[e] = tile[r * (NBP + 1) + (e - r * nb)];
+      }
+    }
+  }
+}
+
+// Adam fused into the adjoint rotation: the gradient element
+//   g = fac * sum_t X_t M_t   (split real/imag, (S,K,G,B) layout)
+// is consumed in registers by the optax Adam update of the parameter, its
+// moments and (optionally) the learned scale; grad is written only when
+// requested.
+
+template <typename R, int J>
+__global__ void __launch_bounds__(256) k_rotate_adam(const C_t<R>* __restrict__ X0,
+                                                     const double2* __restrict__ M0,
+                                                     const C_t<R>* __restrict__ X1,
+                                                     const double2* __restrict__ M1, AdamArgs a,
+                                                     int ng, int nb, R fac) {
+  // One block: 256 G vectors x all nb (<= J) bands of one (s, k).  The
+  // gradient tile goes through shared memory so that the parameter and
+  // moment rows of the block (a contiguous run of 256 * nb elements of the
+  // G-major layout) are read and written coalesced.
+  using C = C_t<R>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* ms = reinterpret_cast<C*>(smem_raw);                     // [2][nb][J]
+  R* gs = reinterpret_cast<R*>(ms + 2 * (size_t)nb * J);      // [256][nb + 1]
+  const int ld = nb + 1;
+  const size_t sk = blockIdx.z;
+  const size_t moff = sk * nb * nb;
+  for (int e = threadIdx.x; e < 2 * nb * J; e += blockDim.x) {
+    const int t = e / (nb * J), rem = e % (nb * J);
+    const int i = rem / J, jj = rem % J;
+    const double2* M = t ? M1 : M0;
+    double2 v = (jj < nb) ? M[moff + (size_t)i * nb + jj] : make_double2(0.0, 0.0);
+    ms[e] = cmk<C>(v.x, v.y);
+  }
+  const int g0 = blockIdx.x * blockDim.x;
+  const int g = g0 + threadIdx.x;
+  const size_t base = (sk * ng + g0) * nb;
+  const int len = min(256, ng - g0) * nb;
+  {
+    // pull this block's parameter / moment / scale rows towards L2 while the
+    // contraction runs; every prefetched line starts inside the row range
+    // (or at a 128-byte boundary at or after the buffer start)
+    const void* rows[8] = {a.p[0], a.p[1], a.m[0], a.m[1], a.v[0], a.v[1], a.scale[0], a.scale[1]};
+    const size_t esz[8] = {sizeof(R), sizeof(R), sizeof(R), sizeof(R), sizeof(R), sizeof(R), 4, 4};
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (!rows[q]) continue;
+      const uintptr_t lo = (uintptr_t)rows[q] + base * esz[q];
+      const uintptr_t hi = lo + (size_t)len * esz[q];
+      for (uintptr_t l = (lo & ~(uintptr_t)127) + (uintptr_t)threadIdx.x * 128; l < hi; l += 256 * 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(l));
+    }
+  }
+  __syncthreads();
+  C acc[J];
+#pragma unroll
+  for (int jj = 0; jj < J; ++jj) acc[jj] = czero<C>();
+  if (g < ng) {
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const C* X = (t ? X1 : X0) + sk * nb * ng;
+      const C* mt = ms + (size_t)t * nb * J;
+#pragma unroll 4
+      for (int i = 0; i < nb; ++i) {
+        const C x = X[(size_t)i * ng + g];
+#pragma unroll
+        for (int jj = 0; jj < J; ++jj) {
+          const C m = mt[i * J + jj];
+          acc[jj].x = fma(x.x, m.x, fma(-x.y, m.y, acc[jj].x));
+          acc[jj].y = fma(x.x, m.y, fma(x.y, m.x, acc[jj].y));
+        }
+      }
+    }
+  }
+  const R lr = (R)a.lr, b1 = (R)a.b1, b2 = (R)a.b2, c1 = (R)a.c1, c2 = (R)a.c2, eps = (R)a.eps;
+#pragma unroll
+  for (int part = 0; part < 2; ++part) {
+    if (part) __syncthreads();
+#pragma unroll
+    for (int jj = 0; jj < J; ++jj)
+      if (jj < nb) gs[threadIdx.x * ld + jj] = fac * (part ? acc[jj].y : acc[jj].x);
+    __syncthreads();
+    R* pp = reinterpret_cast<R*>(a.p[part]) + base;
+    R* mp = reinterpret_cast<R*>(a.m[part]) + base;
+    R* vp = reinterpret_cast<R*>(a.v[part]) + base;
+    R* gp = a.grad[part] ? reinterpret_cast<R*>(a.grad[part]) + base : nullptr;
+    const float* sp = a.scale[part] ? a.scale[part] + base : nullptr;
+    // 8 elements per thread in flight: the loads of a chunk are issued
+    // before any of its updates so that the epilogue is not latency bound
+    constexpr int U = 8;
+    for (int e0 = threadIdx.x; e0 < len; e0 += U * 256) {
+      R mi[U], vi[U], pi[U];
+      float si[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + u * 256;
+        if (e < len) {
+          mi[u] = mp[e];
+          vi[u] = vp[e];
+          pi[u] = pp[e];
+          si[u] = sp ? sp[e] : 1.0f;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + u * 256;
+        if (e < len) {
+          const int r = e / nb;
+          const R gr = gs[r * ld + (e - r * nb)];
+          if (gp) gp[e] = gr;
+          R d = adam_one<R>(gr, mi[u], vi[u], lr, b1, b2, c1, c2, eps);
+          if (sp) d *= (R)si[u];
+          mp[e] = mi[u];
+          vp[e] = vi[u];
+          pp[e] = pi[u] + d;
+        }
+      }
+    }
   }
 }
 
@@ -462,6 +880,9 @@ int launch_rotate_tc(int out_kind, int lx0, const void* X0a, const void* X0b, co
                      const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng,
                      int nb, double fac, uint32_t* bscratch, cudaStream_t st);
 static bool g_tc_enabled = false;   // measured slower than the CUDA-core kernels at B <= 32
+static bool g_gram_rb = true;       // register-blocked Gram for B <= 32 (else 32x32 tiles)
+static bool g_rotate_rb = true;     // register-blocked rotation for B <= 32
+void set_gram_rb(bool on) { g_gram_rb = on; g_rotate_rb = on; }
 
 template <typename R>
 int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, const void* Y1,
@@ -471,6 +892,41 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
                                  ng, nb, nsplit, st);
     if (t < 0) return -t;
     if (t > 0) return JRG_OK;
+  }
+  if (nb <= 32 && g_gram_rb) {
+    // about four blocks per SM in total: long G ranges per block keep the
+    // partial-sum traffic small
+    nsplit = std::max(1, std::min(nsplit, (4 * 152 + nsk - 1) / nsk));
+    const int split_len = (ng + nsplit - 1) / nsplit;
+    auto go = [&](auto kern, int nbp) -> int {
+      const size_t sm = gram_w_smem<R>(nbp);
+      if (sm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(gram_w)");
+      }
+      kern<<<dim3(nsplit, 1, nsk), 256, sm, st>>>(X0, X1, Y0, Y1, part, ng, nb, split_len);
+      JRG_LAUNCH_CHECK("k_gram_w");
+      return JRG_OK;
+    };
+    auto pick = [&](auto lxc, auto lyc) -> int {
+      constexpr int A = decltype(lxc)::value, B = decltype(lyc)::value;
+      if (nb <= 8) return go(k_gram_w<R, A, B, 8>, 8);
+      if (nb <= 16) return go(k_gram_w<R, A, B, 16>, 16);
+      if (nb <= 24) return go(k_gram_w<R, A, B, 24>, 24);
+      return go(k_gram_w<R, A, B, 32>, 32);
+    };
+    int rc;
+    if (lx == LAYOUT_SPLIT && ly == LAYOUT_SPLIT)
+      rc = pick(std::integral_constant<int, LAYOUT_SPLIT>{}, std::integral_constant<int, LAYOUT_SPLIT>{});
+    else if (lx == LAYOUT_BAND && ly == LAYOUT_BAND)
+      rc = pick(std::integral_constant<int, LAYOUT_BAND>{}, std::integral_constant<int, LAYOUT_BAND>{});
+    else
+      return fail(JRG_ERR_INVALID, "launch_gram: unsupported layout pair");
+    if (rc) return rc;
+    const size_t n = (size_t)nsk * nb * nb;
+    k_gram_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, out, nsplit, nb, nsk);
+    JRG_LAUNCH_CHECK("k_gram_reduce");
+    return JRG_OK;
   }
   const int split_len = (ng + nsplit - 1) / nsplit;
   const int ntile = (nb + kGramTile - 1) / kGramTile;
@@ -549,6 +1005,35 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
     if (t < 0) return -t;
     if (t > 0) return JRG_OK;
   }
+  if (nb <= 32 && g_rotate_rb && out_kind != ROT_GMAJOR_C &&
+      (lx0 == LAYOUT_BAND || !X1)) {
+    const int K = (X1 ? 2 : 1) * nb;
+    auto go = [&](auto kern, int nbp) -> int {
+      const size_t sm = rotate_rb_smem<R>(K, nbp);
+      if (sm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate_rb)");
+      }
+      kern<<<dim3((ng + kRbGT - 1) / kRbGT, nsk), 256, sm, st>>>(X0a, X0b, M0, X1, M1, out0, out1, ng,
+                                                                 nb, (R)fac);
+      JRG_LAUNCH_CHECK("k_rotate_rb");
+      return JRG_OK;
+    };
+    auto pick = [&](auto lxc, auto outc) -> int {
+      constexpr int L = decltype(lxc)::value, O = decltype(outc)::value;
+      if (nb <= 8) return go(k_rotate_rb<R, L, O, 8>, 8);
+      if (nb <= 16) return go(k_rotate_rb<R, L, O, 16>, 16);
+      if (nb <= 24) return go(k_rotate_rb<R, L, O, 24>, 24);
+      return go(k_rotate_rb<R, L, O, 32>, 32);
+    };
+    using IS = std::integral_constant<int, LAYOUT_SPLIT>;
+    using IB = std::integral_constant<int, LAYOUT_BAND>;
+    using OB = std::integral_constant<int, ROT_BANDMAJOR>;
+    using OS = std::integral_constant<int, ROT_GMAJOR_SPLIT>;
+    if (lx0 == LAYOUT_SPLIT)
+      return out_kind == ROT_BANDMAJOR ? pick(IS{}, OB{}) : pick(IS{}, OS{});
+    return out_kind == ROT_BANDMAJOR ? pick(IB{}, OB{}) : pick(IB{}, OS{});
+  }
   if (out_kind == ROT_BANDMAJOR)
     return rotate_out<R, ROT_BANDMAJOR>(lx0, X0a, X0b, M0, LAYOUT_BAND, X1, nullptr, M1, out0, out1, nsk, ng, nb, fac, st);
   if (out_kind == ROT_GMAJOR_C)
@@ -556,7 +1041,32 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
   return rotate_out<R, ROT_GMAJOR_SPLIT>(lx0, X0a, X0b, M0, LAYOUT_BAND, X1, nullptr, M1, out0, out1, nsk, ng, nb, fac, st);
 }
 
+template <typename R>
+int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const double2* M1,
+                       const AdamArgs& a, int nsk, int ng, int nb, double fac, cudaStream_t st) {
+  using C = C_t<R>;
+  if (nb > 32) return fail(JRG_ERR_UNSUPPORTED, "k_rotate_adam: num_band > 32");
+  auto go = [&](auto kern, int J) -> int {
+    const size_t sm = sizeof(C) * 2 * (size_t)nb * J + sizeof(R) * 256 * (size_t)(nb + 1);
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate_adam)");
+    }
+    dim3 grid((ng + 255) / 256, 1, nsk);
+    kern<<<grid, 256, sm, st>>>(reinterpret_cast<const C*>(X0), M0, reinterpret_cast<const C*>(X1), M1,
+                                a, ng, nb, (R)fac);
+    JRG_LAUNCH_CHECK("k_rotate_adam");
+    return JRG_OK;
+  };
+  if (nb <= 8) return go(k_rotate_adam<R, 8>, 8);
+  if (nb <= 16) return go(k_rotate_adam<R, 16>, 16);
+  if (nb <= 24) return go(k_rotate_adam<R, 24>, 24);
+  return go(k_rotate_adam<R, 32>, 32);
+}
+
 #define JRG_INST_ORTH(R)                                                                        \
+  template int launch_rotate_adam<R>(const void*, const double2*, const void*, const double2*,    \
+                                     const AdamArgs&, int, int, int, double, cudaStream_t);       \
   template int launch_pack_params<R>(const void*, const void*, void*, int, int, int, bool,         \
                                      cudaStream_t);                                             \
   template int launch_unpack<R>(const void*, void*, void*, void*, int, int, int, double,          \

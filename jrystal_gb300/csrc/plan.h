@@ -49,13 +49,28 @@ struct PlanTables {
 enum Phase {
   PH_PACK = 0, PH_GRAM, PH_CHOL, PH_ROTATE, PH_KINETIC, PH_PLANE_INV, PH_LINE_DENSITY,
   PH_REDUCE_DENSITY, PH_GRID_TERMS, PH_LINE_APPLY_V, PH_PLANE_FWD, PH_ADJ_GRAM, PH_ADJ_SMALL,
-  PH_ADJ_ROTATE, PH_COUNT
+  PH_ADJ_ROTATE, PH_PRECOND, PH_COUNT
 };
 struct Profiler {
   int max_calls = 0;
   int calls = 0;                         // calls recorded so far
   std::vector<cudaEvent_t> ev;           // [max_calls][PH_COUNT][2]
   std::vector<unsigned char> used;       // [max_calls][PH_COUNT]
+};
+
+// One fused optimiser step: Adam applied in the epilogue of the adjoint
+// rotation (k_rotate_adam); all buffers [S][K][G][B], index 0 real parts,
+// 1 imaginary parts.
+struct AdamArgs {
+  void* p[2];
+  void* m[2];
+  void* v[2];
+  float* scale[2];        // per-element update scale (optional; learned scales when mlp_w32)
+  void* grad[2];          // gradient output (optional)
+  double lr, b1, b2, c1, c2, eps;
+  const float* mlp_w32;   // learned preconditioner evaluated inside the step (optional)
+  const void* mlp_wb;
+  float t_frac, smax;
 };
 
 // Workspace offsets (bytes) of one plan.

@@ -144,6 +144,38 @@ class PlaneWavePlan:
     _lib.check(st, "jrg_energy_grad")
     return self.energies, grad_re, grad_im
 
+  def energy_grad_adam(self, params: torch.Tensor, m: torch.Tensor, v: torch.Tensor, occupation,
+                       step: int, lr: float, b1: float = 0.9, b2: float = 0.99, eps: float = 1e-8,
+                       scale: Optional[torch.Tensor] = None, mlp=None, t_frac: float = 0.0,
+                       smax: float = 4.0, grad: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """One fused optimiser step in place on params (2,S,K,G,B) and the Adam
+    moments m, v: the energies of the parameters before the update (device
+    float64[8]) are returned.  ``mlp`` (a precond.MLP) makes the learned
+    preconditioner's scales inside the step into ``scale`` (required then);
+    otherwise ``scale`` is an optional input.  ``grad`` receives the gradient."""
+    shape = (2,) + self.param_shape
+    for name, t in (("params", params), ("m", m), ("v", v), ("grad", grad)):
+      if t is None and name == "grad":
+        continue
+      if tuple(t.shape) != shape or t.dtype != self.rdtype or not t.is_contiguous() \
+          or t.device != self.device:
+        raise ValueError(f"{name}: expected contiguous {self.rdtype} {shape} on {self.device}")
+    if scale is not None and (tuple(scale.shape) != shape or scale.dtype != torch.float32
+                              or not scale.is_contiguous()):
+      raise ValueError(f"scale: expected contiguous float32 {shape}")
+    if mlp is not None and scale is None:
+      raise ValueError("the learned scale needs a scale buffer")
+    occ = self._occ(occupation)
+    addr = lambda t: None if t is None else t.data_ptr()
+    opt = _lib.AdamStep(int(step), float(lr), float(b1), float(b2), float(eps), addr(scale),
+                        addr(None if mlp is None else mlp.w32), addr(None if mlp is None else mlp.wb),
+                        float(t_frac), float(smax))
+    st = self.lib.jrg_energy_grad_adam(self._h, _ptr(params), _ptr(m), _ptr(v), _ptr(occ),
+                                       ct.byref(opt), _ptr(self.energies), _ptr(grad),
+                                       _ptr(self.workspace), _stream())
+    _lib.check(st, "jrg_energy_grad_adam")
+    return self.energies
+
   def coeff(self, w_re: torch.Tensor, w_im: torch.Tensor) -> torch.Tensor:
     self._check_param(w_re, "w_re")
     self._check_param(w_im, "w_im")

@@ -173,13 +173,24 @@ class GuardedScale:
     elif self.fallback_at is None and energy > self.best + self.rise_tol:
       self.fallback_at = step
 
-  def __call__(self, mini):
-    if self.fallback_at is not None:
-      return None
+  def _buf(self, mini):
     if self.buf is None:
       self.buf = torch.empty((2,) + mini.plan.param_shape, dtype=torch.float32,
                              device=mini.plan.device)
-    return self.mlp.scale(mini.plan, min(1.0, mini.t / self.total), mini.occ, self.smax, self.buf)
+    return self.buf
+
+  def __call__(self, mini):
+    if self.fallback_at is not None:
+      return None
+    return self.mlp.scale(mini.plan, min(1.0, mini.t / self.total), mini.occ, self.smax,
+                          self._buf(mini))
+
+  def in_step(self, mini):
+    """(mlp, step fraction, cap, scale buffer) for the fused device step, or
+    None after the fallback to the plain update."""
+    if self.fallback_at is not None:
+      return None
+    return self.mlp, min(1.0, mini.t / self.total), self.smax, self._buf(mini)
 
 
 @dataclass

@@ -36,6 +36,10 @@ CASES = [
   dict(kind="si8", grid=(36, 36, 36), kgrid=(1, 1, 1), nb=5, nocc=3),
   dict(kind="si2", grid=(48, 48, 48), kgrid=(1, 1, 1), nb=3, nocc=2),
   dict(kind="si8", grid=(64, 64, 64), kgrid=(1, 1, 1), nb=3, nocc=2),
+  # register-blocked Gram with 2, 3 and 4 rows per thread (9-32 bands)
+  dict(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 1), nb=12, nocc=6),
+  dict(kind="si8", grid=(24, 24, 24), kgrid=(1, 1, 1), nb=20, nocc=16),
+  dict(kind="si8", grid=(16, 16, 16), kgrid=(2, 1, 1), nb=30, nocc=16),
   # more than 32 bands: tiled Gram, 32-wide rotation tiles, global-memory Cholesky
   dict(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 2), nb=40, nocc=20),
 ]
