@@ -35,7 +35,7 @@ UNIT = "evals/s"
 def _args():
   p = argparse.ArgumentParser()
   p.add_argument("--gpus", type=int, default=1)
-  p.add_argument("--steps", type=int, default=20)
+  p.add_argument("--steps", type=int, default=300)
   p.add_argument("--warmup", type=int, default=3)
   p.add_argument("--impl", default="ours", choices=["ours", "reference"])
   p.add_argument("--workload", default="si8_cubic_64")
@@ -85,6 +85,12 @@ class ClockSampler:
          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
       self.t = threading.Thread(target=self._read, daemon=True)
       self.t.start()
+      # wait for nvidia-smi's first sample, then keep only samples taken
+      # inside the region
+      t0 = time.time()
+      while not self.lines and time.time() - t0 < 5.0:
+        time.sleep(0.01)
+      self.lines = []
     except Exception:
       self.proc = None
     return self
@@ -155,8 +161,11 @@ def run_reference(args, wl):
   for _ in range(args.warmup):
     cpu_sample(wl, nks, workers)
   per_eval = []
+  t_start = time.time()
   for _ in range(args.steps):
     per_eval.append(cpu_sample(wl, nks, workers)[0])
+    if time.time() - t_start > 150.0:   # bound the arm to a few minutes
+      break
   t = statistics.median(per_eval)
   val = 1.0 / t
   sample = (f"FP64 NumPy/SciPy restatement of the path (not jrystal: jax is absent), "
@@ -164,6 +173,7 @@ def run_reference(args, wl):
             f"{wl.grid_sizes[0]}^3 grid), time scaled by {wl.num_kpt}/{nks}")
   out = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
          "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+         "steps_sampled": len(per_eval),
          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
          "data": "synthetic", "config": _config(wl, args.gpus),
          "cpu_baseline": {"value": val, "unit": UNIT, "cores": workers, "kind": "port",
@@ -178,6 +188,13 @@ def _config(wl, n):
           "occupied": wl.num_occ, "xc": wl.xc, "precision": f"fp{wl.precision}",
           "parallelism": f"replicas{n}" if n > 1 else "single-gpu",
           "l2": "no explicit flush: each step streams >0.7 GB of plane buffers, >5x the 129 MB L2"}
+
+
+# DRAM bytes (read + write) per band of one k_line_apply_v<float, 64> launch,
+# from the ncu --set full capture of the 64^3 Si8 cell at 2x2x2 k-points (331 MB
+# for 192 bands, profiles/hot_kernels_si8_cubic_64_k8.md); a full launch is
+# scaled by its band count
+LINE_APPLY_V_DRAM_PER_BAND = (196.706304e6 + 133.798656e6) / 192
 
 
 # algorithmic bytes per call of each phase of jrg_energy_grad (fused: the
@@ -324,8 +341,13 @@ def run_ours(args, wl):
     pb = phase_bytes(plan, fused)
     top = max((k for k in phases if k in pb), key=lambda k: phases[k])
     achieved = pb[top] / (phases[top] * 1e-3) / 1e9
+    traffic = None
+    if top == "line_apply_v" and plan.grid == (64, 64, 64) and plan.precision == 32:
+      traffic = LINE_APPLY_V_DRAM_PER_BAND * plan.num_spin * plan.num_kpt * plan.num_band
     roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "traffic_source": None if traffic is None else
+            "ncu dram bytes per band (2x2x2 k-point capture) x bands of this launch",
             "algorithmic_bytes": pb[top], "ms_per_launch": phases[top],
             "phase_ms": {k: round(v, 4) for k, v in phases.items()}}
     out = {"metric": METRIC, "value": 1000.0 / ms * ws, "unit": UNIT, "n_gpus": ws,

@@ -59,4 +59,14 @@ __device__ __forceinline__ R adam_one(R g, R& m, R& v, R lr, R b1, R b2, R c1, R
   return -lr * (m / c1) / (sqrt(v / c2) + eps);
 }
 
+// cp.async (sm_80+) copies of 4, 8 or 16 bytes into shared memory
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(sa), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 }  // namespace jrg

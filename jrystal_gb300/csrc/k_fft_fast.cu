@@ -26,6 +26,11 @@ template <typename R, int N> constexpr int min_blocks_for() {
   return (sizeof(R) == 4 && N <= 64) ? 2 : 1;
 }
 
+// byte offset of the prefetch row buffers in a line kernel's shared memory
+template <typename R, int N> __host__ __device__ constexpr size_t line_pf_offset() {
+  return (sizeof(C_t<R>) * (size_t)(N + 2 * N * N) + sizeof(int) * N + 15) / 16 * 16;
+}
+
 // sphere -> y,z-transformed active planes
 template <typename R, int N>
 __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere(
@@ -86,7 +91,32 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere(
   }
 }
 
-// inverse x transform + occupation-weighted |psi|^2 of a band group
+// Rows [nact][N] of band b for line y go to shared memory with cp.async one
+// band ahead of the transforms (PF, adjoint pass), so that the loads of the
+// next band are in flight while the current one is transformed.
+template <typename R, int N>
+__device__ __forceinline__ void prefetch_row(const C_t<R>* __restrict__ planes, C_t<R>* dst, int b,
+                                             int y, int nact) {
+  using C = C_t<R>;
+  const C* src = planes + (size_t)b * nact * (N * N) + (size_t)y * N;
+  if constexpr ((N * sizeof(C)) % 16 == 0) {
+    constexpr int PER = 16 / sizeof(C);
+    for (int q = threadIdx.x; q < nact * (N / PER); q += blockDim.x) {
+      const int s = q / (N / PER), zz = (q - s * (N / PER)) * PER;
+      cp_async<16>(dst + s * N + zz, src + (size_t)s * (N * N) + zz);
+    }
+  } else {
+    for (int q = threadIdx.x; q < nact * N; q += blockDim.x) {
+      const int s = q / N, zz = q - s * N;
+      cp_async<sizeof(C)>(dst + q, src + (size_t)s * (N * N) + zz);
+    }
+  }
+  cp_async_commit();
+}
+
+// inverse x transform + occupation-weighted |psi|^2 of a band group (one
+// transform per band: the row prefetch of the adjoint pass measured slower
+// here, 0.30 vs 0.25 ms on the 64^3 Si8 cell)
 template <typename R, int N>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_density(
     const C_t<R>* __restrict__ planes, R* __restrict__ rho_part, const double* __restrict__ wband,
@@ -133,7 +163,7 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
 
 // adjoint line pass: inverse x transform, times V(r), forward x transform,
 // active planes written back in place
-template <typename R, int N>
+template <typename R, int N, bool PF>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_apply_v(
     C_t<R>* __restrict__ planes, const R* __restrict__ vr, int nband, int bands_per_group,
     const int* __restrict__ xact, const C_t<R>* __restrict__ tw_g, int nact) {
@@ -144,9 +174,13 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
   C* ex0 = tw + N;
   C* ex1 = ex0 + N * N;
   int* sxact = reinterpret_cast<int*>(ex1 + N * N);
+  C* rowbuf = reinterpret_cast<C*>(smem_raw + line_pf_offset<R, N>());   // [2][nact][N]
   const int y = blockIdx.x, grp = blockIdx.y, tid = threadIdx.x;
   const int z = tid % N, j2 = tid / N;
   for (int i = tid; i < N; i += blockDim.x) { tw[i] = tw_g[i]; sxact[i] = xact[i]; }
+  const int b_begin = grp * bands_per_group;
+  const int b_end = min(nband, b_begin + bands_per_group);
+  if (PF && b_begin < b_end) prefetch_row<R, N>(planes, rowbuf, b_begin, y, nact);
   __syncthreads();
   int slot[N1];
   R vloc[N1];
@@ -155,14 +189,26 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
     slot[j1] = sxact[N2 * j1 + j2];
     vloc[j1] = vr[(size_t)(N2 * j1 + j2) * (N * N) + y * N + z];
   }
-  const int b_begin = grp * bands_per_group;
-  const int b_end = min(nband, b_begin + bands_per_group);
   const C z0 = czero<C>();
   C v[N1];
-  for (int b = b_begin; b < b_end; ++b) {
+  int parity = 0;
+  for (int b = b_begin; b < b_end; ++b, parity ^= 1) {
     C* base = planes + (size_t)b * nact * (N * N) + y * N + z;
+    if constexpr (PF) {
+      if (b + 1 < b_end) {
+        prefetch_row<R, N>(planes, rowbuf + (parity ^ 1) * nact * N, b + 1, y, nact);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();
+      const C* src = rowbuf + parity * nact * N + z;
 #pragma unroll
-    for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : base[(size_t)slot[j1] * (N * N)];
+      for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : src[slot[j1] * N];
+    } else {
+#pragma unroll
+      for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : base[(size_t)slot[j1] * (N * N)];
+    }
     reg::line_step_a<N, +1>(v, tw, j2, ex0, N, z);
     __syncthreads();
     reg::line_step_b<N, +1>(v, j2, ex0, N, z);
@@ -334,6 +380,9 @@ template <typename R, int N> size_t plane_smem() {
 template <typename R, int N> size_t line_smem() {
   return sizeof(C_t<R>) * (size_t)(N + 2 * N * N) + sizeof(int) * N;
 }
+template <typename R, int N> size_t line_pf_smem(int nact) {
+  return line_pf_offset<R, N>() + 2 * sizeof(C_t<R>) * (size_t)nact * N;
+}
 
 static int optin_smem() {
   int dev = 0, v = 0;
@@ -361,6 +410,8 @@ template <typename K> static int prep(K kernel, size_t bytes) {
     return 1;                                                \
   } while (0)
 
+static bool g_line_prefetch = true;   // cp.async row prefetch in the adjoint line kernel
+
 template <typename R, int N>
 static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
   using C = C_t<R>;
@@ -386,10 +437,18 @@ static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
       FAST_LAUNCHED("fast::k_line_density");
     }
     case OP_LINE_APPLY_V: {
-      const size_t sm = line_smem<R, N>();
-      if ((rc = prep(k_line_apply_v<R, N>, sm)) <= 0) return rc;
       const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
-      k_line_apply_v<R, N><<<dim3(N, ngroups), T, sm, st>>>(
+      const size_t smp = line_pf_smem<R, N>(P->nact);
+      if (g_line_prefetch && (long long)smp <= optin_smem()) {
+        if ((rc = prep(k_line_apply_v<R, N, true>, smp)) <= 0) return rc;
+        k_line_apply_v<R, N, true><<<dim3(N, ngroups), T, smp, st>>>(
+            reinterpret_cast<C*>(a.out), reinterpret_cast<const R*>(a.aux), a.nbands,
+            a.bands_per_group, P->d.xact, tw, P->nact);
+        FAST_LAUNCHED("fast::k_line_apply_v");
+      }
+      const size_t sm = line_smem<R, N>();
+      if ((rc = prep(k_line_apply_v<R, N, false>, sm)) <= 0) return rc;
+      k_line_apply_v<R, N, false><<<dim3(N, ngroups), T, sm, st>>>(
           reinterpret_cast<C*>(a.out), reinterpret_cast<const R*>(a.aux), a.nbands,
           a.bands_per_group, P->d.xact, tw, P->nact);
       FAST_LAUNCHED("fast::k_line_apply_v");

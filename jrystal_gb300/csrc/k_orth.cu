@@ -163,16 +163,6 @@ __global__ void __launch_bounds__(256) k_gram_partial(const void* __restrict__ X
     }
 }
 
-// cp.async (sm_80+) copies of 4, 8 or 16 bytes into shared memory
-template <int BYTES>
-__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(sa), "l"(gmem), "n"(BYTES) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
 // num_band <= 32: warp-tiled partial Gram.  A block walks its G range in
 // chunks of 64 G vectors staged in shared memory as [g][band] (cp.async,
 // double-buffered); each of the 8 warps takes 8 G vectors of a chunk and
@@ -491,7 +481,7 @@ __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict
 // [B x B] FP64; output band-major complex, (S,K,G,B) complex, or (S,K,G,B)
 // split real/imag times fac.  Thread per g, J-wide column tile; the M tile is
 // staged in shared memory in precision R.
-enum RotOut { ROT_BANDMAJOR = 0, ROT_GMAJOR_C = 1, ROT_GMAJOR_SPLIT = 2 };
+enum RotOut { ROT_BANDMAJOR = 0, ROT_GMAJOR_C = 1, ROT_GMAJOR_SPLIT = 2, ROT_ADAM = 3 };
 
 template <typename R, int OUT, int J, int LX0, int LX1>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_rotate(const void* __restrict__ X0a, const void* __restrict__ X0b,
@@ -596,7 +586,7 @@ template <typename R, int LX0, int OUT, int NBP>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
 k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const double2* __restrict__ M0,
             const void* __restrict__ X1, const double2* __restrict__ M1, void* out0, void* out1,
-            int ng, int nb, R fac) {
+            int ng, int nb, R fac, AdamArgs adam) {
   using C = C_t<R>;
   constexpr int KC = kRbKC, GT = kRbGT, TG = 4, TJ = NBP / 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -614,6 +604,23 @@ k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const do
     double2 v = make_double2(0.0, 0.0);
     if (k < K && j < nb) v = (k < nb ? M0 : M1)[moff + (size_t)(k < nb ? k : k - nb) * nb + j];
     ms[e] = cmk<C>(v.x, v.y);
+  }
+  if constexpr (OUT == ROT_ADAM) {
+    // pull the block's parameter / moment / scale rows towards L2 while the
+    // contraction runs (every line address lies inside the buffers: rows
+    // start at or after a 128-byte boundary that is not before the buffer)
+    const size_t base = (sk * ng + g0) * nb;
+    const size_t len = (size_t)min(GT, ng - g0) * nb;
+    const void* rows[8] = {adam.p[0], adam.p[1], adam.m[0], adam.m[1],
+                           adam.v[0], adam.v[1], adam.scale[0], adam.scale[1]};
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (!rows[q]) continue;
+      const size_t esz = q < 6 ? sizeof(R) : sizeof(float);
+      const uintptr_t lo = (uintptr_t)rows[q] + base * esz, hi = lo + len * esz;
+      for (uintptr_t l = (lo & ~(uintptr_t)127) + (uintptr_t)t * 128; l < hi; l += 256 * 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(l));
+    }
   }
   const int gs = g0 + t;            // staging column of this thread
   const bool gv = gs < ng;
@@ -714,126 +721,50 @@ k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const do
           tile[gl * (NBP + 1) + wj * TJ + b] = fac * (part ? acc[a][b].y : acc[a][b].x);
       }
       __syncthreads();
-      R* o = reinterpret_cast<R*>(part ? out1 : out0) + base;
-      for (int e = t; e < len; e += 256) {
-        const int r = e / nb;
-        o[e] = tile[r * (NBP + 1) + (e - r * nb)];
-      }
-    }
-  }
-}
-
-// Adam fused into the adjoint rotation: the gradient element
-//   g = fac * sum_t X_t M_t   (split real/imag, (S,K,G,B) layout)
-// is consumed in registers by the optax Adam update of the parameter, its
-// moments and (optionally) the learned scale; grad is written only when
-// requested.
-
-template <typename R, int J>
-__global__ void __launch_bounds__(256) k_rotate_adam(const C_t<R>* __restrict__ X0,
-                                                     const double2* __restrict__ M0,
-                                                     const C_t<R>* __restrict__ X1,
-                                                     const double2* __restrict__ M1, AdamArgs a,
-                                                     int ng, int nb, R fac) {
-  // One block: 256 G vectors x all nb (<= J) bands of one (s, k).  The
-  // gradient tile goes through shared memory so that the parameter and
-  // moment rows of the block (a contiguous run of 256 * nb elements of the
-  // G-major layout) are read and written coalesced.
-  using C = C_t<R>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* ms = reinterpret_cast<C*>(smem_raw);                     // [2][nb][J]
-  R* gs = reinterpret_cast<R*>(ms + 2 * (size_t)nb * J);      // [256][nb + 1]
-  const int ld = nb + 1;
-  const size_t sk = blockIdx.z;
-  const size_t moff = sk * nb * nb;
-  for (int e = threadIdx.x; e < 2 * nb * J; e += blockDim.x) {
-    const int t = e / (nb * J), rem = e % (nb * J);
-    const int i = rem / J, jj = rem % J;
-    const double2* M = t ? M1 : M0;
-    double2 v = (jj < nb) ? M[moff + (size_t)i * nb + jj] : make_double2(0.0, 0.0);
-    ms[e] = cmk<C>(v.x, v.y);
-  }
-  const int g0 = blockIdx.x * blockDim.x;
-  const int g = g0 + threadIdx.x;
-  const size_t base = (sk * ng + g0) * nb;
-  const int len = min(256, ng - g0) * nb;
-  {
-    // pull this block's parameter / moment / scale rows towards L2 while the
-    // contraction runs; every prefetched line starts inside the row range
-    // (or at a 128-byte boundary at or after the buffer start)
-    const void* rows[8] = {a.p[0], a.p[1], a.m[0], a.m[1], a.v[0], a.v[1], a.scale[0], a.scale[1]};
-    const size_t esz[8] = {sizeof(R), sizeof(R), sizeof(R), sizeof(R), sizeof(R), sizeof(R), 4, 4};
+      if constexpr (OUT == ROT_ADAM) {
+        // optax Adam on the block's contiguous run of parameters, 4 elements
+        // per thread in flight
+        const R lr = (R)adam.lr, b1 = (R)adam.b1, b2 = (R)adam.b2, c1 = (R)adam.c1,
+                c2 = (R)adam.c2, eps = (R)adam.eps;
+        R* pp = reinterpret_cast<R*>(adam.p[part]) + base;
+        R* mp = reinterpret_cast<R*>(adam.m[part]) + base;
+        R* vp = reinterpret_cast<R*>(adam.v[part]) + base;
+        R* gp = adam.grad[part] ? reinterpret_cast<R*>(adam.grad[part]) + base : nullptr;
+        const float* sp = adam.scale[part] ? adam.scale[part] + base : nullptr;
+        constexpr int U = 4;
+        for (int e0 = t; e0 < len; e0 += U * 256) {
+          R mi[U], vi[U], pi[U];
+          float si[U];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (!rows[q]) continue;
-      const uintptr_t lo = (uintptr_t)rows[q] + base * esz[q];
-      const uintptr_t hi = lo + (size_t)len * esz[q];
-      for (uintptr_t l = (lo & ~(uintptr_t)127) + (uintptr_t)threadIdx.x * 128; l < hi; l += 256 * 128)
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(l));
-    }
-  }
-  __syncthreads();
-  C acc[J];
+          for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * 256;
+            if (e < len) {
+              mi[u] = mp[e];
+              vi[u] = vp[e];
+              pi[u] = pp[e];
+              si[u] = sp ? sp[e] : 1.0f;
+            }
+          }
 #pragma unroll
-  for (int jj = 0; jj < J; ++jj) acc[jj] = czero<C>();
-  if (g < ng) {
-#pragma unroll
-    for (int t = 0; t < 2; ++t) {
-      const C* X = (t ? X1 : X0) + sk * nb * ng;
-      const C* mt = ms + (size_t)t * nb * J;
-#pragma unroll 4
-      for (int i = 0; i < nb; ++i) {
-        const C x = X[(size_t)i * ng + g];
-#pragma unroll
-        for (int jj = 0; jj < J; ++jj) {
-          const C m = mt[i * J + jj];
-          acc[jj].x = fma(x.x, m.x, fma(-x.y, m.y, acc[jj].x));
-          acc[jj].y = fma(x.x, m.y, fma(x.y, m.x, acc[jj].y));
+          for (int u = 0; u < U; ++u) {
+            const int e = e0 + u * 256;
+            if (e < len) {
+              const int r = e / nb;
+              const R gr = tile[r * (NBP + 1) + (e - r * nb)];
+              if (gp) gp[e] = gr;
+              R d = adam_one<R>(gr, mi[u], vi[u], lr, b1, b2, c1, c2, eps);
+              if (sp) d *= (R)si[u];
+              mp[e] = mi[u];
+              vp[e] = vi[u];
+              pp[e] = pi[u] + d;
+            }
+          }
         }
-      }
-    }
-  }
-  const R lr = (R)a.lr, b1 = (R)a.b1, b2 = (R)a.b2, c1 = (R)a.c1, c2 = (R)a.c2, eps = (R)a.eps;
-#pragma unroll
-  for (int part = 0; part < 2; ++part) {
-    if (part) __syncthreads();
-#pragma unroll
-    for (int jj = 0; jj < J; ++jj)
-      if (jj < nb) gs[threadIdx.x * ld + jj] = fac * (part ? acc[jj].y : acc[jj].x);
-    __syncthreads();
-    R* pp = reinterpret_cast<R*>(a.p[part]) + base;
-    R* mp = reinterpret_cast<R*>(a.m[part]) + base;
-    R* vp = reinterpret_cast<R*>(a.v[part]) + base;
-    R* gp = a.grad[part] ? reinterpret_cast<R*>(a.grad[part]) + base : nullptr;
-    const float* sp = a.scale[part] ? a.scale[part] + base : nullptr;
-    // 8 elements per thread in flight: the loads of a chunk are issued
-    // before any of its updates so that the epilogue is not latency bound
-    constexpr int U = 8;
-    for (int e0 = threadIdx.x; e0 < len; e0 += U * 256) {
-      R mi[U], vi[U], pi[U];
-      float si[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int e = e0 + u * 256;
-        if (e < len) {
-          mi[u] = mp[e];
-          vi[u] = vp[e];
-          pi[u] = pp[e];
-          si[u] = sp ? sp[e] : 1.0f;
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int e = e0 + u * 256;
-        if (e < len) {
+      } else {
+        R* o = reinterpret_cast<R*>(part ? out1 : out0) + base;
+        for (int e = t; e < len; e += 256) {
           const int r = e / nb;
-          const R gr = gs[r * ld + (e - r * nb)];
-          if (gp) gp[e] = gr;
-          R d = adam_one<R>(gr, mi[u], vi[u], lr, b1, b2, c1, c2, eps);
-          if (sp) d *= (R)si[u];
-          mp[e] = mi[u];
-          vp[e] = vi[u];
-          pp[e] = pi[u] + d;
+          o[e] = tile[r * (NBP + 1) + (e - r * nb)];
         }
       }
     }
@@ -1015,7 +946,7 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate_rb)");
       }
       kern<<<dim3((ng + kRbGT - 1) / kRbGT, nsk), 256, sm, st>>>(X0a, X0b, M0, X1, M1, out0, out1, ng,
-                                                                 nb, (R)fac);
+                                                                 nb, (R)fac, AdamArgs{});
       JRG_LAUNCH_CHECK("k_rotate_rb");
       return JRG_OK;
     };
@@ -1044,24 +975,22 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
 template <typename R>
 int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const double2* M1,
                        const AdamArgs& a, int nsk, int ng, int nb, double fac, cudaStream_t st) {
-  using C = C_t<R>;
-  if (nb > 32) return fail(JRG_ERR_UNSUPPORTED, "k_rotate_adam: num_band > 32");
-  auto go = [&](auto kern, int J) -> int {
-    const size_t sm = sizeof(C) * 2 * (size_t)nb * J + sizeof(R) * 256 * (size_t)(nb + 1);
+  if (nb > 32) return fail(JRG_ERR_UNSUPPORTED, "k_rotate_rb: num_band > 32");
+  auto go = [&](auto kern, int nbp) -> int {
+    const size_t sm = rotate_rb_smem<R>(2 * nb, nbp);
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate_adam)");
+      if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate_rb adam)");
     }
-    dim3 grid((ng + 255) / 256, 1, nsk);
-    kern<<<grid, 256, sm, st>>>(reinterpret_cast<const C*>(X0), M0, reinterpret_cast<const C*>(X1), M1,
-                                a, ng, nb, (R)fac);
-    JRG_LAUNCH_CHECK("k_rotate_adam");
+    kern<<<dim3((ng + kRbGT - 1) / kRbGT, nsk), 256, sm, st>>>(X0, nullptr, M0, X1, M1, nullptr,
+                                                               nullptr, ng, nb, (R)fac, a);
+    JRG_LAUNCH_CHECK("k_rotate_rb(adam)");
     return JRG_OK;
   };
-  if (nb <= 8) return go(k_rotate_adam<R, 8>, 8);
-  if (nb <= 16) return go(k_rotate_adam<R, 16>, 16);
-  if (nb <= 24) return go(k_rotate_adam<R, 24>, 24);
-  return go(k_rotate_adam<R, 32>, 32);
+  if (nb <= 8) return go(k_rotate_rb<R, LAYOUT_BAND, ROT_ADAM, 8>, 8);
+  if (nb <= 16) return go(k_rotate_rb<R, LAYOUT_BAND, ROT_ADAM, 16>, 16);
+  if (nb <= 24) return go(k_rotate_rb<R, LAYOUT_BAND, ROT_ADAM, 24>, 24);
+  return go(k_rotate_rb<R, LAYOUT_BAND, ROT_ADAM, 32>, 32);
 }
 
 #define JRG_INST_ORTH(R)                                                                        \

@@ -2,6 +2,7 @@
 implementation generates.
 
   python -m jrystal_gb300.precond_train --out weights.npz [--eval-json eval.json]
+  python -m jrystal_gb300.precond_train --weights weights.npz --eval-json eval.json
 
 1. Trajectories: 64 strained cells (Si, C, Al; seed 2; grids from
    {24, 27, 32, 36, 48}; 2x2x2 k-grid; 8-16 bands, the lower half doubly
@@ -124,15 +125,21 @@ def evaluate(mlp, ncells=16, nsteps=8000, seed=99, grids=(24, 27, 32), smax=4.0,
 
 def main():
   ap = argparse.ArgumentParser()
-  ap.add_argument("--out", required=True)
+  ap.add_argument("--out", default=None)
+  ap.add_argument("--weights", default=None, help="evaluate these weights instead of training")
   ap.add_argument("--eval-json", default=None)
   ap.add_argument("--rounds", type=int, default=1)
   ap.add_argument("--eval-cells", type=int, default=16)
   ap.add_argument("--eval-steps", type=int, default=8000)
   ap.add_argument("--refine-steps", type=int, default=1500)
   args = ap.parse_args()
-  mlp = fit(rounds=args.rounds, refine_steps=args.refine_steps)
-  mlp.save(args.out)
+  if args.weights:
+    mlp = precond.MLP.load(args.weights)
+  else:
+    if not args.out:
+      ap.error("--out is required when training")
+    mlp = fit(rounds=args.rounds, refine_steps=args.refine_steps)
+    mlp.save(args.out)
   if args.eval_json:
     res = evaluate(mlp, ncells=args.eval_cells, nsteps=args.eval_steps)
     with open(args.eval_json, "w") as f:
