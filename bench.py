@@ -224,7 +224,7 @@ def phase_bytes(plan, fused=False):
   }
 
 
-def time_to_tolerance(nsteps=8000, cell_index=1):
+def time_to_tolerance(nsteps=20000, cell_index=1):
   """Learned vs plain optimiser on a held-out strained cell (the evaluation
   sequence of the preconditioner, seed 99): wall time until |E - E_ref| <
   1e-5 Ha/atom, E_ref the lower of the two final energies."""

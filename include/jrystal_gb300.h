@@ -106,6 +106,22 @@ int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
                     const double* occupation, double* energies, void* grad_re,
                     void* grad_im, void* workspace, cudaStream_t stream);
 
+/* Kohn-Sham band trace of a fixed effective potential, the objective of the
+ * band-structure driver (jrystal/calc/calc_band_structure_all_electrons.py:78-92,
+ * hamiltonian.hamiltonian_matrix_trace with kohn_sham=True,
+ * jrystal/_src/hamiltonian.py:105-168):
+ *   out[0] = sum_{s,k,b} w_skb <psi_skb| T + V_eff |psi_skb>,  out[1] = its kinetic part,
+ * its gradient with respect to {w_re, w_im} (optional, both or neither), and
+ * optionally the band Hamiltonian hmat[s,k][i][j] = w_skj <psi_i| T + V_eff |psi_j>
+ * (jrystal/_src/hamiltonian.py:171-240; complex FP64 [S*K][B][B]).
+ * v_eff: device [nx][ny][nz] real grid in the plan's precision (V_H + V_ext
+ * + v_xc, e.g. the three parts of jrg_potential with kohn_sham = 1 summed);
+ * weights: device double [S*K*B] (ones for the band structure); out: device
+ * double[2].  num_spin 1. */
+int jrg_band_trace_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
+                        const void* v_eff, const double* weights, double* out, void* hmat,
+                        void* grad_re, void* grad_im, void* workspace, cudaStream_t stream);
+
 /* One optimiser step (no counterpart in the reference as one call: it
  * fuses value_and_grad(total_energy) and optax.adam's update of
  * jrystal/calc/calc_ground_state_energy_all_electrons.py:175-190).

@@ -7,7 +7,7 @@ hand-written sm_103a kernels (``libjrystal_gb300.so``).
 """
 __version__ = "0.1.0"
 
-from . import (braket, calc, crystal, energy, entropy, ewald, grid, hamiltonian, kinetic,  # noqa
-               occupation, potential, pw, utils, workloads, xc)
+from . import (band, braket, calc, crystal, energy, entropy, ewald, grid, hamiltonian,  # noqa
+               kinetic, occupation, potential, pw, utils, workloads, xc)
 from .crystal import Crystal  # noqa: F401
 from ._ops import get_precision, set_precision  # noqa: F401

@@ -143,6 +143,7 @@ class GroundStateEnergyOutput:
   steps: int = 0
   converged: bool = False
   train_time: float = 0.0
+  density_grid: Optional[torch.Tensor] = None
 
 
 def _merge(config):
@@ -227,8 +228,116 @@ def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
   e, _, _ = plan.energy_and_grad(mini.params[0], mini.params[1], mini.occ, with_grad=False)
   e = e.cpu().numpy()
   terms = dict(kinetic=e[0], external=e[1], hartree=e[2], xc=e[3], total=e[4])
+  rho = plan.density(plan.coeff(mini.params[0], mini.params[1]), mini.occ)
   return GroundStateEnergyOutput(config=cfg, crystal=crystal,
                                  params_pw={"w_re": mini.params[0], "w_im": mini.params[1]},
                                  total_energy=float(e[4] + ew), total_energy_history=history,
                                  energy_terms=terms, ewald=ew, steps=i + 1, converged=converged,
-                                 train_time=train_time)
+                                 train_time=train_time, density_grid=rho)
+
+
+@dataclass
+class BandStructureOutput:
+  config: dict
+  crystal: Crystal
+  k_path: np.ndarray                 # (num_kpoints, 3) Cartesian, 1/bohr
+  eigenvalues: np.ndarray            # (spin, num_kpoints, bands), hartree
+  ground_state: GroundStateEnergyOutput
+  band_trace: float = 0.0
+  train_time: float = 0.0
+  effective_potential: Optional[torch.Tensor] = None   # V_H + V_ext + v_xc (nx, ny, nz)
+
+
+BAND_DEFAULTS = {
+  "k_path_special_points": None,
+  "num_kpoints": 60,
+  "band_structure_empty_bands": None,
+  "band_structure_epoch": 1000,
+  "k_path_fine_tuning": True,
+  "k_path_fine_tuning_epoch": 400,
+  "save_path": None,
+}
+
+
+def _band_minimise(plan, v_eff, params, m, v, steps, lr, b1, b2, eps, t0=0):
+  """Adam on the band trace of a fixed potential; no host synchronisation."""
+  grads = torch.empty_like(params)
+  for t in range(t0 + 1, t0 + steps + 1):
+    plan.band_trace_grad(params[0], params[1], v_eff, grad_re=grads[0], grad_im=grads[1])
+    adam_update(params, grads, m, v, t, lr, b1, b2, eps)
+  return t0 + steps
+
+
+def band_structure_all_electrons(config: dict) -> BandStructureOutput:
+  """Kohn-Sham band structure along a k path
+  (calc/calc_band_structure_all_electrons.py:37-209): the ground state of the
+  same config gives the density and V_eff = V_H + V_ext + v_xc; the band
+  trace sum_b <psi_b|T + V_eff|psi_b> is minimised with Adam, first at the
+  path's first k-point (``band_structure_epoch`` steps), then at all other
+  k-points at once starting from those parameters and moments
+  (``k_path_fine_tuning_epoch`` steps; jrystal walks the path one k-point
+  at a time, each starting from the previous one); the eigenvalues of the
+  band Hamiltonian H_ij = <psi_i|H|psi_j> at each k-point are returned as
+  (spin, k, band)."""
+  from .band import get_k_path
+  cfg = dict(BAND_DEFAULTS)
+  cfg.update(_merge(config))
+  gs = energy_all_electrons(cfg)
+  crystal = gs.crystal
+  precision = 64 if cfg["jax_enable_x64"] else 32
+  grid_sizes = tuple(int(g) for g in _grid.proper_grid_size(cfg["grid_sizes"]))
+  if cfg["freq_mask_method"] == "spherical":
+    mask = _grid.spherical_mask(crystal.cell_vectors, grid_sizes, cfg["cutoff_energy"])
+  else:
+    mask = _grid.cubic_mask(grid_sizes)
+  k_path = get_k_path(crystal.cell_vectors, cfg["k_path_special_points"], int(cfg["num_kpoints"]))
+  extra = cfg["band_structure_empty_bands"]
+  num_bands = math.ceil(crystal.num_electron / 2) + (int(extra) if extra is not None else 0)
+  oa = cfg["optimizer_args"]
+  lr, b1, b2, eps = (oa.get("learning_rate", 1e-2), oa.get("b1", 0.9), oa.get("b2", 0.999),
+                     oa.get("eps", 1e-8))
+
+  def make_plan(kpts):
+    return PlaneWavePlan(crystal.cell_vectors, crystal.positions, crystal.charges, grid_sizes,
+                         mask, kpts, num_bands, 1, precision, cfg["xc"])
+
+  t_start = time.perf_counter()
+  plan0 = make_plan(k_path[:1])
+  v_h, v_ext, v_xc = plan0.potential(gs.density_grid, kohn_sham=True)
+  v_eff = (v_h + v_ext + v_xc).contiguous()
+  gen = torch.Generator(device=plan0.device)
+  gen.manual_seed(int(cfg["seed"]))
+  ng = int(mask.sum())
+  p0 = torch.rand((2, 1, 1, ng, num_bands), generator=gen, device=plan0.device,
+                  dtype=plan0.rdtype)
+  m0, v0 = torch.zeros_like(p0), torch.zeros_like(p0)
+  t = _band_minimise(plan0, v_eff, p0, m0, v0, int(cfg["band_structure_epoch"]), lr, b1, b2, eps)
+  out0, _, _, h0 = plan0.band_trace_grad(p0[0], p0[1], v_eff, with_grad=False, hmat=True)
+  hs, trace = [h0], float(out0[0])
+  plan0.close()
+  nk = k_path.shape[0]
+  if nk > 1:
+    plan1 = make_plan(k_path[1:])
+    rep = lambda x: x.expand(2, 1, nk - 1, ng, num_bands).contiguous()
+    if cfg["k_path_fine_tuning"]:
+      p1, m1, v1 = rep(p0), rep(m0), rep(v0)
+      steps = int(cfg["k_path_fine_tuning_epoch"])
+    else:
+      p1 = rep(p0.new_empty(p0.shape).uniform_(generator=gen))
+      m1, v1, t, steps = torch.zeros_like(p1), torch.zeros_like(p1), 0, int(cfg["band_structure_epoch"])
+    _band_minimise(plan1, v_eff, p1, m1, v1, steps, lr, b1, b2, eps, t0=t)
+    out1, _, _, h1 = plan1.band_trace_grad(p1[0], p1[1], v_eff, with_grad=False, hmat=True)
+    hs.append(h1)
+    trace += float(out1[0])
+    plan1.close()
+  h = torch.cat(hs, dim=1)                               # (S, nk, B, B)
+  eig = torch.linalg.eigvalsh(h).cpu().numpy()           # (S, nk, B), ascending
+  torch.cuda.synchronize()
+  out = BandStructureOutput(config=cfg, crystal=crystal, k_path=k_path, eigenvalues=eig,
+                            ground_state=gs, band_trace=trace,
+                            train_time=time.perf_counter() - t_start, effective_potential=v_eff)
+  if cfg.get("save_path"):
+    np.save(cfg["save_path"], eig)
+  return out
+# the reference's name for the all-electron band driver (jrystal/calc/__init__.py:18)
+band_all_electrons = band_structure_all_electrons

@@ -34,6 +34,7 @@ template <typename R> int launch_hartree_g(const void*, const double*, void*, lo
 template <typename R> int launch_kinetic(const void*, const double*, const double*, double*, double*, int, int, int, int, cudaStream_t);
 int launch_precond_scale(const float*, const void*, const double*, const double*, const double*, int, int, int, long long, float, float, float*, cudaStream_t);
 int launch_sum_slots(const double*, const int*, double*, int, const int*, cudaStream_t);
+int launch_band_trace_sums(const double2*, int, int, const double*, int, double*, cudaStream_t);
 template <typename R> int launch_geometry_tables(double*, double*, void*, const double*, const double*, const double*, int, int, int, int, double, cudaStream_t);
 int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
 template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t);
@@ -499,6 +500,69 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
                           g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st);
 }
 
+// Band trace of a fixed effective potential (band-structure objective):
+// orthonormalise, kinetic, planes, x lines times v_eff, planes back to the
+// sphere gradient, C^H g_C (= the weighted band Hamiltonian), its trace, and
+// the orthonormalisation adjoint.
+template <typename R>
+static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im, const void* v_eff,
+                           const double* wts, double* out, void* hmat, void* g_re, void* g_im,
+                           void* ws, cudaStream_t st) {
+  const Workspace& w = P->ws;
+  const int nsk = P->ns * P->nk;
+  const int nbt = nsk * P->nb;
+  const double N = (double)P->ngrid;
+  int rc;
+  JRG_CUDA(cudaMemsetAsync(wsp(ws, w.flags), 0, 64, st));
+  if ((rc = orthonormalise<R>(P, w_re, w_im, ws, st))) return rc;
+  double* slots = (double*)wsp(ws, w.epart);
+  {
+    PHASE(PH_KINETIC);
+    if ((rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, wts, slots, (double*)wsp(ws, w.ekin), nbt,
+                                P->ng, P->nb, P->nk, st)))
+      return rc;
+  }
+  {
+    PHASE(PH_PLANE_INV);
+    if ((rc = launch_plane_inv_sphere<R>(P, wsp(ws, w.c), wsp(ws, w.t), nbt, st))) return rc;
+  }
+  {
+    PHASE(PH_LINE_APPLY_V);
+    if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), v_eff, nbt, P->nb, st))) return rc;
+  }
+  {
+    PHASE(PH_PLANE_FWD);
+    if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), wsp(ws, w.c), wsp(ws, w.gc), wts, 0, nbt,
+                                         1.0 / N, st)))
+      return rc;
+  }
+  {
+    PHASE(PH_ADJ_GRAM);
+    if ((rc = launch_gram<R>(kBand, wsp(ws, w.c), nullptr, kBand, wsp(ws, w.gc), nullptr,
+                             (double2*)wsp(ws, w.adj_part), (double2*)wsp(ws, w.adj), nsk, P->ng,
+                             P->nb, w.gram_splits, st)))
+      return rc;
+  }
+  if ((rc = launch_band_trace_sums((const double2*)wsp(ws, w.adj), nsk, P->nb, slots, nbt, out, st)))
+    return rc;
+  if (hmat)
+    JRG_CUDA(cudaMemcpyAsync(hmat, wsp(ws, w.adj), sizeof(double2) * (size_t)nsk * P->nb * P->nb,
+                             cudaMemcpyDeviceToDevice, st));
+  if (!g_re && !g_im) return JRG_OK;
+  if (!g_re || !g_im) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
+  double2* rh = (double2*)wsp(ws, w.kmat);
+  double2* negm2 = rh + (size_t)nsk * P->nb * P->nb;
+  {
+    PHASE(PH_ADJ_SMALL);
+    if ((rc = launch_adjoint_small((double2*)wsp(ws, w.adj), (double2*)wsp(ws, w.rinv), rh, negm2,
+                                   nsk, P->nb, st)))
+      return rc;
+  }
+  PHASE(PH_ADJ_ROTATE);
+  return launch_rotate<R>(kRotGSplit, kBand, wsp(ws, w.gc), nullptr, rh, wsp(ws, w.c), negm2, g_re,
+                          g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st);
+}
+
 template <typename R>
 static int energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
                        double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
@@ -568,6 +632,18 @@ int jrg_energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const
   if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad: spin-polarised LDA is not implemented");
   return P->prec == 64 ? energy_grad<double>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st)
                        : energy_grad<float>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st);
+}
+
+int jrg_band_trace_grad(const jrg_plan* P, const void* w_re, const void* w_im, const void* v_eff,
+                        const double* weights, double* out, void* hmat, void* grad_re, void* grad_im,
+                        void* ws, cudaStream_t st) {
+  if (!P || !w_re || !w_im || !v_eff || !weights || !out || !ws)
+    return fail(JRG_ERR_INVALID, "jrg_band_trace_grad: null argument");
+  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_band_trace_grad: num_spin must be 1");
+  int rc = P->prec == 64 ? band_trace_impl<double>(P, w_re, w_im, v_eff, weights, out, hmat, grad_re, grad_im, ws, st)
+                         : band_trace_impl<float>(P, w_re, w_im, v_eff, weights, out, hmat, grad_re, grad_im, ws, st);
+  profile_call_done(P);
+  return rc;
 }
 
 int jrg_energy_grad_adam(const jrg_plan* P, void* params, void* m, void* v, const double* occ,

@@ -219,6 +219,26 @@ __global__ void k_sum_slots(const double* __restrict__ slots, const int* __restr
   }
 }
 
+// band trace of a fixed Hamiltonian: out[0] = sum over (s,k,b) of Re A_bb
+// with A = C^H g_C (g_C = w H c), out[1] = the kinetic part (slots [0, nkin))
+__global__ void k_band_trace_sums(const double2* __restrict__ A, int nsk, int nb,
+                                  const double* __restrict__ slots, int nkin, double* __restrict__ out) {
+  __shared__ double red[32];
+  double a = 0.0;
+  for (int i = threadIdx.x; i < nsk * nb; i += blockDim.x) {
+    const int sk = i / nb, b = i - sk * nb;
+    a += A[((size_t)sk * nb + b) * nb + b].x;
+  }
+  a = block_sum(a, red);
+  double k = 0.0;
+  for (int i = threadIdx.x; i < nkin; i += blockDim.x) k += slots[i];
+  k = block_sum(k, red);
+  if (threadIdx.x == 0) {
+    out[0] = a;
+    out[1] = k;
+  }
+}
+
 // ------------------------------------------------------------------------
 // geometry tables (FP64): G vectors, 4 pi/|G|^2, external potential
 //   Vext(G) = -(4 pi N/vol) sum_a Z_a exp(-i G.R_a)/(|G|^2 + 1e-10), 0 at G=0
@@ -467,6 +487,13 @@ int launch_kinetic(const void* coef, const double* tk, const double* occ, double
   k_kinetic<R><<<nbands, 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(coef), tk, occ, slot, ekin, ng,
                                        nb, nk);
   JRG_LAUNCH_CHECK("k_kinetic");
+  return JRG_OK;
+}
+
+int launch_band_trace_sums(const double2* A, int nsk, int nb, const double* slots, int nkin,
+                          double* out, cudaStream_t st) {
+  k_band_trace_sums<<<1, 256, 0, st>>>(A, nsk, nb, slots, nkin, out);
+  JRG_LAUNCH_CHECK("k_band_trace_sums");
   return JRG_OK;
 }
 

@@ -574,11 +574,11 @@ constexpr int kRbKC = 8;     // rows per chunk
 constexpr int kRbGT = 256;   // G vectors per block
 
 template <typename R>
-size_t rotate_rb_smem(int K, int NBP) {
+size_t rotate_rb_smem(int K, int NBP, bool two_tiles = false) {
   const size_t KP = (size_t)(K + kRbKC - 1) / kRbKC * kRbKC;
   const size_t ms = KP * NBP * sizeof(C_t<R>);
   const size_t xs = 2 * (size_t)kRbKC * kRbGT * sizeof(C_t<R>);
-  const size_t tile = (size_t)kRbGT * (NBP + 1) * sizeof(R);
+  const size_t tile = (two_tiles ? 2 : 1) * (size_t)kRbGT * (NBP + 1) * sizeof(R);
   return ms + (xs > tile ? xs : tile);
 }
 
@@ -704,7 +704,7 @@ k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const do
         if (g < ng && j < nb) o[(size_t)j * ng + g] = acc[a][b];
       }
     }
-  } else {
+  } else if constexpr (OUT == ROT_GMAJOR_SPLIT) {
     // (S,K,G,B) split real/imag times fac, one part at a time through shared
     // memory: tile[g_local][band], row stride NBP + 1
     R* tile = reinterpret_cast<R*>(xs);
@@ -721,50 +721,59 @@ k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const do
           tile[gl * (NBP + 1) + wj * TJ + b] = fac * (part ? acc[a][b].y : acc[a][b].x);
       }
       __syncthreads();
-      if constexpr (OUT == ROT_ADAM) {
-        // optax Adam on the block's contiguous run of parameters, 4 elements
-        // per thread in flight
-        const R lr = (R)adam.lr, b1 = (R)adam.b1, b2 = (R)adam.b2, c1 = (R)adam.c1,
-                c2 = (R)adam.c2, eps = (R)adam.eps;
-        R* pp = reinterpret_cast<R*>(adam.p[part]) + base;
-        R* mp = reinterpret_cast<R*>(adam.m[part]) + base;
-        R* vp = reinterpret_cast<R*>(adam.v[part]) + base;
-        R* gp = adam.grad[part] ? reinterpret_cast<R*>(adam.grad[part]) + base : nullptr;
-        const float* sp = adam.scale[part] ? adam.scale[part] + base : nullptr;
-        constexpr int U = 4;
-        for (int e0 = t; e0 < len; e0 += U * 256) {
-          R mi[U], vi[U], pi[U];
-          float si[U];
+      R* o = reinterpret_cast<R*>(part ? out1 : out0) + base;
+      for (int e = t; e < len; e += 256) {
+        const int r = e / nb;
+        o[e] = tile[r * (NBP + 1) + (e - r * nb)];
+      }
+    }
+  } else {
+    // Adam on the block's contiguous run of parameters (both parts): the
+    // gradient tiles go to shared memory first so that the accumulators are
+    // dead and 8 elements per thread can be in flight
+    R* tile = reinterpret_cast<R*>(xs);   // [2][GT][NBP + 1]
+    const size_t base = (sk * ng + g0) * nb;
+    const int len = min(GT, ng - g0) * nb;
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            const int e = e0 + u * 256;
-            if (e < len) {
-              mi[u] = mp[e];
-              vi[u] = vp[e];
-              pi[u] = pp[e];
-              si[u] = sp ? sp[e] : 1.0f;
-            }
-          }
+    for (int a = 0; a < TG; ++a) {
+      const int gl = wg * 128 + (a / 2) * 64 + 2 * lane + (a % 2);
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            const int e = e0 + u * 256;
-            if (e < len) {
-              const int r = e / nb;
-              const R gr = tile[r * (NBP + 1) + (e - r * nb)];
-              if (gp) gp[e] = gr;
-              R d = adam_one<R>(gr, mi[u], vi[u], lr, b1, b2, c1, c2, eps);
-              if (sp) d *= (R)si[u];
-              mp[e] = mi[u];
-              vp[e] = vi[u];
-              pp[e] = pi[u] + d;
-            }
-          }
+      for (int b = 0; b < TJ; ++b) {
+        tile[gl * (NBP + 1) + wj * TJ + b] = fac * acc[a][b].x;
+        tile[(GT + gl) * (NBP + 1) + wj * TJ + b] = fac * acc[a][b].y;
+      }
+    }
+    __syncthreads();
+    const R lr = (R)adam.lr, b1 = (R)adam.b1, b2 = (R)adam.b2, c1 = (R)adam.c1, c2 = (R)adam.c2,
+            eps = (R)adam.eps;
+    constexpr int U = 8;
+    for (int e0 = t; e0 < 2 * len; e0 += U * 256) {
+      R mi[U], vi[U], pi[U];
+      float si[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + u * 256;
+        if (e < 2 * len) {
+          const int part = e >= len, el = e - part * len;
+          mi[u] = reinterpret_cast<const R*>(adam.m[part])[base + el];
+          vi[u] = reinterpret_cast<const R*>(adam.v[part])[base + el];
+          pi[u] = reinterpret_cast<const R*>(adam.p[part])[base + el];
+          si[u] = adam.scale[part] ? adam.scale[part][base + el] : 1.0f;
         }
-      } else {
-        R* o = reinterpret_cast<R*>(part ? out1 : out0) + base;
-        for (int e = t; e < len; e += 256) {
-          const int r = e / nb;
-          o[e] = tile[r * (NBP + 1) + (e - r * nb)];
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int e = e0 + u * 256;
+        if (e < 2 * len) {
+          const int part = e >= len, el = e - part * len;
+          const int r = el / nb;
+          const R gr = tile[(part * GT + r) * (NBP + 1) + (el - r * nb)];
+          if (adam.grad[part]) reinterpret_cast<R*>(adam.grad[part])[base + el] = gr;
+          R d = adam_one<R>(gr, mi[u], vi[u], lr, b1, b2, c1, c2, eps);
+          if (adam.scale[part]) d *= (R)si[u];
+          reinterpret_cast<R*>(adam.m[part])[base + el] = mi[u];
+          reinterpret_cast<R*>(adam.v[part])[base + el] = vi[u];
+          reinterpret_cast<R*>(adam.p[part])[base + el] = pi[u] + d;
         }
       }
     }
@@ -977,7 +986,7 @@ int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const 
                        const AdamArgs& a, int nsk, int ng, int nb, double fac, cudaStream_t st) {
   if (nb > 32) return fail(JRG_ERR_UNSUPPORTED, "k_rotate_rb: num_band > 32");
   auto go = [&](auto kern, int nbp) -> int {
-    const size_t sm = rotate_rb_smem<R>(2 * nb, nbp);
+    const size_t sm = rotate_rb_smem<R>(2 * nb, nbp, true);
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate_rb adam)");

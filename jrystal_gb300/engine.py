@@ -144,6 +144,41 @@ class PlaneWavePlan:
     _lib.check(st, "jrg_energy_grad")
     return self.energies, grad_re, grad_im
 
+  def band_trace_grad(self, w_re: torch.Tensor, w_im: torch.Tensor, v_eff, weights=None,
+                      grad_re: Optional[torch.Tensor] = None,
+                      grad_im: Optional[torch.Tensor] = None, with_grad: bool = True,
+                      hmat: bool = False):
+    """Band trace sum w <psi|T + V_eff|psi> for a fixed effective potential
+    (device float64[2]: trace, kinetic part), its gradient with respect to
+    {w_re, w_im}, and optionally the band Hamiltonian (S,K,B,B) complex128
+    with entries w_j <psi_i|H|psi_j>.  ``weights`` (S,K,B) default to ones."""
+    self._check_param(w_re, "w_re")
+    self._check_param(w_im, "w_im")
+    v = torch.as_tensor(v_eff, device=self.device).to(self.rdtype)
+    if v.dim() == 4 and v.shape[0] == 1:
+      v = v[0]
+    if tuple(v.shape) != self.grid:
+      raise ValueError(f"v_eff has shape {tuple(v.shape)}, expected {self.grid}")
+    v = v.contiguous()
+    wts = self._occ(torch.ones((self.num_spin, self.num_kpt, self.num_band), dtype=torch.float64)
+                    if weights is None else weights)
+    if with_grad:
+      if grad_re is None:
+        grad_re = torch.empty_like(w_re)
+      if grad_im is None:
+        grad_im = torch.empty_like(w_im)
+    out = torch.empty(2, dtype=torch.float64, device=self.device)
+    hm = None
+    if hmat:
+      hm = torch.empty((self.num_spin, self.num_kpt, self.num_band, self.num_band),
+                       dtype=torch.complex128, device=self.device)
+    st = self.lib.jrg_band_trace_grad(self._h, _ptr(w_re), _ptr(w_im), _ptr(v), _ptr(wts),
+                                      _ptr(out), _ptr(hm), _ptr(grad_re) if with_grad else None,
+                                      _ptr(grad_im) if with_grad else None, _ptr(self.workspace),
+                                      _stream())
+    _lib.check(st, "jrg_band_trace_grad")
+    return out, grad_re if with_grad else None, grad_im if with_grad else None, hm
+
   def energy_grad_adam(self, params: torch.Tensor, m: torch.Tensor, v: torch.Tensor, occupation,
                        step: int, lr: float, b1: float = 0.9, b2: float = 0.99, eps: float = 1e-8,
                        scale: Optional[torch.Tensor] = None, mlp=None, t_frac: float = 0.0,

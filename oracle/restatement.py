@@ -525,6 +525,71 @@ def hamiltonian_matrix_trace(coeff_dense, position, charge, density_grid,
   return np.sum(tr, axis=(1, 2)) if keep_kpts_axis else np.sum(tr)
 
 
+def hamiltonian_matrix(coeff_dense, position, charge, density_grid,
+                       g_vector_grid, kpts, vol, xc="lda_x", kohn_sham=True):
+  """jrystal/_src/hamiltonian.py:171-240: H_ij = <psi_i|T + V_eff|psi_j> per
+  (spin, kpt).  jrystal forms it as the complex Hessian of half the trace of
+  a single combined band; for an operator independent of the coefficients
+  that is the matrix of T + V_eff in the band basis, formed here directly."""
+  v_eff = effective(density_grid, position, charge, g_vector_grid, vol,
+                    False, xc, kohn_sham)
+  wave = wave_grid(coeff_dense, vol)
+  f_eff = expectation(wave, v_eff, vol, diagonal=False, mode="real")
+  t_kin = kinetic_operator(g_vector_grid, kpts)
+  f_kin = expectation(coeff_dense, t_kin, vol, diagonal=False, mode="kinetic")
+  return f_eff + f_kin
+
+
+def band_trace_terms(w_re, w_im, v_eff, sysm, weights=None, with_grad=True):
+  """Band-structure objective for a fixed effective potential
+  (calc/calc_band_structure_all_electrons.py:78-92 with
+  hamiltonian_matrix_trace, kohn_sham=True): trace = sum w <psi|T+V|psi>,
+  its kinetic part, the weighted band Hamiltonian A_ij = w_j <psi_i|H|psi_j>
+  and d trace / d {w_re, w_im} through the same orthonormalisation adjoint as
+  energy_terms (g_C = w (T c + sqrt(vol)/N FFT(V psi))|_sphere)."""
+  vol = sysm.vol
+  gvec = sysm.g_vector_grid
+  mask = sysm.mask
+  n = np.prod(sysm.grid)
+  c, r = cholesky_qr(w_re, w_im)                  # (s,k,g,b)
+  if weights is None:
+    weights = np.ones(c.shape[:2] + c.shape[-1:])
+  dense = expand_coefficient(c, mask)
+  wave = _ifftn(dense) * n / np.sqrt(vol)
+  v = np.asarray(v_eff).reshape(sysm.grid)
+  hpsi = _fftn(v[None, None, None] * wave)[..., mask] * (np.sqrt(vol) / n)
+  tk = kinetic_operator(gvec, sysm.kpts)[:, mask]  # (k,g)
+  hc = tk[None, :, None, :] * np.swapaxes(c, -1, -2) + hpsi   # (s,k,b,g) = H c_b
+  g_c = np.swapaxes(weights[..., None] * hc, -1, -2)          # (s,k,g,b)
+  a = np.einsum("...gi,...gj->...ij", c.conj(), g_c)
+  kin = np.sum(weights * np.einsum("kg,skgb->skb", tk, np.abs(c)**2))
+  out = dict(trace=float(np.sum(np.einsum("...ii->...i", a).real)), kinetic=float(kin), hmat=a)
+  if not with_grad:
+    return out
+  up = np.triu(a, 1)
+  kmat = up + np.swapaxes(up.conj(), -1, -2)
+  kmat = kmat + np.einsum("...ii->...i", a).real[..., None] * np.eye(a.shape[-1])
+  rinv_h = np.swapaxes(np.linalg.inv(r).conj(), -1, -2)
+  g_w = (g_c - c @ kmat) @ rinv_h
+  out["grad_re"], out["grad_im"] = 2 * g_w.real, 2 * g_w.imag
+  return out
+
+
+def plane_wave_hamiltonian(v_eff, sysm, k_index):
+  """Full Hamiltonian of one k-point in the sphere basis:
+  H[G, G'] = |G+k|^2/2 delta_GG' + V(G - G'), V(G) = (1/N) sum_r V(r) e^{-iG.r},
+  in the normalisation of braket.expectation (real mode) and the kinetic
+  mode; its lowest eigenvalues are what the band-structure minimisation
+  converges to."""
+  v = np.asarray(v_eff).reshape(sysm.grid)
+  vg = np.fft.fftn(v) / np.prod(sysm.grid)
+  idx = np.argwhere(sysm.mask)                    # (g, 3) FFT indices, row-major mask order
+  d = (idx[:, None, :] - idx[None, :, :]) % np.asarray(sysm.grid)
+  h = vg[d[..., 0], d[..., 1], d[..., 2]]
+  tk = kinetic_operator(sysm.g_vector_grid, sysm.kpts[k_index:k_index + 1])[0][sysm.mask]
+  return h + np.diag(tk)
+
+
 def ewald_coulomb_repulsion(positions, charges, g_vector_grid, vol, ewald_eta,
                             ewald_grid):
   """jrystal/_src/ewald.py:21-86, evaluated pair by pair (same sums)."""
