@@ -229,10 +229,12 @@ int jrg_kinetic_table(const jrg_plan* plan, double* out, cudaStream_t stream);
  * previous setting.  Process-wide; no reference counterpart. */
 int jrg_fast_paths(int enable);
 
-/* Selects tensor-core (mma.sync TF32, three-product hi/lo split) Gram and
- * rotation contractions for the FP32 path with num_band <= 32 (enable = 1)
- * or the CUDA-core kernels (0, the default: faster at these band counts);
- * < 0 only queries.  Returns the previous setting.  No reference counterpart. */
+/* Selects the contraction kernels of the FP32 path (num_band <= 32):
+ * 0 = CUDA cores (the default: fastest at these band counts), 1 = mma.sync
+ * TF32 Gram and rotation with a three-product hi/lo split, 2 = tcgen05
+ * (5th-generation tensor cores, tensor-memory accumulators) TF32 x 3 Gram
+ * with CUDA-core rotation; enable < 0 only queries.  Returns the previous
+ * setting.  Process-wide; no reference counterpart. */
 int jrg_tensor_core_paths(int enable);
 
 /* Per-phase CUDA-event timing of jrg_energy_grad (no reference counterpart;

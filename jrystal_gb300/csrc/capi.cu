@@ -19,7 +19,7 @@ template <typename R> int launch_plane_fwd_sphere(const jrg_plan*, const void*, 
 template <typename R> int launch_fft3d_dense(const FftAxis*, const C_t<R>*, int, int, bool, const void*, C_t<R>*, C_t<R>*, double, cudaStream_t);
 template <typename R> int launch_pack_params(const void*, const void*, void*, int, int, int, bool, cudaStream_t);
 template <typename R> int launch_unpack(const void*, void*, void*, void*, int, int, int, double, cudaStream_t);
-template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t);
+template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t, int* = nullptr);
 int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t);
 int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t);
 template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t);
@@ -377,7 +377,8 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
   {
     PHASE(PH_GRAM);
     if ((rc = launch_gram<R>(kSplit, w_re, w_im, kSplit, w_re, w_im, (double2*)wsp(ws, w.gram_part),
-                             (double2*)wsp(ws, w.gram), nsk, P->ng, P->nb, w.gram_splits, st)))
+                             (double2*)wsp(ws, w.gram), nsk, P->ng, P->nb, w.gram_splits, st,
+                             (int*)wsp(ws, w.flags))))
       return rc;
   }
   {
@@ -481,7 +482,7 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
     PHASE(PH_ADJ_GRAM);
     if ((rc = launch_gram<R>(kBand, wsp(ws, w.c), nullptr, kBand, wsp(ws, w.gc), nullptr,
                              (double2*)wsp(ws, w.adj_part), (double2*)wsp(ws, w.adj), nsk, P->ng,
-                             P->nb, w.gram_splits, st)))
+                             P->nb, w.gram_splits, st, (int*)wsp(ws, w.flags))))
       return rc;
   }
   double2* rh = (double2*)wsp(ws, w.kmat);
@@ -540,7 +541,7 @@ static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im
     PHASE(PH_ADJ_GRAM);
     if ((rc = launch_gram<R>(kBand, wsp(ws, w.c), nullptr, kBand, wsp(ws, w.gc), nullptr,
                              (double2*)wsp(ws, w.adj_part), (double2*)wsp(ws, w.adj), nsk, P->ng,
-                             P->nb, w.gram_splits, st)))
+                             P->nb, w.gram_splits, st, (int*)wsp(ws, w.flags))))
       return rc;
   }
   if ((rc = launch_band_trace_sums((const double2*)wsp(ws, w.adj), nsk, P->nb, slots, nbt, out, st)))

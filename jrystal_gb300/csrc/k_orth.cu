@@ -819,15 +819,30 @@ int launch_gram_tc(int lx, const void* X0, const void* X1, int ly, const void* Y
 int launch_rotate_tc(int out_kind, int lx0, const void* X0a, const void* X0b, const double2* M0,
                      const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng,
                      int nb, double fac, uint32_t* bscratch, cudaStream_t st);
-static bool g_tc_enabled = false;   // measured slower than the CUDA-core kernels at B <= 32
+// tensor-core contractions of the FP32 path: 0 CUDA cores (default), 1
+// mma.sync TF32 x 3 Gram and rotation, 2 tcgen05 TF32 x 3 Gram
+static int g_tc_mode = 0;
+int launch_gram_tc5(int lay, const void* X0, const void* X1, const void* Y0, const void* Y1,
+                    double2* part, int nsk, int ng, int nb, int nsplit, int* err, cudaStream_t st);
 static bool g_gram_rb = true;       // register-blocked Gram for B <= 32 (else 32x32 tiles)
 static bool g_rotate_rb = true;     // register-blocked rotation for B <= 32
 void set_gram_rb(bool on) { g_gram_rb = on; g_rotate_rb = on; }
 
 template <typename R>
 int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, const void* Y1,
-                double2* part, double2* out, int nsk, int ng, int nb, int nsplit, cudaStream_t st) {
-  if (sizeof(R) == 4 && g_tc_enabled) {   // FP32 path: tensor cores (TF32 x3)
+                double2* part, double2* out, int nsk, int ng, int nb, int nsplit, cudaStream_t st,
+                int* flags) {
+  if (sizeof(R) == 4 && g_tc_mode == 2 && lx == ly) {   // tcgen05 Gram (TF32 x 3)
+    const int ns = launch_gram_tc5(lx, X0, X1, Y0, Y1, part, nsk, ng, nb, nsplit, flags, st);
+    if (ns < 0) return -ns;
+    if (ns > 0) {
+      const size_t n = (size_t)nsk * nb * nb;
+      k_gram_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, out, ns, nb, nsk);
+      JRG_LAUNCH_CHECK("k_gram_reduce");
+      return JRG_OK;
+    }
+  }
+  if (sizeof(R) == 4 && g_tc_mode == 1) {   // FP32 path: mma.sync tensor cores (TF32 x3)
     const int t = launch_gram_tc(lx, X0, X1, ly, Y0, Y1, reinterpret_cast<double*>(part), out, nsk,
                                  ng, nb, nsplit, st);
     if (t < 0) return -t;
@@ -939,7 +954,7 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
                   const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng, int nb,
                   double fac, void* scratch, cudaStream_t st) {
   if (X1 && lx0 != LAYOUT_BAND) return fail(JRG_ERR_INVALID, "launch_rotate: two-term form needs band-major inputs");
-  if (sizeof(R) == 4 && g_tc_enabled) {
+  if (sizeof(R) == 4 && g_tc_mode == 1) {
     const int t = launch_rotate_tc(out_kind, lx0, X0a, X0b, M0, X1, M1, out0, out1, nsk, ng, nb, fac,
                                    reinterpret_cast<uint32_t*>(scratch), st);
     if (t < 0) return -t;
@@ -1010,7 +1025,7 @@ int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const 
   template int launch_unpack<R>(const void*, void*, void*, void*, int, int, int, double,          \
                                 cudaStream_t);                                                  \
   template int launch_gram<R>(int, const void*, const void*, int, const void*, const void*,       \
-                              double2*, double2*, int, int, int, int, cudaStream_t);            \
+                              double2*, double2*, int, int, int, int, cudaStream_t, int*);      \
   template int launch_rotate<R>(int, int, const void*, const void*, const double2*, const void*,  \
                                 const double2*, void*, void*, int, int, int, double, void*,     \
                                 cudaStream_t);
@@ -1020,7 +1035,7 @@ JRG_INST_ORTH(double)
 }  // namespace jrg
 
 extern "C" int jrg_tensor_core_paths(int enable) {
-  const int prev = jrg::g_tc_enabled ? 1 : 0;
-  if (enable >= 0) jrg::g_tc_enabled = enable != 0;
+  const int prev = jrg::g_tc_mode;
+  if (enable >= 0 && enable <= 2) jrg::g_tc_mode = enable;
   return prev;
 }

@@ -179,11 +179,18 @@ def test_fast_and_generic_slab_kernels_agree(prec):
   assert np.abs(out[1][2] - out[0][2]).max() <= tol["g_rel"] * scale
 
 
-def test_tensor_core_and_cuda_core_contractions_agree():
+@pytest.mark.parametrize("nb,nocc,grid,kgrid", [(24, 12, (36, 36, 36), (2, 1, 1)),
+                                                (5, 3, (24, 24, 24), (1, 1, 2)),
+                                                (12, 8, (16, 16, 16), (2, 1, 1)),
+                                                (30, 16, (24, 24, 24), (1, 1, 1))])
+def test_tensor_core_and_cuda_core_contractions_agree(nb, nocc, grid, kgrid):
+  """mode 1: mma.sync TF32 x 3 Gram and rotation; mode 2: tcgen05 TF32 x 3
+  Gram (tensor memory accumulator); mode 0: CUDA cores.  All against the
+  oracle, and the flag word (energies[6]) stays clear."""
   torch = _torch()
   from jrystal_gb300 import _lib
   lib = _lib.load()
-  sysm = make_system(kind="si8", grid=(36, 36, 36), kgrid=(2, 1, 1), nb=24, nocc=12)
+  sysm = make_system(kind="si8", grid=grid, kgrid=kgrid, nb=nb, nocc=nocc)
   wr, wi = random_params(sysm, seed=31)
   terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
   plan = _plan(sysm, 32)
@@ -192,7 +199,7 @@ def test_tensor_core_and_cuda_core_contractions_agree():
   out = {}
   prev = lib.jrg_tensor_core_paths(-1)
   try:
-    for tc in (1, 0):
+    for tc in (2, 1, 0):
       lib.jrg_tensor_core_paths(tc)
       e, g1, g2 = plan.energy_and_grad(twr, twi, sysm.occupation)
       out[tc] = (e.cpu().numpy().copy(), g1.cpu().numpy(), g2.cpu().numpy())
@@ -200,8 +207,9 @@ def test_tensor_core_and_cuda_core_contractions_agree():
     lib.jrg_tensor_core_paths(prev)
   tol = TOL[32]
   scale = max(np.abs(gr).max(), np.abs(gi).max())
-  for tc in (1, 0):
+  for tc in (2, 1, 0):
     e, g1, g2 = out[tc]
+    assert e[6] == 0.0, (tc, e[6])
     for i, name in enumerate(["kinetic", "external", "hartree", "xc", "total"]):
       assert abs(e[i] - terms[name]) <= tol["e_rel"] * max(1.0, abs(terms[name])), (tc, name)
     assert max(np.abs(g1 - gr).max(), np.abs(g2 - gi).max()) <= tol["g_rel"] * scale, tc
