@@ -106,6 +106,16 @@ int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
                     const double* occupation, double* energies, void* grad_re,
                     void* grad_im, void* workspace, cudaStream_t stream);
 
+/* jrg_energy_grad plus the band energies band_energies[s,k,b] =
+ * <psi_skb| T + V_eff |psi_skb> = d total / d occupation[s,k,b] (device
+ * double[S*K*B]), the occupation gradient the reference driver takes with
+ * value_and_grad over its occupation parameters
+ * (jrystal/calc/calc_ground_state_energy_all_electrons.py:119-147,175-181).
+ * num_spin 1. */
+int jrg_energy_grad_bands(const jrg_plan* plan, const void* w_re, const void* w_im,
+                          const double* occupation, double* energies, double* band_energies,
+                          void* grad_re, void* grad_im, void* workspace, cudaStream_t stream);
+
 /* Kohn-Sham band trace of a fixed effective potential, the objective of the
  * band-structure driver (jrystal/calc/calc_band_structure_all_electrons.py:78-92,
  * hamiltonian.hamiltonian_matrix_trace with kohn_sham=True,

@@ -144,6 +144,7 @@ class GroundStateEnergyOutput:
   converged: bool = False
   train_time: float = 0.0
   density_grid: Optional[torch.Tensor] = None
+  occupation: Optional[torch.Tensor] = None
 
 
 def _merge(config):
@@ -167,8 +168,10 @@ def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
   cfg = _merge(config)
   if cfg["optimizer"] != "adam":
     raise NotImplementedError("only the adam optimiser is implemented on the device")
+  if cfg["occupation"] in ("simplex-projector", "idempotent"):
+    return _energy_learnable_occupation(cfg)
   if cfg["occupation"] not in ("uniform", "gamma"):
-    raise NotImplementedError("fixed occupations (uniform, gamma) only")
+    raise ValueError(f"Invalid method: {cfg['occupation']}")
   if not cfg["spin_restricted"]:
     raise NotImplementedError("spin-polarised LDA is not implemented")
   crystal = create_crystal(cfg)
@@ -234,6 +237,116 @@ def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
                                  total_energy=float(e[4] + ew), total_energy_history=history,
                                  energy_terms=terms, ewald=ew, steps=i + 1, converged=converged,
                                  train_time=train_time, density_grid=rho)
+
+
+def temperature_schedule(cfg):
+  """Smearing temperature of step i (calc/…all_electrons.py:193-203):
+  optax.exponential_decay(100, epoch // 2, smearing / 100, end_value=smearing),
+  i.e. 100 (smearing/100)^(i / (epoch//2)) clipped below at smearing; 0
+  without smearing."""
+  sm = float(cfg.get("smearing", 0.0))
+  if sm <= 0.0:
+    return lambda i: 0.0
+  steps = max(1, int(cfg["epoch"]) // 2)
+  rate = sm / 100.0
+  return lambda i: max(sm, 100.0 * rate ** (i / steps))
+
+
+def _energy_learnable_occupation(cfg) -> GroundStateEnergyOutput:
+  """Free-energy minimisation F = E - T S over the plane-wave parameters and
+  learnable occupations (simplex projector or idempotent), the reference
+  driver's path for metals (calc/calc_ground_state_energy_all_electrons.py:
+  103-147 and 150-220): the device returns E, dE/dW and the band energies
+  dE/df (jrg_energy_grad_bands); dF/d(occupation parameters) follows by
+  torch autograd through the occupation map and the Fermi-Dirac entropy;
+  both parameter sets take Adam steps with the same hyper-parameters."""
+  from . import entropy as _entropy
+  from . import occupation as _occupation
+  if not cfg["spin_restricted"]:
+    raise NotImplementedError("spin-polarised LDA is not implemented")
+  crystal = create_crystal(cfg)
+  precision = 64 if cfg["jax_enable_x64"] else 32
+  grid_sizes = tuple(int(g) for g in _grid.proper_grid_size(cfg["grid_sizes"]))
+  k_grid = tuple(int(k) for k in np.broadcast_to(cfg["k_grid_sizes"], 3))
+  kpts = _grid.k_vectors(crystal.cell_vectors, k_grid)
+  if cfg["freq_mask_method"] == "spherical":
+    mask = _grid.spherical_mask(crystal.cell_vectors, grid_sizes, cfg["cutoff_energy"])
+  else:
+    mask = _grid.cubic_mask(grid_sizes)
+  nelec = crystal.num_electron
+  num_bands = math.ceil(nelec / 2) + cfg["empty_bands"]
+  K = kpts.shape[0]
+  plan = PlaneWavePlan(crystal.cell_vectors, crystal.positions, crystal.charges, grid_sizes, mask,
+                       kpts, num_bands, 1, precision, cfg["xc"])
+  ew = plan.ewald(cfg["ewald_args"]["ewald_eta"], cfg["ewald_args"]["ewald_cutoff"])
+  ng = int(mask.sum())
+  gen = torch.Generator(device=plan.device)
+  gen.manual_seed(int(cfg["seed"]))
+  if "init_params" in cfg:
+    w_re, w_im = cfg["init_params"]
+    params = torch.tensor(np.stack([w_re, w_im]), dtype=plan.rdtype, device=plan.device)
+  else:
+    params = torch.rand((2, 1, K, ng, num_bands), generator=gen, device=plan.device,
+                        dtype=plan.rdtype)
+  method = cfg["occupation"]
+  spin = int(crystal.spin)
+  if method == "idempotent":
+    occ_params = _occupation.idempotent_param_init(gen, num_bands, nelec, K, spin)
+    leaves = [occ_params["param_up"]["w_re"]]
+    if occ_params["param_down"] is not occ_params["param_up"]:
+      leaves.append(occ_params["param_down"]["w_re"])
+  else:
+    occ_params = _occupation.simplex_projector_init(num_bands, K, device=plan.device)
+    leaves = [occ_params["param_up"], occ_params["param_down"]]
+  for t in leaves:
+    t.requires_grad_(True)
+
+  def occ_of():
+    return _occupation.occupation(occ_params, K, nelec, spin, method, True)
+
+  oa = cfg["optimizer_args"]
+  lr, b1, b2, eps = (oa.get("learning_rate", 1e-2), oa.get("b1", 0.9), oa.get("b2", 0.999),
+                     oa.get("eps", 1e-8))
+  grads = torch.empty_like(params)
+  m, v = torch.zeros_like(params), torch.zeros_like(params)
+  om = [torch.zeros_like(t) for t in leaves]
+  ov = [torch.zeros_like(t) for t in leaves]
+  temp_of = temperature_schedule(cfg)
+  checker = ConvergenceChecker(cfg["convergence_window_size"], cfg["convergence_condition"])
+  history, converged, train_time = [], False, 0.0
+  ent_eps = float(cfg.get("eps", 1e-8))
+  i = 0
+  for i in range(cfg["epoch"]):
+    t0 = time.perf_counter()
+    temp = temp_of(i)
+    occ = occ_of()
+    e, _, _, band_e = plan.energy_grad_bands(params[0], params[1], occ.detach(), grads[0], grads[1])
+    ent = _entropy.fermi_dirac(occ, eps=ent_eps)
+    # dF/dtheta = sum_b (dE/df_b) df_b/dtheta - T dS/dtheta
+    surrogate = (occ * band_e).sum() - temp * ent
+    og = torch.autograd.grad(surrogate, leaves)
+    adam_update(params, grads, m, v, i + 1, lr, b1, b2, eps)
+    with torch.no_grad():
+      for t, g, mm, vv in zip(leaves, og, om, ov):
+        adam_update(t.data, g.contiguous(), mm, vv, i + 1, lr, b1, b2, eps)
+    etot = float(e[4].item())
+    train_time += time.perf_counter() - t0
+    history.append(etot)
+    if checker.check(etot):
+      converged = True
+      break
+  with torch.no_grad():
+    occ = occ_of().detach()
+  e, _, _ = plan.energy_and_grad(params[0], params[1], occ, with_grad=False)
+  e = e.cpu().numpy()
+  terms = dict(kinetic=e[0], external=e[1], hartree=e[2], xc=e[3], total=e[4],
+               entropy=float(_entropy.fermi_dirac(occ, eps=ent_eps)), temperature=temp_of(i))
+  rho = plan.density(plan.coeff(params[0], params[1]), occ)
+  return GroundStateEnergyOutput(config=cfg, crystal=crystal,
+                                 params_pw={"w_re": params[0], "w_im": params[1]},
+                                 total_energy=float(e[4] + ew), total_energy_history=history,
+                                 energy_terms=terms, ewald=ew, steps=i + 1, converged=converged,
+                                 train_time=train_time, density_grid=rho, occupation=occ)
 
 
 @dataclass

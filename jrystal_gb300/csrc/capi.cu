@@ -21,7 +21,8 @@ template <typename R> int launch_pack_params(const void*, const void*, void*, in
 template <typename R> int launch_unpack(const void*, void*, void*, void*, int, int, int, double, cudaStream_t);
 template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t, int* = nullptr);
 int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t);
-int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t);
+int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t,
+                         const double* = nullptr, double* = nullptr);
 template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t);
 constexpr int kSplit = 0, kBand = 1;           // tall-operand layouts (k_orth.cu)
 constexpr int kRotBand = 0, kRotGC = 1, kRotGSplit = 2;
@@ -137,6 +138,7 @@ int jrg_plan_destroy(jrg_plan* P) {
   if (P->slot_begin) cudaFree(P->slot_begin);
   if (P->d_cell) cudaFree(P->d_cell);
   if (P->d_atoms) cudaFree(P->d_atoms);
+  if (P->d_ones) cudaFree(P->d_ones);
   if (P->prof) {
     for (cudaEvent_t e : P->prof->ev) cudaEventDestroy(e);
     delete P->prof;
@@ -303,6 +305,10 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
   if (!rc) rc = up((void**)&P->d_atoms, atoms.data(), atoms.size() * sizeof(double));
   if (!rc) { d_pos = P->d_atoms; d_chg = P->d_atoms + 3 * d->num_atom; }
   if (!rc) {
+    std::vector<double> ones((size_t)P->ns * P->nk * P->nb, 1.0);
+    rc = up((void**)&P->d_ones, ones.data(), ones.size() * sizeof(double));
+  }
+  if (!rc) {
     cudaError_t e = cudaMalloc((void**)&P->d.gvec, 3 * P->ngrid * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void**)&P->d.ginv, P->ngrid * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&P->d.vext, P->ngrid * csize(P->prec));
@@ -418,7 +424,7 @@ static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* 
 template <typename R>
 static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
                             double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st,
-                            const AdamArgs* adam = nullptr) {
+                            const AdamArgs* adam = nullptr, double* band_e = nullptr) {
   using C = C_t<R>;
   const Workspace& w = P->ws;
   const int nsk = P->ns * P->nk;
@@ -472,9 +478,11 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
       return rc;
   }
   {
+    // with band energies requested, g_C = H c unweighted; the occupations
+    // are folded into the small adjoint matrices below
     PHASE(PH_PLANE_FWD);
-    if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), wsp(ws, w.c), wsp(ws, w.gc), occ, 0, nbt,
-                                         1.0 / N, st)))
+    if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), wsp(ws, w.c), wsp(ws, w.gc),
+                                         band_e ? P->d_ones : occ, 0, nbt, 1.0 / N, st)))
       return rc;
   }
   // orthonormalisation adjoint
@@ -490,7 +498,7 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
   {
     PHASE(PH_ADJ_SMALL);
     if ((rc = launch_adjoint_small((double2*)wsp(ws, w.adj), (double2*)wsp(ws, w.rinv), rh, negm2,
-                                   nsk, P->nb, st)))
+                                   nsk, P->nb, st, band_e ? occ : nullptr, band_e)))
       return rc;
   }
   PHASE(PH_ADJ_ROTATE);
@@ -633,6 +641,19 @@ int jrg_energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const
   if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad: spin-polarised LDA is not implemented");
   return P->prec == 64 ? energy_grad<double>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st)
                        : energy_grad<float>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st);
+}
+
+int jrg_energy_grad_bands(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
+                          double* energies, double* band_energies, void* g_re, void* g_im, void* ws,
+                          cudaStream_t st) {
+  if (!P || !w_re || !w_im || !occ || !energies || !band_energies || !g_re || !g_im || !ws)
+    return fail(JRG_ERR_INVALID, "jrg_energy_grad_bands: null argument");
+  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_bands: spin-polarised LDA is not implemented");
+  int rc = P->prec == 64
+               ? energy_grad_impl<double>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st, nullptr, band_energies)
+               : energy_grad_impl<float>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st, nullptr, band_energies);
+  profile_call_done(P);
+  return rc;
 }
 
 int jrg_band_trace_grad(const jrg_plan* P, const void* w_re, const void* w_im, const void* v_eff,

@@ -447,18 +447,28 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_big(const double2* __rest
 
 // Adjoint small matrices per (s,k), one CTA each:
 //   Rh = R^{-H};  K from A;  M2 = K R^{-H}  (stored negated: -M2)
+// With occupations f given, A holds C^H (H C) (unweighted): the band energies
+// Re A_bb are written to eps and the occupations are folded in as
+// A diag(f) (for K) and diag(f) R^{-H} (for Rh).
 __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict__ A,
                                                        const double2* __restrict__ Ri,
                                                        double2* __restrict__ Rh,
-                                                       double2* __restrict__ negM2, int nb) {
+                                                       double2* __restrict__ negM2, int nb,
+                                                       const double* __restrict__ f,
+                                                       double* __restrict__ eps) {
   const int sk = blockIdx.x;
   const size_t off = (size_t)sk * nb * nb;
   const double2* a = A + off;
   const double2* ri = Ri + off;
+  const double* fb = f ? f + (size_t)sk * nb : nullptr;
+  auto fw = [&](int j) { return fb ? fb[j] : 1.0; };
+  if (eps)
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) eps[(size_t)sk * nb + b] = a[b * nb + b].x;
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int i = e / nb, j = e % nb;
     const double2 v = ri[j * nb + i];
-    Rh[off + e] = make_double2(v.x, -v.y);
+    const double s = fw(i);
+    Rh[off + e] = make_double2(s * v.x, -s * v.y);
   }
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int i = e / nb, j = e % nb;
@@ -466,9 +476,9 @@ __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict
     double sx = 0.0, sy = 0.0;
     for (int l = j; l < nb; ++l) {
       double2 kil;
-      if (l > i) kil = a[i * nb + l];
-      else if (l < i) { const double2 t = a[l * nb + i]; kil = make_double2(t.x, -t.y); }
-      else kil = make_double2(a[i * nb + i].x, 0.0);
+      if (l > i) { const double2 t = a[i * nb + l]; const double s = fw(l); kil = make_double2(s * t.x, s * t.y); }
+      else if (l < i) { const double2 t = a[l * nb + i]; const double s = fw(i); kil = make_double2(s * t.x, -s * t.y); }
+      else kil = make_double2(fw(i) * a[i * nb + i].x, 0.0);
       const double2 r = ri[j * nb + l];   // conj later
       sx += kil.x * r.x + kil.y * r.y;
       sy += kil.y * r.x - kil.x * r.y;
@@ -911,8 +921,8 @@ int launch_cholesky_inv(const double2* S, double2* Rm, double2* Ri, int nsk, int
 }
 
 int launch_adjoint_small(const double2* A, const double2* Ri, double2* Rh, double2* negM2, int nsk,
-                         int nb, cudaStream_t st) {
-  k_adjoint_small<<<nsk, 256, 0, st>>>(A, Ri, Rh, negM2, nb);
+                         int nb, cudaStream_t st, const double* f, double* eps) {
+  k_adjoint_small<<<nsk, 256, 0, st>>>(A, Ri, Rh, negM2, nb, f, eps);
   JRG_LAUNCH_CHECK("k_adjoint_small");
   return JRG_OK;
 }

@@ -101,5 +101,6 @@ struct jrg_plan {
   int* slot_begin = nullptr;  // energy slot boundaries [5]
   double* d_cell = nullptr;   // cell (9) then reciprocal vectors (9)
   double* d_atoms = nullptr;  // positions [natom][3] then charges [natom]
+  double* d_ones = nullptr;   // [S*K*B] ones: unweighted band weights
   jrg::Profiler* prof = nullptr;
 };

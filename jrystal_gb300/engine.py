@@ -144,6 +144,24 @@ class PlaneWavePlan:
     _lib.check(st, "jrg_energy_grad")
     return self.energies, grad_re, grad_im
 
+  def energy_grad_bands(self, w_re: torch.Tensor, w_im: torch.Tensor, occupation,
+                        grad_re: Optional[torch.Tensor] = None,
+                        grad_im: Optional[torch.Tensor] = None):
+    """energy_and_grad plus the band energies <psi|T + V_eff|psi> (S,K,B)
+    float64 = d total / d occupation."""
+    self._check_param(w_re, "w_re")
+    self._check_param(w_im, "w_im")
+    occ = self._occ(occupation)
+    grad_re = torch.empty_like(w_re) if grad_re is None else grad_re
+    grad_im = torch.empty_like(w_im) if grad_im is None else grad_im
+    eps = torch.empty((self.num_spin, self.num_kpt, self.num_band), dtype=torch.float64,
+                      device=self.device)
+    st = self.lib.jrg_energy_grad_bands(self._h, _ptr(w_re), _ptr(w_im), _ptr(occ),
+                                        _ptr(self.energies), _ptr(eps), _ptr(grad_re),
+                                        _ptr(grad_im), _ptr(self.workspace), _stream())
+    _lib.check(st, "jrg_energy_grad_bands")
+    return self.energies, grad_re, grad_im, eps
+
   def band_trace_grad(self, w_re: torch.Tensor, w_im: torch.Tensor, v_eff, weights=None,
                       grad_re: Optional[torch.Tensor] = None,
                       grad_im: Optional[torch.Tensor] = None, with_grad: bool = True,

@@ -314,6 +314,39 @@ def gamma_occupation(num_k, num_electrons, spin=0, num_bands=None,
   return occ
 
 
+def simplex_proj(x, total):
+  """jrystal/_src/occupation.py:294-343 (push down / push up)."""
+  x = np.asarray(x, dtype=np.float64)
+  n = x.shape[0]
+  ar = np.arange(n)
+  xsum = x.sum()
+  with np.errstate(divide="ignore", invalid="ignore"):
+    if xsum <= total:
+      xs = np.sort(x)[::-1]
+      cs = np.cumsum(xs)
+      rho = (xsum - total + (ar + 1 - cs)) / (n - ar - 1)
+      k = int(np.argmax(xs - rho < 1.0))
+      lam = (total - xsum) / n if k == 0 else (total - xsum - (k - cs[k - 1])) / (n - k)
+      return np.minimum(x + lam, 1.0)
+    xs = np.sort(x)
+    cs = np.cumsum(xs)
+    rho = (xsum - total - cs) / (n - ar - 1)
+    k = int(np.argmax(xs > rho))
+    lam = (xsum - total) / n if k == 0 else (xsum - total - cs[k - 1]) / (n - k)
+    return np.maximum(x - lam, 0.0)
+
+
+def simplex_projector(param_up, param_down, num_electrons, spin=0, spin_restricted=True):
+  """jrystal/_src/occupation.py:346-375."""
+  nk, nb = param_up.shape
+  out = []
+  for p, m in ((param_up, (num_electrons + spin) // 2), (param_down, (num_electrons - spin) // 2)):
+    x = 1.0 / (1.0 + np.exp(-np.asarray(p, dtype=np.float64).ravel()))
+    out.append((simplex_proj(x, m * nk) / nk).reshape(nk, nb))
+  occ = np.stack(out)
+  return occ.sum(0, keepdims=True) if spin_restricted else occ
+
+
 def fermi_dirac_entropy(occ, eps=1e-8):
   """jrystal/_src/entropy.py:19-54."""
   num_spin, num_k, _ = occ.shape

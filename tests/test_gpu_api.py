@@ -105,8 +105,15 @@ def test_occupation_and_entropy():
   np.testing.assert_allclose(_np(gm), R.gamma_occupation(3, 8, num_bands=6))
   s = jr.entropy.fermi_dirac(u)
   assert abs(float(s) - R.fermi_dirac_entropy(_np(u))) < 1e-12
-  with pytest.raises(NotImplementedError):
-    jr.occupation.param_init(0, 4, 8, 1, method="idempotent")
+  prm = jr.occupation.param_init(0, 4, 8, 1, method="idempotent")
+  occ = jr.occupation.occupation(prm, 1, 8, method="idempotent")
+  assert abs(float(occ.sum()) - 8) < 1e-10
+  sp = jr.occupation.param_init(0, 4, 8, 1, method="simplex-projector")
+  occ = jr.occupation.occupation(sp, 1, 8, method="simplex-projector")
+  np.testing.assert_allclose(_np(occ), R.simplex_projector(_np(sp["param_up"]), _np(sp["param_down"]), 8),
+                             atol=1e-12)
+  with pytest.raises(ValueError):
+    jr.occupation.param_init(0, 4, 8, 1, method="fermi-dirac")
 
 
 def test_autograd_binding_matches_oracle(case):
