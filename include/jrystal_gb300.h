@@ -50,6 +50,8 @@ typedef enum {
 /* exchange-correlation terms, OR-ed: "lda_x" and "lda_c_vwn" */
 #define JRG_XC_LDA_X 1
 #define JRG_XC_LDA_C_VWN 2
+#define JRG_XC_GGA_X_PBE 4   /* PBE exchange (jax_xc gga_x_pbe); not combinable with the LDA flags */
+#define JRG_XC_GGA_C_PBE 8   /* PBE correlation (jax_xc gga_c_pbe) */
 
 typedef struct jrg_plan jrg_plan;
 

@@ -19,7 +19,7 @@ JRG_ERR_INVALID = 1
 JRG_ERR_CUDA = 2
 JRG_ERR_NUMERIC = 3
 JRG_ERR_UNSUPPORTED = 4
-XC_FLAGS = {"lda_x": 1, "lda_c_vwn": 2}
+XC_FLAGS = {"lda_x": 1, "lda_c_vwn": 2, "gga_x_pbe": 4, "gga_c_pbe": 8}
 
 # exported entry points and their argument types
 _vp = ct.c_void_p

@@ -36,6 +36,11 @@ template <typename R> int launch_kinetic(const void*, const double*, const doubl
 int launch_precond_scale(const float*, const void*, const double*, const double*, const double*, int, int, int, long long, float, float, float*, cudaStream_t);
 int launch_sum_slots(const double*, const int*, double*, int, const int*, cudaStream_t);
 int launch_band_trace_sums(const double2*, int, int, const double*, int, double*, cudaStream_t);
+template <typename R> int launch_mul_ig(const void*, const double*, void*, int, long long, double, cudaStream_t);
+template <typename R> int launch_gga_local(const void*, void*, void*, void*, void*, double*, int, long long, int, double, int, cudaStream_t);
+template <typename R> int launch_div_g(void*, const void*, const void*, const double*, long long, double, cudaStream_t);
+template <typename R> int launch_potential_gga(const void*, double, void*, const void*, long long, cudaStream_t);
+constexpr int kXcGga = JRG_XC_GGA_X_PBE | JRG_XC_GGA_C_PBE;
 template <typename R> int launch_geometry_tables(double*, double*, void*, const double*, const double*, const double*, int, int, int, int, double, cudaStream_t);
 int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
 template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t);
@@ -116,6 +121,7 @@ static void layout_workspace(jrg_plan* P) {
   w.ekin = take(nbt * sizeof(double));
   w.dinv = take(nbt * sizeof(double));
   w.rot_scratch = take(nsk * 2 * 128 * 64 * sizeof(uint32_t));   // split B of the TF32 rotations
+  w.gga = (P->xc & kXcGga) ? take(3 * (size_t)P->ngrid * C) : 0;   // gradient / flux grids of PBE
   w.total = o;
 }
 
@@ -170,6 +176,10 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
   P->ngrid = (long long)P->nx * P->ny * P->nz;
   P->ns = d->num_spin; P->nk = d->num_kpt; P->nb = d->num_band; P->ng = d->num_g;
   P->xc = d->xc;
+  if ((P->xc & ~15) || ((P->xc & 3) && (P->xc & kXcGga))) {
+    delete P;
+    return fail(JRG_ERR_UNSUPPORTED, "xc: LDA and PBE terms cannot be combined");
+  }
   std::memcpy(P->cell, d->cell, sizeof(P->cell));
   {
     const double* a = d->cell;
@@ -400,6 +410,53 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
                           wsp(ws, w.rot_scratch), st);
 }
 
+// PBE terms of the grid phase.  Step 1 (from rho(G) in rhog, before it is
+// overwritten): the three gradient grids grad_a rho = IFFT(i G_a rho(G))/N.
+template <typename R>
+static int gga_gradients(const jrg_plan* P, const C_t<R>* rhog, void* ws, cudaStream_t st) {
+  using C = C_t<R>;
+  const Workspace& w = P->ws;
+  C* g = (C*)wsp(ws, w.gga);
+  C* scratch = (C*)wsp(ws, w.fft_scratch);
+  const C* tw = (const C*)P->d.tw;
+  const double N = (double)P->ngrid;
+  int rc;
+  for (int a = 0; a < 3; ++a) {
+    C* ga = g + (size_t)a * P->ngrid;
+    if ((rc = launch_mul_ig<R>(rhog, P->d.gvec, ga, a, P->ngrid, 1.0 / N, st))) return rc;
+    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, ga, scratch, ga, 1.0, st))) return rc;
+  }
+  return JRG_OK;
+}
+
+// Step 2: local terms (E_xc partials into slot_x, f_rho into vout) and, for the
+// potential, vout = Re(vri) vscale + f_rho - 2 div(f_sigma grad rho); with
+// eps_only, vout = eps(rho, sigma) per particle instead.
+template <typename R>
+static int gga_potential(const jrg_plan* P, const void* rho, const C_t<R>* vri, double vscale,
+                         void* vout, double* slot_x, int eps_only, void* ws, cudaStream_t st) {
+  using C = C_t<R>;
+  const Workspace& w = P->ws;
+  C* g = (C*)wsp(ws, w.gga);
+  C* g1 = g + P->ngrid;
+  C* g2 = g + 2 * (size_t)P->ngrid;
+  C* scratch = (C*)wsp(ws, w.fft_scratch);
+  const C* tw = (const C*)P->d.tw;
+  const double N = (double)P->ngrid;
+  int rc;
+  if ((rc = launch_gga_local<R>(rho, g, g1, g2, vout, slot_x, kXcBlocks, P->ngrid, P->xc,
+                                P->vol / N, eps_only, st)))
+    return rc;
+  if (eps_only) return JRG_OK;
+  for (int a = 0; a < 3; ++a) {
+    C* ga = g + (size_t)a * P->ngrid;
+    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, false, ga, scratch, ga, 1.0, st))) return rc;
+  }
+  if ((rc = launch_div_g<R>(g, g1, g2, P->d.gvec, P->ngrid, 1.0 / N, st))) return rc;
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, g, scratch, g, 1.0, st))) return rc;
+  return launch_potential_gga<R>(vri, vscale, vout, g, P->ngrid, st);
+}
+
 // density of the band-major coefficients held in workspace slot c
 template <typename R>
 static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* rho_out,
@@ -456,6 +513,8 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
     C* scratch = (C*)wsp(ws, w.fft_scratch);
     const C* tw = (const C*)P->d.tw;
     if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+    const bool gga = (P->xc & kXcGga) != 0;
+    if (gga && (rc = gga_gradients<R>(P, rhog, ws, st))) return rc;
     // Hartree / external (slots after the kinetic ones) and dE/drho in G space (in place)
     const double pref = P->vol / (N * N);
     if ((rc = launch_recip_terms<R>(rhog, P->d.ginv, P->d.vext, rhog, slots + nbt + kRecipBlocks,
@@ -463,9 +522,14 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
       return rc;
     if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st)))
       return rc;
-    if ((rc = launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks,
-                                  kXcBlocks, P->ngrid, P->xc, P->vol / N, st)))
+    if (gga) {
+      if ((rc = gga_potential<R>(P, rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks, 0,
+                                 ws, st)))
+        return rc;
+    } else if ((rc = launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks,
+                                         kXcBlocks, P->ngrid, P->xc, P->vol / N, st))) {
       return rc;
+    }
     if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st)))
       return rc;
   }
@@ -613,6 +677,11 @@ static int potential_entry(const jrg_plan* P, const void* rho, int ks, void* out
   if ((rc = launch_real_part<R>(rhog, o, P->ngrid, 1.0, st))) return rc;
   if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, P->d.vext, scratch, rhog, 1.0 / N, st))) return rc;
   if ((rc = launch_real_part<R>(rhog, o + P->ngrid, P->ngrid, 1.0, st))) return rc;
+  if (P->xc & kXcGga) {
+    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+    if ((rc = gga_gradients<R>(P, rhog, ws, st))) return rc;
+    return gga_potential<R>(P, rho, nullptr, 0.0, o + 2 * P->ngrid, nullptr, ks ? 0 : 1, ws, st);
+  }
   return launch_xc_field<R>(rho, o + 2 * P->ngrid, P->ngrid, P->xc, ks, st);
 }
 

@@ -120,6 +120,146 @@ template <typename R> __device__ __forceinline__ void lda_eps_v_t(R rho, int xc,
   else lda_eps_v(rho, xc, eps, v);
 }
 
+// ------------------------------------------------------------------------
+// PBE (Perdew, Burke & Ernzerhof 1996), unpolarised, libxc parameters:
+// f(rho, sigma) = rho (eps_x + eps_c) with exact partials f_rho, f_sigma from
+// forward-mode dual numbers (value and the two partials carried together).
+// Evaluated in FP64 on both precision paths.
+// ------------------------------------------------------------------------
+struct D2 {
+  double v, r, s;   // value, d/d rho, d/d sigma
+};
+__device__ __forceinline__ D2 dconst(double c) { return D2{c, 0.0, 0.0}; }
+__device__ __forceinline__ D2 operator+(D2 a, D2 b) { return D2{a.v + b.v, a.r + b.r, a.s + b.s}; }
+__device__ __forceinline__ D2 operator-(D2 a, D2 b) { return D2{a.v - b.v, a.r - b.r, a.s - b.s}; }
+__device__ __forceinline__ D2 operator*(D2 a, D2 b) {
+  return D2{a.v * b.v, a.r * b.v + a.v * b.r, a.s * b.v + a.v * b.s};
+}
+__device__ __forceinline__ D2 operator/(D2 a, D2 b) {
+  const double q = a.v / b.v;
+  return D2{q, (a.r - q * b.r) / b.v, (a.s - q * b.s) / b.v};
+}
+__device__ __forceinline__ D2 operator*(double c, D2 a) { return D2{c * a.v, c * a.r, c * a.s}; }
+__device__ __forceinline__ D2 operator+(double c, D2 a) { return D2{c + a.v, a.r, a.s}; }
+__device__ __forceinline__ D2 operator-(double c, D2 a) { return D2{c - a.v, -a.r, -a.s}; }
+__device__ __forceinline__ D2 dlog(D2 a) { return D2{log(a.v), a.r / a.v, a.s / a.v}; }
+__device__ __forceinline__ D2 dexp(D2 a) { const double e = exp(a.v); return D2{e, e * a.r, e * a.s}; }
+__device__ __forceinline__ D2 dsqrt(D2 a) {
+  const double q = sqrt(a.v);
+  return D2{q, 0.5 * a.r / q, 0.5 * a.s / q};
+}
+__device__ __forceinline__ D2 dcbrt(D2 a) {
+  const double q = cbrt(a.v);
+  return D2{q, q * a.r / (3.0 * a.v), q * a.s / (3.0 * a.v)};
+}
+
+__device__ D2 pbe_f(double rho_v, double sigma_v, int xc) {
+  constexpr double kPi = 3.14159265358979323846;
+  const D2 rho{rho_v, 1.0, 0.0}, sigma{sigma_v, 0.0, 1.0};
+  const D2 kf = dcbrt((3.0 * kPi * kPi) * rho);
+  D2 eps = dconst(0.0);
+  if (xc & JRG_XC_GGA_X_PBE) {
+    constexpr double kappa = 0.804, mu = 0.2195149727645171;
+    const D2 s2 = sigma / (4.0 * (kf * kf) * (rho * rho));
+    const D2 fx = (1.0 + kappa) - kappa * (dconst(1.0) / (1.0 + (mu / kappa) * s2));
+    const double cx = -0.75 * cbrt(3.0 / kPi);
+    eps = eps + cx * (dcbrt(rho) * fx);
+  }
+  if (xc & JRG_XC_GGA_C_PBE) {
+    constexpr double A = 0.0310907, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382,
+                     b4 = 0.49294;
+    constexpr double beta = 0.06672455060314922;
+    const double gamma = (1.0 - log(2.0)) / (kPi * kPi);
+    const D2 rs = dcbrt(dconst(3.0 / (4.0 * kPi)) / rho);
+    const D2 srs = dsqrt(rs);
+    const D2 den = (2.0 * A) * (b1 * srs + b2 * rs + b3 * (rs * srs) + b4 * (rs * rs));
+    const D2 ec = (-2.0 * A) * ((1.0 + a1 * rs) * dlog(1.0 + dconst(1.0) / den));
+    const D2 ks2 = (4.0 / kPi) * kf;
+    const D2 t2 = sigma / (4.0 * ks2 * (rho * rho));
+    const D2 aa = dconst(beta / gamma) / (dexp((-1.0 / gamma) * ec) - dconst(1.0));
+    const D2 at2 = aa * t2;
+    const D2 h = gamma * dlog(1.0 + (beta / gamma) * (t2 * (1.0 + at2) / (1.0 + at2 + at2 * at2)));
+    eps = eps + ec + h;
+  }
+  return rho * eps;
+}
+
+// out = i G_a in * scale   (gradient component a in reciprocal space)
+template <typename R>
+__global__ void k_mul_ig(const C_t<R>* __restrict__ in, const double* __restrict__ gvec,
+                         C_t<R>* __restrict__ out, int a, long long n, double scale) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double g = gvec[3 * i + a] * scale;
+    const C_t<R> v = in[i];
+    out[i] = cmk<C_t<R>>(-g * (double)v.y, g * (double)v.x);
+  }
+}
+
+// Local PBE terms: sigma = |grad rho|^2 from the real parts of the three
+// gradient grids; E_xc partials (vol/N sum f), vloc = f_rho, and the
+// vector field h_a = f_sigma grad_a rho (0 where sigma = 0) written over the
+// gradient grids.
+// eps_only: write eps = f / rho (energy per particle) into vloc instead.
+template <typename R>
+__global__ void __launch_bounds__(256) k_gga_local(const R* __restrict__ rho, C_t<R>* __restrict__ g0,
+                                                   C_t<R>* __restrict__ g1, C_t<R>* __restrict__ g2,
+                                                   R* __restrict__ vloc, double* __restrict__ slot_x,
+                                                   long long n, int xc, double pref, int eps_only) {
+  __shared__ double red[32];
+  double ex = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double r = rho[i];
+    const double d0 = g0[i].x, d1 = g1[i].x, d2 = g2[i].x;
+    const double sig = d0 * d0 + d1 * d1 + d2 * d2;
+    double fr = 0.0, fs = 0.0, fe = 0.0;
+    if (r > 1e-15) {
+      const D2 f = pbe_f(r, sig, xc);
+      ex += f.v;
+      fr = f.r;
+      fs = sig > 0.0 ? f.s : 0.0;
+      fe = f.v / r;
+    }
+    vloc[i] = (R)(eps_only ? fe : fr);
+    g0[i] = cmk<C_t<R>>(fs * d0, 0.0);
+    g1[i] = cmk<C_t<R>>(fs * d1, 0.0);
+    g2[i] = cmk<C_t<R>>(fs * d2, 0.0);
+  }
+  ex = block_sum(ex, red);
+  if (threadIdx.x == 0 && slot_x) slot_x[blockIdx.x] = ex * pref;
+}
+
+// g0 = scale * sum_a i G_a h_a   (divergence in reciprocal space)
+template <typename R>
+__global__ void k_div_g(C_t<R>* __restrict__ g0, const C_t<R>* __restrict__ g1,
+                        const C_t<R>* __restrict__ g2, const double* __restrict__ gvec, long long n,
+                        double scale) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const C_t<R> h[3] = {g0[i], g1[i], g2[i]};
+    double x = 0.0, y = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const double g = gvec[3 * i + a];
+      x -= g * (double)h[a].y;
+      y += g * (double)h[a].x;
+    }
+    g0[i] = cmk<C_t<R>>(x * scale, y * scale);
+  }
+}
+
+// vr = Re(vri) * vscale + vr - 2 Re(div)   (vr holds f_rho on entry; vri may be null)
+template <typename R>
+__global__ void k_potential_gga(const C_t<R>* __restrict__ vri, double vscale, R* __restrict__ vr,
+                                const C_t<R>* __restrict__ div, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double base = vri ? (double)vri[i].x * vscale : 0.0;
+    vr[i] = (R)(base + (double)vr[i] - 2.0 * (double)div[i].x);
+  }
+}
+
 // V(r) = Re(vri)*vscale + v_xc(rho) (when vr is given);  E_xc = vol/N * sum eps(rho) rho.
 template <typename R>
 __global__ void __launch_bounds__(256) k_potential(const R* __restrict__ rho,
@@ -490,6 +630,44 @@ int launch_kinetic(const void* coef, const double* tk, const double* occ, double
   return JRG_OK;
 }
 
+template <typename R>
+int launch_mul_ig(const void* in, const double* gvec, void* out, int a, long long n, double scale,
+                  cudaStream_t st) {
+  k_mul_ig<R><<<grid_for(n), 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(in), gvec,
+                                           reinterpret_cast<C_t<R>*>(out), a, n, scale);
+  JRG_LAUNCH_CHECK("k_mul_ig");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_gga_local(const void* rho, void* g0, void* g1, void* g2, void* vloc, double* slot_x,
+                     int nblocks, long long n, int xc, double pref, int eps_only, cudaStream_t st) {
+  k_gga_local<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const R*>(rho), reinterpret_cast<C_t<R>*>(g0),
+                                          reinterpret_cast<C_t<R>*>(g1), reinterpret_cast<C_t<R>*>(g2),
+                                          reinterpret_cast<R*>(vloc), slot_x, n, xc, pref, eps_only);
+  JRG_LAUNCH_CHECK("k_gga_local");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_div_g(void* g0, const void* g1, const void* g2, const double* gvec, long long n,
+                 double scale, cudaStream_t st) {
+  k_div_g<R><<<grid_for(n), 256, 0, st>>>(reinterpret_cast<C_t<R>*>(g0), reinterpret_cast<const C_t<R>*>(g1),
+                                          reinterpret_cast<const C_t<R>*>(g2), gvec, n, scale);
+  JRG_LAUNCH_CHECK("k_div_g");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_potential_gga(const void* vri, double vscale, void* vr, const void* div, long long n,
+                         cudaStream_t st) {
+  k_potential_gga<R><<<grid_for(n), 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(vri), vscale,
+                                                  reinterpret_cast<R*>(vr),
+                                                  reinterpret_cast<const C_t<R>*>(div), n);
+  JRG_LAUNCH_CHECK("k_potential_gga");
+  return JRG_OK;
+}
+
 int launch_band_trace_sums(const double2* A, int nsk, int nb, const double* slots, int nkin,
                           double* out, cudaStream_t st) {
   k_band_trace_sums<<<1, 256, 0, st>>>(A, nsk, nb, slots, nkin, out);
@@ -563,6 +741,14 @@ int launch_twiddles(int n, int prec, void* out, cudaStream_t st) {
                                  int, int, int, cudaStream_t);                                  \
   template int launch_geometry_tables<R>(double*, double*, void*, const double*, const double*,   \
                                          const double*, int, int, int, int, double, cudaStream_t); \
+  template int launch_mul_ig<R>(const void*, const double*, void*, int, long long, double,        \
+                                cudaStream_t);                                                  \
+  template int launch_gga_local<R>(const void*, void*, void*, void*, void*, double*, int,          \
+                                   long long, int, double, int, cudaStream_t);                  \
+  template int launch_div_g<R>(void*, const void*, const void*, const double*, long long, double, \
+                               cudaStream_t);                                                   \
+  template int launch_potential_gga<R>(const void*, double, void*, const void*, long long,        \
+                                       cudaStream_t);                                           \
   template int launch_adam<R>(void*, const void*, void*, void*, const float*, long long, double,  \
                               double, double, double, double, double, cudaStream_t);
 JRG_INST_GRID(float)

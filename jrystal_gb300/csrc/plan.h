@@ -76,7 +76,7 @@ struct AdamArgs {
 // Workspace offsets (bytes) of one plan.
 struct Workspace {
   size_t wc, c, gram_part, gram, rmat, rinv, t, u, rho_part, rho, rhog, fft_scratch, vr,
-      gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, total;
+      gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, total;
   int gram_splits;
   int ngroups;    // density partial groups
   int nepart;     // energy partial slots

@@ -43,6 +43,20 @@ def mask_plan(mask, num_kpt, num_band, num_spin, precision) -> PlaneWavePlan:
                   num_band, num_spin, precision)
 
 
+def field_plan(g_vector_grid, xc, precision) -> PlaneWavePlan:
+  """Plan for grid-only work (potentials, PBE fields) on the cell whose G
+  grid is given: the reciprocal vectors are the G vectors of the FFT indices
+  (1,0,0), (0,1,0), (0,0,1), and the cell follows as 2 pi B^{-T}."""
+  g = np.asarray(g_vector_grid, dtype=np.float64)
+  grid = g.shape[:3]
+  recip = np.stack([g[1, 0, 0], g[0, 1, 0], g[0, 0, 1]])
+  cell = 2.0 * np.pi * np.linalg.inv(recip).T
+  mask = np.zeros(grid, dtype=bool)
+  mask[0, 0, 0] = True
+  return get_plan(cell, np.zeros((0, 3)), np.zeros(0), grid, mask, np.zeros((1, 3)), 1, 1,
+                  precision, xc)
+
+
 def clear():
   for p in _CACHE.values():
     p.close()

@@ -393,6 +393,99 @@ def lda_c_vwn(rho):
   return np.where(ok, eps, 0.0), np.where(ok, v, 0.0)
 
 
+# PBE generalised-gradient approximation (Perdew, Burke & Ernzerhof, Phys.
+# Rev. Lett. 77, 3865 (1996)), unpolarised, with the libxc parameters that
+# jax_xc's gga_x_pbe / gga_c_pbe use: kappa 0.804, mu 0.2195149727645171,
+# beta 0.06672455060314922, gamma (1 - ln 2)/pi^2, and the Perdew-Wang 1992
+# correlation (Phys. Rev. B 45, 13244) with A = 0.0310907 underneath.
+# Written with operations that accept complex arguments, so that exact first
+# derivatives come from the complex step f'(x) = Im f(x + i h) / h.
+PBE_KAPPA, PBE_MU = 0.804, 0.2195149727645171
+PBE_BETA = 0.06672455060314922
+PBE_GAMMA = (1.0 - math.log(2.0)) / math.pi**2
+PW92_A, PW92_A1 = 0.0310907, 0.21370
+PW92_B = (7.5957, 3.5876, 1.6382, 0.49294)
+
+
+def pw92_c(rho):
+  """Perdew-Wang 1992 paramagnetic correlation energy per particle."""
+  rs = (3.0 / (4.0 * np.pi * rho))**(1.0 / 3.0)
+  srs = np.sqrt(rs)
+  b1, b2, b3, b4 = PW92_B
+  den = 2.0 * PW92_A * (b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs)
+  return -2.0 * PW92_A * (1.0 + PW92_A1 * rs) * np.log(1.0 + 1.0 / den)
+
+
+def pbe_x(rho, sigma):
+  """PBE exchange energy per particle."""
+  kf = (3.0 * np.pi**2 * rho)**(1.0 / 3.0)
+  s2 = sigma / (4.0 * kf * kf * rho * rho)
+  fx = 1.0 + PBE_KAPPA - PBE_KAPPA / (1.0 + PBE_MU * s2 / PBE_KAPPA)
+  return -0.75 * (3.0 / np.pi)**(1.0 / 3.0) * rho**(1.0 / 3.0) * fx
+
+
+def pbe_c(rho, sigma):
+  """PBE correlation energy per particle: PW92 + H(r_s, t), phi = 1."""
+  ec = pw92_c(rho)
+  kf = (3.0 * np.pi**2 * rho)**(1.0 / 3.0)
+  ks2 = 4.0 * kf / np.pi
+  t2 = sigma / (4.0 * ks2 * rho * rho)
+  a = (PBE_BETA / PBE_GAMMA) / (np.exp(-ec / PBE_GAMMA) - 1.0)
+  at2 = a * t2
+  h = PBE_GAMMA * np.log(1.0 + (PBE_BETA / PBE_GAMMA) * t2 * (1.0 + at2) / (1.0 + at2 + at2 * at2))
+  return ec + h
+
+
+_GGA = {"gga_x_pbe": pbe_x, "gga_c_pbe": pbe_c}
+
+
+def is_gga(xc_type):
+  parts = xc_type.split("+")
+  g = [p in _GGA for p in parts]
+  if any(g) and not all(g):
+    raise NotImplementedError("mixed LDA/GGA functional strings are not supported")
+  return all(g)
+
+
+def gga_f(rho, sigma, xc_type):
+  """f = rho * eps(rho, sigma) summed over the parts, 0 below the density
+  threshold; with complex-step derivatives f_rho and f_sigma."""
+  rho = np.asarray(rho, dtype=np.float64)
+  sigma = np.maximum(np.asarray(sigma, dtype=np.float64), 0.0)
+  ok = rho > DENS_THRESHOLD
+  r = np.where(ok, rho, 1.0)
+  sg = np.where(ok, sigma, 0.0)
+  h = 1e-40
+
+  def f(rr, ss):
+    return rr * sum(_GGA[p](rr, ss) for p in xc_type.split("+"))
+
+  val = f(r.astype(complex), sg.astype(complex)).real
+  f_rho = f(r + 1j * h * r, sg.astype(complex)).imag / (h * r)
+  f_sig = f(r.astype(complex), sg + 1j * h).imag / h
+  return (np.where(ok, val, 0.0), np.where(ok, f_rho, 0.0), np.where(ok, f_sig, 0.0))
+
+
+def grad_real(x, g_vector_grid):
+  """Cartesian gradient of a real grid function by FFT, (3, x, y, z)."""
+  xg = _fftn(x)
+  return np.stack([np.real(_ifftn(1j * g_vector_grid[..., a] * xg)) for a in range(3)])
+
+
+def gga_energy_potential(rho, g_vector_grid, vol, xc_type):
+  """E_xc = sum f(rho, |grad rho|^2) vol/N and dE_xc/d rho(r) (vol/N units):
+  v = f_rho - 2 div(f_sigma grad rho)  (jrystal/_src/xc.py:67-219: the local
+  term minus 2 (grad t . grad rho + t lap rho), t = f_sigma)."""
+  n = rho.size
+  gr = grad_real(rho, g_vector_grid)
+  sigma = np.sum(gr * gr, axis=0)
+  fval, f_rho, f_sig = gga_f(rho, sigma, xc_type)
+  t = np.where(sigma > 0, f_sig, 0.0)
+  hg = [_fftn(t * gr[a]) for a in range(3)]
+  div = np.real(_ifftn(sum(1j * g_vector_grid[..., a] * hg[a] for a in range(3))))
+  return float(np.sum(fval) * vol / n), f_rho - 2.0 * div, fval
+
+
 _XC = {"lda_x": lda_x, "lda_c_vwn": lda_c_vwn}
 
 
@@ -708,7 +801,10 @@ def energy_terms(w_re, w_im, sysm: System, with_grad=True):
   e_kin = kinetic_energy(gvec, sysm.kpts, dense, occ)
   e_ext = external_energy(rho_g, sysm.positions, sysm.charges, gvec, vol)
   e_har = hartree_energy(rho_g, gvec, vol, False)
-  e_xc = xc_energy(rho, vol, sysm.xc, False)
+  if is_gga(sysm.xc):
+    e_xc, v_xc_gga, _ = gga_energy_potential(rho[0], gvec, vol, sysm.xc)
+  else:
+    e_xc = xc_energy(rho, vol, sysm.xc, False)
   terms = dict(kinetic=e_kin, external=e_ext, hartree=e_har, xc=e_xc)
   terms["total"] = e_kin + e_ext + e_har + e_xc
   if not with_grad:
@@ -716,7 +812,7 @@ def energy_terms(w_re, w_im, sysm: System, with_grad=True):
   # dE/d rho(r) = (vol/N) V(r)
   v_g = (hartree_reciprocal(rho_g, gvec, kohn_sham=True) +
          external_reciprocal(sysm.positions, sysm.charges, gvec, vol))
-  _, v_xc = xc_eps_v(rho[0], sysm.xc)
+  v_xc = v_xc_gga if is_gga(sysm.xc) else xc_eps_v(rho[0], sysm.xc)[1]
   v_r = np.real(_ifftn(v_g)) + v_xc
   hpsi = _fftn(v_r[None, None, None] * wave)
   hpsi = hpsi[..., mask] * (np.sqrt(vol) / n)     # (s,k,b,g)
