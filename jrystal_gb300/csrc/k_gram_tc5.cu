@@ -12,18 +12,20 @@
 //
 // Warp-specialised pipeline of one CTA (one (s,k), one G range, 256
 // threads), coordinated by mbarriers only:
-//   producers (warps 1-3, 6-7): load a chunk of 32 G vectors of X and Y from
-//     global memory (registers, one chunk ahead), split it into TF32 hi/lo
-//     parts in the no-swizzle K-major core-matrix layout of one of three MMA
-//     stages, and arrive on the stage's "full" barrier;
+//   producers (warps 1-3, 6-7): stream chunks of 32 G vectors of X and Y into
+//     a ring of raw shared-memory buffers with cp.async four chunks ahead
+//     (named barrier 1 among the producers only), split each chunk into TF32
+//     hi/lo parts in the no-swizzle K-major core-matrix layout of one of the
+//     MMA stages, and arrive on the stage's "full" barrier;
 //   MMA issuer (warp 0, one lane): waits "full", issues the chunk's 24 MMAs
 //     into one of two 32-column tensor-memory accumulators and commits them
 //     to the stage's "empty" barrier and the accumulator's "ready" barrier;
-//   epilogue (warps 4-5, tensor-memory lanes 0-63): waits "ready", moves the
-//     2nb accumulator rows into FP64 registers (tcgen05.ld) and arrives on the
-//     accumulator's "free" barrier.
-// FP32 sums therefore never run over more than one chunk (64 real terms x 3
-// products), as in the CUDA-core Gram.  Every wait is bounded: on a timeout
+//   epilogue (warps 4-5, tensor-memory lanes 0-63): waits "ready", adds the
+//     2nb accumulator rows (tcgen05.ld) into Kahan-compensated FP32 sums and
+//     arrives on the accumulator's "free" barrier.
+// Plain FP32 sums therefore never run over more than one chunk (64 real
+// terms x 3 products); across chunks the compensated sums keep the error at
+// the level of the CUDA-core Gram's FP64 reduction.  Every wait is bounded: on a timeout
 // the waiting thread sets bit 2 of the workspace flag word and a shared
 // abort flag that ends every role's loop; the CTA then waits (bounded) for
 // its issued MMAs, frees its tensor memory and returns.
@@ -50,13 +52,17 @@ constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kN 
                             ((uint32_t)(kM >> 4) << 24);
 constexpr long kWaitLimit = 1L << 22;
 
-constexpr int kStages = 3;
+constexpr int kMaxStages = 3;
 constexpr int kNProd = 160;              // producer threads (warps 1, 2, 3, 6, 7)
+constexpr int kRawDepth = 4;             // raw chunks in flight per CTA
+constexpr int kRawPitch = kGC + 1;       // complex elements per raw row (padded)
 
 struct Layout {
   int ga, gb;                      // 8-row groups holding A (2nb rows) and B (nb rows)
   int a_hi, a_lo, b_hi, b_lo;      // part offsets inside a stage
+  int stages;                      // MMA stages (3, or 2 when 3 do not fit)
   int stage;                       // bytes per MMA stage
+  int raw, raw_stage;              // raw chunk ring
   int bars;                        // mbarriers: full[3], empty[3], ready[2], free[2]
   int total;
 };
@@ -70,10 +76,17 @@ __host__ __device__ inline Layout layout_for(int nb) {
   L.b_hi = 2 * L.ga * kSBO;
   L.b_lo = (2 * L.ga + L.gb) * kSBO;
   L.stage = 2 * (L.ga + L.gb) * kSBO;
-  // an MMA reads 16 row groups of A (4 of B) from a part's start: the span
-  // past the last stage stays inside the allocation
-  L.bars = kStages * L.stage + 16 * kSBO;
-  L.total = L.bars + 128;
+  L.raw_stage = 2 * nb * kRawPitch * 8;
+  L.stages = kMaxStages;
+  for (;;) {
+    // an MMA reads 16 row groups of A (4 of B) from a part's start: the span
+    // past the last stage stays inside the allocation (pad before the raw ring)
+    L.raw = L.stages * L.stage + 16 * kSBO;
+    L.bars = L.raw + kRawDepth * L.raw_stage;
+    L.total = L.bars + 128;
+    if (L.total <= 227 * 1024 || L.stages == 2) break;
+    --L.stages;
+  }
   return L;
 }
 
@@ -158,14 +171,15 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
   }
   const uint32_t bar_base = smem_u32(sm + L.bars);
   auto full = [&](int s) { return bar_base + 8u * s; };
-  auto empty = [&](int s) { return bar_base + 8u * (kStages + s); };
-  auto ready = [&](int b) { return bar_base + 8u * (2 * kStages + b); };
-  auto freed = [&](int b) { return bar_base + 8u * (2 * kStages + 2 + b); };
+  const int S = L.stages;
+  auto empty = [&](int s) { return bar_base + 8u * (kMaxStages + s); };
+  auto ready = [&](int b) { return bar_base + 8u * (2 * kMaxStages + b); };
+  auto freed = [&](int b) { return bar_base + 8u * (2 * kMaxStages + 2 + b); };
   volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + L.bars + 96);
   int* issued = reinterpret_cast<int*>(sm + L.bars + 100);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + L.bars + 104);
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < S; ++s) {
       mbar_init(full(s), kNProd);
       mbar_init(empty(s), 1);
     }
@@ -196,8 +210,8 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       for (int c = 0; c < nchunk && !*abort_flag; ++c) {
-        const int s = c % kStages, b = c & 1;
-        if (!mbar_wait(full(s), (c / kStages) & 1)) { timed_out(); break; }
+        const int s = c % S, b = c & 1;
+        if (!mbar_wait(full(s), (c / S) & 1)) { timed_out(); break; }
         if (c >= 2 && !mbar_wait(freed(b), ((c - 2) >> 1) & 1)) { timed_out(); break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t base = smem_u32(sm + s * L.stage);
@@ -218,10 +232,10 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
     }
     __syncwarp();
   } else if (warp == 4 || warp == 5) {
-    // ---------------- epilogue: accumulator rows 0..63 -> FP64 ----------------
-    double acc64[32];
+    // ---------------- epilogue: accumulator rows 0..63, compensated sums ----------------
+    float sum[32], comp[32];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) acc64[j] = 0.0;
+    for (int j = 0; j < 32; ++j) { sum[j] = 0.f; comp[j] = 0.f; }
     for (int c = 0; c < nchunk; ++c) {
       const int b = c & 1;
       const bool ok = mbar_wait(ready(b), (c >> 1) & 1);
@@ -244,80 +258,89 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
           : "r"(tmem + ((uint32_t)((warp - 4) * 32) << 16) + (uint32_t)(b * 32))
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-      for (int j = 0; j < 32; ++j) acc64[j] += (double)__uint_as_float(v[j]);
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(freed(b));
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {   // Kahan: sum - comp is the running total
+        const float y = __uint_as_float(v[j]) - comp[j];
+        const float t = sum[j] + y;
+        comp[j] = (t - sum[j]) - y;
+        sum[j] = t;
+      }
     }
     const bool done = !*abort_flag;
     const int row = (warp - 4) * 32 + lane;
     if (row < nb) {
 #pragma unroll
       for (int j = 0; j < 32; ++j)
-        if (j < nb) out[row * nb + j].x = done ? acc64[j] : 0.0;
+        if (j < nb) out[row * nb + j].x = done ? (double)sum[j] - (double)comp[j] : 0.0;
     } else if (row < 2 * nb) {
 #pragma unroll
       for (int j = 0; j < 32; ++j)
-        if (j < nb) out[(row - nb) * nb + j].y = done ? -acc64[j] : 0.0;
+        if (j < nb) out[(row - nb) * nb + j].y = done ? (double)comp[j] - (double)sum[j] : 0.0;
     }
   } else {
     // ---------------- producers ----------------
     const int p = (warp < 4 ? warp - 1 : warp - 3) * 32 + lane;   // 0 .. kNProd-1
-    const int ncore = L.gb * kNKC * 16;    // (row, k pair) slots of an nb-row part
-    constexpr int kMaxSlots = (4 * kNKC * 16 + kNProd - 1) / kNProd;   // nb <= 32
-    float2 xv[kMaxSlots], yv[kMaxSlots];
-    auto slot_rg = [&](int e, int& r, int& gl) {
-      const int cm = e >> 4, w = e & 15;
-      const int rg = cm / kNKC, kc = cm - rg * kNKC;
-      r = rg * 8 + (w >> 1);
-      gl = 2 * kc + (w & 1);
-    };
-    auto load = [&](int c) {
-      const int g0 = g_begin + c * kGC;
-#pragma unroll
-      for (int q = 0; q < kMaxSlots; ++q) {
-        const int e = p + q * kNProd;
-        int r, gl;
-        slot_rg(e, r, gl);
-        const int g = g0 + gl;
-        float2 x = make_float2(0.f, 0.f), y = x;
-        if (e < ncore && r < nb && g < g_end) {
-          if (LAY == kLaySplit) {
+    auto prod_sync = [] { asm volatile("bar.sync 1, %0;" ::"n"(kNProd) : "memory"); };
+    auto raw_x = [&](int q) { return reinterpret_cast<float2*>(sm + L.raw + q * L.raw_stage); };
+    auto load_raw = [&](int c) {   // cp.async of chunk c into raw slot c % kRawDepth
+      if (c < nchunk) {
+        float2* xr = raw_x(c % kRawDepth);
+        float2* yr = xr + nb * kRawPitch;
+        const int g0 = g_begin + c * kGC;
+        for (int e = p; e < 2 * nb * kGC; e += kNProd) {
+          const int which = e >= nb * kGC;
+          const int rem = e - which * nb * kGC;
+          int r, gl;
+          if (LAY == kLaySplit) { r = rem % nb; gl = rem / nb; }
+          else { gl = rem % kGC; r = rem / kGC; }
+          const int g = g0 + gl;
+          float2* d = (which ? yr : xr) + r * kRawPitch + gl;
+          if (g >= g_end) {
+            *d = make_float2(0.f, 0.f);
+          } else if (LAY == kLaySplit) {
             const size_t o = (sk * ng + g) * nb + r;
-            x = make_float2(reinterpret_cast<const float*>(X0)[o], reinterpret_cast<const float*>(X1)[o]);
-            y = make_float2(reinterpret_cast<const float*>(Y0)[o], reinterpret_cast<const float*>(Y1)[o]);
+            cp_async<4>(&d->x, reinterpret_cast<const float*>(which ? Y0 : X0) + o);
+            cp_async<4>(&d->y, reinterpret_cast<const float*>(which ? Y1 : X1) + o);
           } else {
-            x = reinterpret_cast<const float2*>(X0)[(sk * nb + r) * ng + g];
-            y = reinterpret_cast<const float2*>(Y0)[(sk * nb + r) * ng + g];
+            cp_async<8>(d, reinterpret_cast<const float2*>(which ? Y0 : X0) + (sk * nb + r) * ng + g);
           }
         }
-        xv[q] = x;
-        yv[q] = y;
       }
+      cp_async_commit();   // one group per chunk index, empty past the end
     };
-    load(0);
-    for (int c = 0; c < nchunk && !*abort_flag; ++c) {
-      const int s = c % kStages;
-      float2 xc[kMaxSlots], yc[kMaxSlots];
-#pragma unroll
-      for (int q = 0; q < kMaxSlots; ++q) { xc[q] = xv[q]; yc[q] = yv[q]; }
-      if (c + 1 < nchunk) load(c + 1);   // next chunk's loads in flight during this one
-      if (c >= kStages && !mbar_wait(empty(s), ((c / kStages) - 1) & 1)) { timed_out(); break; }
+    const int ncore = L.gb * kNKC * 16;    // (row, k pair) slots of an nb-row part
+    for (int c = 0; c < kRawDepth - 1; ++c) load_raw(c);
+    // Every producer runs all nchunk iterations and both named barriers of
+    // each (an abort only skips the work), so the barriers always complete.
+    for (int c = 0; c < nchunk; ++c) {
+      const int s = c % S;
+      prod_sync();                          // raw slot of chunk c - 1 has been converted
+      load_raw(c + kRawDepth - 1);
+      cp_async_wait<kRawDepth - 1>();
+      prod_sync();                          // chunk c is in shared memory for every producer
+      if (*abort_flag) continue;
+      if (c >= S && !mbar_wait(empty(s), ((c / S) - 1) & 1)) { timed_out(); continue; }
+      const float2* xr = raw_x(c % kRawDepth);
+      const float2* yr = xr + nb * kRawPitch;
       unsigned char* st = sm + s * L.stage;
-#pragma unroll
-      for (int q = 0; q < kMaxSlots; ++q) {
-        const int e = p + q * kNProd;
-        int r, gl;
-        slot_rg(e, r, gl);
-        if (e < ncore && r < nb) {
-          put(st + L.a_hi, st + L.a_lo, r, 2 * gl, xc[q].x, xc[q].y);
-          put(st + L.a_hi, st + L.a_lo, nb + r, 2 * gl, xc[q].y, -xc[q].x);
-          put(st + L.b_hi, st + L.b_lo, r, 2 * gl, yc[q].x, yc[q].y);
+      for (int e = p; e < ncore; e += kNProd) {
+        const int cm = e >> 4, w = e & 15;
+        const int rg = cm / kNKC, kc = cm - rg * kNKC;
+        const int r = rg * 8 + (w >> 1), gl = 2 * kc + (w & 1);
+        if (r < nb) {
+          const float2 x = xr[r * kRawPitch + gl];
+          const float2 y = yr[r * kRawPitch + gl];
+          put(st + L.a_hi, st + L.a_lo, r, 2 * gl, x.x, x.y);
+          put(st + L.a_hi, st + L.a_lo, nb + r, 2 * gl, x.y, -x.x);
+          put(st + L.b_hi, st + L.b_lo, r, 2 * gl, y.x, y.y);
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(full(s));
     }
+    cp_async_wait<0>();
   }
   __syncthreads();
   // every issued MMA has completed before the tensor memory is released
@@ -341,7 +364,7 @@ int launch_gram_tc5(int lay, const void* X0, const void* X1, const void* Y0, con
                     cudaStream_t st) {
   using namespace tc5;
   if (nb > 32 || nb < 1 || !err) return 0;
-  // one CTA per SM (about 140 KB of shared memory): about four waves
+  // one CTA per SM (150-220 KB of shared memory): about four waves
   nsplit = std::max(1, std::min(nsplit, (4 * 152 + nsk - 1) / nsk));
   const int split_len = (ng + nsplit - 1) / nsplit;
   const size_t sm = layout_for(nb).total;
