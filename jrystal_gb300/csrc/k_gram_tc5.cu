@@ -10,22 +10,22 @@
 // operand is split into TF32 hi and lo parts (cvt.rna), and the three MMAs
 // lo*hi + hi*lo + hi*hi keep FP32 accuracy.
 //
-// Warp-specialised pipeline of one CTA (one (s,k), one G range, 256
+// Warp-specialised pipeline of one CTA (one (s,k), one G range, 512
 // threads), coordinated by mbarriers only:
-//   producers (warps 1-3, 6-7): stream chunks of 32 G vectors of X and Y into
+//   producers (warps 1-3, 6-15): stream chunks of 32 G vectors of X and Y into
 //     a ring of raw shared-memory buffers with cp.async four chunks ahead
 //     (named barrier 1 among the producers only), split each chunk into TF32
 //     hi/lo parts in the no-swizzle K-major core-matrix layout of one of the
-//     MMA stages, and arrive on the stage's "full" barrier;
+//     MMA stages, and arrive (one lane per warp) on the stage's "full" barrier;
 //   MMA issuer (warp 0, one lane): waits "full", issues the chunk's 24 MMAs
 //     into one of two 32-column tensor-memory accumulators and commits them
 //     to the stage's "empty" barrier and the accumulator's "ready" barrier;
 //   epilogue (warps 4-5, tensor-memory lanes 0-63): waits "ready", adds the
 //     2nb accumulator rows (tcgen05.ld) into Kahan-compensated FP32 sums and
 //     arrives on the accumulator's "free" barrier.
-// Plain FP32 sums therefore never run over more than one chunk (64 real
-// terms x 3 products); across chunks the compensated sums keep the error at
-// the level of the CUDA-core Gram's FP64 reduction.  Every wait is bounded: on a timeout
+// Plain FP32 sums in tensor memory run over kFlush chunks (128 real terms x
+// 3 products); across those groups the compensated sums keep the error at the
+// level of the CUDA-core Gram's FP64 reduction.  Every wait is bounded: on a timeout
 // the waiting thread sets bit 2 of the workspace flag word and a shared
 // abort flag that ends every role's loop; the CTA then waits (bounded) for
 // its issued MMAs, frees its tensor memory and returns.
@@ -38,9 +38,10 @@ namespace tc5 {
 constexpr int kLaySplit = 0;             // parameters: re and im arrays [S][K][G][B]
 constexpr int kLayBand = 1;              // band-major complex [S*K*B][G]
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kKC = 64;                  // K floats per chunk (32 complex G vectors)
 constexpr int kGC = kKC / 2;             // G vectors per chunk
+static_assert(kGC == 32, "the producer index arithmetic assumes 32 G vectors per chunk");
 constexpr int kNKC = kKC / 4;            // core-matrix columns (16 bytes) per chunk
 constexpr int kCore = 128;               // bytes per core matrix: 8 rows x 16 bytes
 constexpr int kLBO = kCore;              // K-adjacent core matrices
@@ -53,9 +54,10 @@ constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kN 
 constexpr long kWaitLimit = 1L << 22;
 
 constexpr int kMaxStages = 3;
-constexpr int kNProd = 160;              // producer threads (warps 1, 2, 3, 6, 7)
+constexpr int kNProd = 416;              // producer threads (warps 1-3 and 6-15)
 constexpr int kRawDepth = 4;             // raw chunks in flight per CTA
 constexpr int kRawPitch = kGC + 1;       // complex elements per raw row (padded)
+constexpr int kFlush = 2;                // chunks accumulated per tensor-memory buffer
 
 struct Layout {
   int ga, gb;                      // 8-row groups holding A (2nb rows) and B (nb rows)
@@ -83,7 +85,7 @@ __host__ __device__ inline Layout layout_for(int nb) {
     // past the last stage stays inside the allocation (pad before the raw ring)
     L.raw = L.stages * L.stage + 16 * kSBO;
     L.bars = L.raw + kRawDepth * L.raw_stage;
-    L.total = L.bars + 128;
+    L.total = L.bars + 192;
     if (L.total <= 227 * 1024 || L.stages == 2) break;
     --L.stages;
   }
@@ -99,6 +101,15 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 __device__ __forceinline__ uint64_t mdesc(uint32_t addr) {
   return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(kLBO >> 4) << 16) |
          ((uint64_t)(kSBO >> 4) << 32) | (1ull << 46);
+}
+
+// cp.async of BYTES bytes, or BYTES zero bytes when !valid (source size 0)
+template <int BYTES>
+__device__ __forceinline__ void cp_async_zfill(void* smem, const void* gmem, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(sa), "l"(gmem), "n"(BYTES),
+               "r"(valid ? BYTES : 0)
+               : "memory");
 }
 
 __device__ __forceinline__ uint32_t tf32(float x) {
@@ -175,18 +186,19 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
   auto empty = [&](int s) { return bar_base + 8u * (kMaxStages + s); };
   auto ready = [&](int b) { return bar_base + 8u * (2 * kMaxStages + b); };
   auto freed = [&](int b) { return bar_base + 8u * (2 * kMaxStages + 2 + b); };
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + L.bars + 96);
-  int* issued = reinterpret_cast<int*>(sm + L.bars + 100);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + L.bars + 104);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + L.bars + 160);
+  int* issued = reinterpret_cast<int*>(sm + L.bars + 164);   // accumulator groups committed
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + L.bars + 168);
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
-      mbar_init(full(s), kNProd);
+      mbar_init(full(s), kNProd / 32);   // one arrival per producer warp
       mbar_init(empty(s), 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(ready(b), 1);
-      mbar_init(freed(b), 64);
+      mbar_init(freed(b), 2);            // one arrival per epilogue warp
     }
+
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     *abort_flag = 0;
     *issued = 0;
@@ -209,10 +221,13 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
   if (warp == 0) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
+      int open_grp = -1;   // group with MMAs issued but not yet committed to its ready barrier
       for (int c = 0; c < nchunk && !*abort_flag; ++c) {
-        const int s = c % S, b = c & 1;
+        const int s = c % S, grp = c / kFlush, b = grp & 1;
+        const bool first = (c % kFlush) == 0;
+        const bool last = (c % kFlush) == kFlush - 1 || c == nchunk - 1;
         if (!mbar_wait(full(s), (c / S) & 1)) { timed_out(); break; }
-        if (c >= 2 && !mbar_wait(freed(b), ((c - 2) >> 1) & 1)) { timed_out(); break; }
+        if (first && grp >= 2 && !mbar_wait(freed(b), ((grp - 2) >> 1) & 1)) { timed_out(); break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t base = smem_u32(sm + s * L.stage);
         const uint32_t d = tmem + (uint32_t)(b * 32);
@@ -221,13 +236,21 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
           const uint32_t ko = k * 2 * kCore;
           const uint64_t ah = mdesc(base + L.a_hi + ko), al = mdesc(base + L.a_lo + ko);
           const uint64_t bh = mdesc(base + L.b_hi + ko), bl = mdesc(base + L.b_lo + ko);
-          mma(d, al, bh, k == 0 ? 0u : 1u);
+          mma(d, al, bh, (first && k == 0) ? 0u : 1u);
           mma(d, ah, bl, 1u);
           mma(d, ah, bh, 1u);
         }
         commit(empty(s));
-        commit(ready(b));
-        *issued = c + 1;
+        open_grp = grp;
+        if (last) {
+          commit(ready(b));
+          *issued = grp + 1;
+          open_grp = -1;
+        }
+      }
+      if (open_grp >= 0) {   // after an abort: track the open group's MMAs too
+        commit(ready(open_grp & 1));
+        *issued = open_grp + 1;
       }
     }
     __syncwarp();
@@ -236,7 +259,8 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
     float sum[32], comp[32];
 #pragma unroll
     for (int j = 0; j < 32; ++j) { sum[j] = 0.f; comp[j] = 0.f; }
-    for (int c = 0; c < nchunk; ++c) {
+    const int ngroup = (nchunk + kFlush - 1) / kFlush;
+    for (int c = 0; c < ngroup; ++c) {
       const int b = c & 1;
       const bool ok = mbar_wait(ready(b), (c >> 1) & 1);
       if (!__all_sync(0xffffffffu, ok)) {   // warp-uniform exit before the warp-wide load
@@ -259,7 +283,8 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(freed(b));
+      __syncwarp();
+      if (lane == 0) mbar_arrive(freed(b));
 #pragma unroll
       for (int j = 0; j < 32; ++j) {   // Kahan: sum - comp is the running total
         const float y = __uint_as_float(v[j]) - comp[j];
@@ -289,22 +314,25 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
         float2* xr = raw_x(c % kRawDepth);
         float2* yr = xr + nb * kRawPitch;
         const int g0 = g_begin + c * kGC;
-        for (int e = p; e < 2 * nb * kGC; e += kNProd) {
-          const int which = e >= nb * kGC;
-          const int rem = e - which * nb * kGC;
+        // element e: X then Y, 32 rows (bands, padded) x 32 G vectors; rows past
+        // nb skipped, G vectors past the range zero-filled by the copy itself
+        for (int e = p; e < 2 * 32 * kGC; e += kNProd) {
+          const int which = e >> 10;
+          const int rem = e & 1023;
           int r, gl;
-          if (LAY == kLaySplit) { r = rem % nb; gl = rem / nb; }
-          else { gl = rem % kGC; r = rem / kGC; }
+          if (LAY == kLaySplit) { r = rem & 31; gl = rem >> 5; }   // consecutive bands: contiguous
+          else { gl = rem & 31; r = rem >> 5; }                     // consecutive G: contiguous
+          if (r >= nb) continue;
           const int g = g0 + gl;
+          const bool in = g < g_end;
           float2* d = (which ? yr : xr) + r * kRawPitch + gl;
-          if (g >= g_end) {
-            *d = make_float2(0.f, 0.f);
-          } else if (LAY == kLaySplit) {
-            const size_t o = (sk * ng + g) * nb + r;
-            cp_async<4>(&d->x, reinterpret_cast<const float*>(which ? Y0 : X0) + o);
-            cp_async<4>(&d->y, reinterpret_cast<const float*>(which ? Y1 : X1) + o);
+          if (LAY == kLaySplit) {
+            const size_t o = in ? (sk * ng + g) * nb + r : 0;
+            cp_async_zfill<4>(&d->x, reinterpret_cast<const float*>(which ? Y0 : X0) + o, in);
+            cp_async_zfill<4>(&d->y, reinterpret_cast<const float*>(which ? Y1 : X1) + o, in);
           } else {
-            cp_async<8>(d, reinterpret_cast<const float2*>(which ? Y0 : X0) + (sk * nb + r) * ng + g);
+            const size_t o = in ? (sk * nb + r) * ng + g : 0;
+            cp_async_zfill<8>(d, reinterpret_cast<const float2*>(which ? Y0 : X0) + o, in);
           }
         }
       }
@@ -320,8 +348,15 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
       load_raw(c + kRawDepth - 1);
       cp_async_wait<kRawDepth - 1>();
       prod_sync();                          // chunk c is in shared memory for every producer
-      if (*abort_flag) continue;
-      if (c >= S && !mbar_wait(empty(s), ((c / S) - 1) & 1)) { timed_out(); continue; }
+      // warp-uniform decision: every lane polls, the warp acts together (the
+      // per-warp arrival below needs all 32 lanes)
+      const bool aborted = *abort_flag != 0;
+      bool go = !aborted && (c < S || mbar_wait(empty(s), ((c / S) - 1) & 1));
+      go = __all_sync(0xffffffffu, go);
+      if (!go) {
+        if (lane == 0 && !aborted) timed_out();
+        continue;
+      }
       const float2* xr = raw_x(c % kRawDepth);
       const float2* yr = xr + nb * kRawPitch;
       unsigned char* st = sm + s * L.stage;
@@ -338,7 +373,8 @@ k_gram_tc5(const void* __restrict__ X0, const void* __restrict__ X1, const void*
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(full(s));
+      __syncwarp();
+      if (lane == 0) mbar_arrive(full(s));
     }
     cp_async_wait<0>();
   }
