@@ -249,6 +249,17 @@ int jrg_fast_paths(int enable);
  * setting.  Process-wide; no reference counterpart. */
 int jrg_tensor_core_paths(int enable);
 
+/* Two-way k-point pipeline of jrg_energy_grad (enable = 1, the default):
+ * with at least two (s,k) blocks, num_band <= 32, the default contraction
+ * and slab kernels and no phase profiling, the blocks are split in two
+ * halves that run on the caller's stream and a second stream owned by the
+ * plan (joined back before the call returns, in stream order), so that the
+ * latency-bound small kernels of one half overlap the other half's
+ * bandwidth-bound kernels.  enable = 0 runs everything on the caller's
+ * stream; < 0 only queries.  Returns the previous setting.  Process-wide; no
+ * reference counterpart. */
+int jrg_pipeline(int enable);
+
 /* Per-phase CUDA-event timing of jrg_energy_grad (no reference counterpart;
  * the reference only times whole steps, calc driver :207-211).  enable
  * creates events for up to max_calls calls (0 disables); read synchronises

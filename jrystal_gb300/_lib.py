@@ -52,6 +52,7 @@ _SIGS = {
   "jrg_density": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
   "jrg_energy_grad": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
   "jrg_band_trace_grad": ([_vp] * 11, ct.c_int),
+  "jrg_pipeline": ([ct.c_int], ct.c_int),
   "jrg_energy_grad_bands": ([_vp] * 10, ct.c_int),
   "jrg_energy_grad_adam": ([_vp, _vp, _vp, _vp, _vp, ct.POINTER(AdamStep), _vp, _vp, _vp, _vp],
                            ct.c_int),

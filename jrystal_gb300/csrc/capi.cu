@@ -36,6 +36,8 @@ template <typename R> int launch_kinetic(const void*, const double*, const doubl
 int launch_precond_scale(const float*, const void*, const double*, const double*, const double*, int, int, int, long long, float, float, float*, cudaStream_t);
 int launch_sum_slots(const double*, const int*, double*, int, const int*, cudaStream_t);
 int launch_band_trace_sums(const double2*, int, int, const double*, int, double*, cudaStream_t);
+int launch_kin_reduce(int, const void*, int, int, int, const double*, double*, double*, cudaStream_t);
+template <typename R> int launch_rotate_kinetic(const void*, const void*, const double2*, void*, int, int, int, const double*, int, void*, cudaStream_t, int = 0);
 template <typename R> int launch_mul_ig(const void*, const double*, void*, int, long long, double, cudaStream_t);
 template <typename R> int launch_gga_local(const void*, void*, void*, void*, void*, double*, int, long long, int, double, int, cudaStream_t);
 template <typename R> int launch_div_g(void*, const void*, const void*, const double*, long long, double, cudaStream_t);
@@ -122,6 +124,7 @@ static void layout_workspace(jrg_plan* P) {
   w.dinv = take(nbt * sizeof(double));
   w.rot_scratch = take(nsk * 2 * 128 * 64 * sizeof(uint32_t));   // split B of the TF32 rotations
   w.gga = (P->xc & kXcGga) ? take(3 * (size_t)P->ngrid * C) : 0;   // gradient / flux grids of PBE
+  w.kin_part = take(nbt * (size_t)((P->ng + 255) / 256) * Rz);   // kinetic block partials
   w.total = o;
 }
 
@@ -145,6 +148,9 @@ int jrg_plan_destroy(jrg_plan* P) {
   if (P->d_cell) cudaFree(P->d_cell);
   if (P->d_atoms) cudaFree(P->d_atoms);
   if (P->d_ones) cudaFree(P->d_ones);
+  if (P->fork_ev) cudaEventDestroy(P->fork_ev);
+  if (P->join_ev) cudaEventDestroy(P->join_ev);
+  if (P->side) cudaStreamDestroy(P->side);
   if (P->prof) {
     for (cudaEvent_t e : P->prof->ev) cudaEventDestroy(e);
     delete P->prof;
@@ -319,6 +325,12 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
     rc = up((void**)&P->d_ones, ones.data(), ones.size() * sizeof(double));
   }
   if (!rc) {
+    cudaError_t e = cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&P->join_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) rc = cuda_fail(e, "stream/event creation");
+  }
+  if (!rc) {
     cudaError_t e = cudaMalloc((void**)&P->d.gvec, 3 * P->ngrid * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void**)&P->d.ginv, P->ngrid * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&P->d.vext, P->ngrid * csize(P->prec));
@@ -386,7 +398,8 @@ static void profile_call_done(const jrg_plan* P) {
 
 template <typename R>
 static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im, void* ws,
-                          cudaStream_t st, int out_kind = kRotBand, void* out = nullptr) {
+                          cudaStream_t st, int out_kind = kRotBand, void* out = nullptr,
+                          int* kin_blocks = nullptr) {
   const Workspace& w = P->ws;
   const int nsk = P->ns * P->nk;
   int rc;
@@ -405,6 +418,13 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
       return rc;
   }
   PHASE(PH_ROTATE);
+  if (kin_blocks) {
+    // C and the kinetic block partials in one pass over the parameters
+    *kin_blocks = launch_rotate_kinetic<R>(w_re, w_im, (double2*)wsp(ws, w.rinv), wsp(ws, w.c), nsk,
+                                           P->ng, P->nb, P->d.tk, P->nk, wsp(ws, w.kin_part), st);
+    if (*kin_blocks < 0) return -*kin_blocks;
+    if (*kin_blocks > 0) return JRG_OK;
+  }
   return launch_rotate<R>(out_kind, kSplit, w_re, w_im, (double2*)wsp(ws, w.rinv), nullptr, nullptr,
                           out ? out : wsp(ws, w.c), nullptr, nsk, P->ng, P->nb, 1.0,
                           wsp(ws, w.rot_scratch), st);
@@ -489,13 +509,18 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
   const double N = (double)P->ngrid;
   int rc;
   JRG_CUDA(cudaMemsetAsync(wsp(ws, w.flags), 0, 64, st));
-  if ((rc = orthonormalise<R>(P, w_re, w_im, ws, st))) return rc;
+  int kin_blocks = 0;
+  if ((rc = orthonormalise<R>(P, w_re, w_im, ws, st, kRotBand, nullptr, &kin_blocks))) return rc;
   double* slots = (double*)wsp(ws, w.epart);
   {
     PHASE(PH_KINETIC);
-    if ((rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, occ, slots, (double*)wsp(ws, w.ekin), nbt,
-                                P->ng, P->nb, P->nk, st)))
-      return rc;
+    if (kin_blocks > 0)
+      rc = launch_kin_reduce(P->prec, wsp(ws, w.kin_part), kin_blocks, P->nb, nbt, occ, slots,
+                             (double*)wsp(ws, w.ekin), st);
+    else
+      rc = launch_kinetic<R>(wsp(ws, w.c), P->d.tk, occ, slots, (double*)wsp(ws, w.ekin), nbt,
+                             P->ng, P->nb, P->nk, st);
+    if (rc) return rc;
   }
   if (adam && adam->mlp_w32) {
     // learned update scales from this step's band kinetic energies
@@ -636,10 +661,155 @@ static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im
                           g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st);
 }
 
+// Two-way k-point pipeline of the energy/gradient evaluation: the (s,k)
+// blocks are split in two halves that run on the caller's stream and the
+// plan's side stream, so that the latency-bound small kernels of one half
+// (Cholesky, small adjoint matrices) overlap the bandwidth-bound kernels of
+// the other.  The density reduction and the grid terms run once, on the
+// caller's stream, between the two forks.
+template <typename R>
+static int phase_forward_range(const jrg_plan* P, const void* w_re, const void* w_im,
+                               const double* occ, void* ws, int k0, int n, cudaStream_t st) {
+  using C = C_t<R>;
+  const Workspace& w = P->ws;
+  const size_t nb2 = (size_t)P->nb * P->nb;
+  const size_t po = (size_t)k0 * P->ng * P->nb;                         // parameter offset
+  const size_t co = (size_t)k0 * P->nb * P->ng;                         // band-major offset
+  const size_t to = (size_t)k0 * P->nb * P->nact * P->ny * P->nz;       // plane buffer offset
+  const int nblk = (P->ng + 255) / 256;
+  const R* wr = reinterpret_cast<const R*>(w_re) + po;
+  const R* wi = reinterpret_cast<const R*>(w_im) + po;
+  int* flags = (int*)wsp(ws, w.flags);
+  int rc;
+  if ((rc = launch_gram<R>(kSplit, wr, wi, kSplit, wr, wi,
+                           (double2*)wsp(ws, w.gram_part) + (size_t)k0 * w.gram_splits * nb2,
+                           (double2*)wsp(ws, w.gram) + k0 * nb2, n, P->ng, P->nb, w.gram_splits, st,
+                           flags)))
+    return rc;
+  if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram) + k0 * nb2, (double2*)wsp(ws, w.rmat) + k0 * nb2,
+                                (double2*)wsp(ws, w.rinv) + k0 * nb2, n, P->nb, flags,
+                                (double*)wsp(ws, w.dinv) + (size_t)k0 * P->nb, st)))
+    return rc;
+  const int kb = launch_rotate_kinetic<R>(wr, wi, (double2*)wsp(ws, w.rinv) + k0 * nb2,
+                                          (C*)wsp(ws, w.c) + co, n, P->ng, P->nb, P->d.tk, P->nk,
+                                          (R*)wsp(ws, w.kin_part) + (size_t)k0 * nblk * P->nb, st, k0);
+  if (kb < 0) return -kb;
+  if (kb == 0) return fail(JRG_ERR_UNSUPPORTED, "pipelined path needs the fused kinetic rotation");
+  if ((rc = launch_plane_inv_sphere<R>(P, (C*)wsp(ws, w.c) + co, (C*)wsp(ws, w.t) + to, n * P->nb, st)))
+    return rc;
+  return launch_line_density<R>(P, (C*)wsp(ws, w.t) + to, (R*)wsp(ws, w.rho_part) + (size_t)k0 * P->ngrid,
+                                occ, 1.0 / P->vol, k0 * P->nb, n * P->nb, P->nb, st);
+}
+
+template <typename R>
+static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re, void* g_im, void* ws,
+                               int k0, int n, cudaStream_t st) {
+  using C = C_t<R>;
+  const Workspace& w = P->ws;
+  const int nsk = P->ns * P->nk;
+  const size_t nb2 = (size_t)P->nb * P->nb;
+  const size_t po = (size_t)k0 * P->ng * P->nb;
+  const size_t co = (size_t)k0 * P->nb * P->ng;
+  const size_t to = (size_t)k0 * P->nb * P->nact * P->ny * P->nz;
+  const double N = (double)P->ngrid;
+  C* t = (C*)wsp(ws, w.t) + to;
+  C* c = (C*)wsp(ws, w.c) + co;
+  C* gc = (C*)wsp(ws, w.gc) + co;
+  int rc;
+  if ((rc = launch_line_apply_v<R>(P, t, t, wsp(ws, w.vr), n * P->nb, P->nb, st))) return rc;
+  if ((rc = launch_plane_fwd_sphere<R>(P, t, c, gc, occ, k0 * P->nb, n * P->nb, 1.0 / N, st))) return rc;
+  if ((rc = launch_gram<R>(kBand, c, nullptr, kBand, gc, nullptr,
+                           (double2*)wsp(ws, w.adj_part) + (size_t)k0 * w.gram_splits * nb2,
+                           (double2*)wsp(ws, w.adj) + k0 * nb2, n, P->ng, P->nb, w.gram_splits, st,
+                           (int*)wsp(ws, w.flags))))
+    return rc;
+  double2* rh = (double2*)wsp(ws, w.kmat);
+  double2* negm2 = rh + (size_t)nsk * nb2;
+  if ((rc = launch_adjoint_small((double2*)wsp(ws, w.adj) + k0 * nb2, (double2*)wsp(ws, w.rinv) + k0 * nb2,
+                                 rh + k0 * nb2, negm2 + k0 * nb2, n, P->nb, st)))
+    return rc;
+  return launch_rotate<R>(kRotGSplit, kBand, gc, nullptr, rh + k0 * nb2, c, negm2 + k0 * nb2,
+                          reinterpret_cast<R*>(g_re) + po, reinterpret_cast<R*>(g_im) + po, n, P->ng,
+                          P->nb, 2.0, wsp(ws, w.rot_scratch), st);
+}
+
+static bool g_pipeline = true;   // two-way k-point pipeline of jrg_energy_grad
+
+static bool pipeline_ok(const jrg_plan* P) {
+  return P->ns * P->nk >= 2 && P->nb <= 32 && jrg_tensor_core_paths(-1) == 0 &&
+         jrg_fast_paths(-1) == 1 && !(P->prof && P->prof->max_calls > 0);
+}
+
+template <typename R>
+static int energy_grad_pipelined(const jrg_plan* P, const void* w_re, const void* w_im,
+                                 const double* occ, double* energies, void* g_re, void* g_im,
+                                 void* ws, cudaStream_t st) {
+  using C = C_t<R>;
+  const Workspace& w = P->ws;
+  const int nsk = P->ns * P->nk;
+  const int nbt = nsk * P->nb;
+  const int ka = (nsk + 1) / 2, kb = nsk - ka;
+  const double N = (double)P->ngrid;
+  int rc;
+  auto fork = [&]() -> int {
+    JRG_CUDA(cudaEventRecord(P->fork_ev, st));
+    JRG_CUDA(cudaStreamWaitEvent(P->side, P->fork_ev, 0));
+    return JRG_OK;
+  };
+  auto join = [&]() -> int {
+    JRG_CUDA(cudaEventRecord(P->join_ev, P->side));
+    JRG_CUDA(cudaStreamWaitEvent(st, P->join_ev, 0));
+    return JRG_OK;
+  };
+  JRG_CUDA(cudaMemsetAsync(wsp(ws, w.flags), 0, 64, st));
+  if ((rc = fork())) return rc;
+  if ((rc = phase_forward_range<R>(P, w_re, w_im, occ, ws, 0, ka, st))) return rc;
+  if ((rc = phase_forward_range<R>(P, w_re, w_im, occ, ws, ka, kb, P->side))) return rc;
+  if ((rc = join())) return rc;
+  double* slots = (double*)wsp(ws, w.epart);
+  if ((rc = launch_kin_reduce(P->prec, wsp(ws, w.kin_part), (P->ng + 255) / 256, P->nb, nbt, occ, slots,
+                              (double*)wsp(ws, w.ekin), st)))
+    return rc;
+  void* rho = wsp(ws, w.rho);
+  if ((rc = launch_reduce_density<R>(wsp(ws, w.rho_part), rho, P->nk, P->ns, P->ngrid, st))) return rc;
+  {
+    C* rhog = (C*)wsp(ws, w.rhog);
+    C* scratch = (C*)wsp(ws, w.fft_scratch);
+    const C* tw = (const C*)P->d.tw;
+    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+    const bool gga = (P->xc & kXcGga) != 0;
+    if (gga && (rc = gga_gradients<R>(P, rhog, ws, st))) return rc;
+    const double pref = P->vol / (N * N);
+    if ((rc = launch_recip_terms<R>(rhog, P->d.ginv, P->d.vext, rhog, slots + nbt + kRecipBlocks,
+                                    slots + nbt, kRecipBlocks, P->ngrid, pref, st)))
+      return rc;
+    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st)))
+      return rc;
+    if (gga) {
+      if ((rc = gga_potential<R>(P, rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks, 0,
+                                 ws, st)))
+        return rc;
+    } else if ((rc = launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks,
+                                         kXcBlocks, P->ngrid, P->xc, P->vol / N, st))) {
+      return rc;
+    }
+    if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st)))
+      return rc;
+  }
+  if (!g_re && !g_im) return JRG_OK;
+  if (!g_re || !g_im) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
+  if ((rc = fork())) return rc;
+  if ((rc = phase_adjoint_range<R>(P, occ, g_re, g_im, ws, 0, ka, st))) return rc;
+  if ((rc = phase_adjoint_range<R>(P, occ, g_re, g_im, ws, ka, kb, P->side))) return rc;
+  return join();
+}
+
 template <typename R>
 static int energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const double* occ,
                        double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
-  const int rc = energy_grad_impl<R>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st);
+  const int rc = pipeline_ok(P) && g_pipeline
+                     ? energy_grad_pipelined<R>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st)
+                     : energy_grad_impl<R>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st);
   profile_call_done(P);
   return rc;
 }
@@ -723,6 +893,12 @@ int jrg_energy_grad_bands(const jrg_plan* P, const void* w_re, const void* w_im,
                : energy_grad_impl<float>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st, nullptr, band_energies);
   profile_call_done(P);
   return rc;
+}
+
+int jrg_pipeline(int enable) {
+  const int prev = jrg::g_pipeline ? 1 : 0;
+  if (enable >= 0) jrg::g_pipeline = enable != 0;
+  return prev;
 }
 
 int jrg_band_trace_grad(const jrg_plan* P, const void* w_re, const void* w_im, const void* v_eff,

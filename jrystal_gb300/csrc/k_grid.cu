@@ -340,6 +340,27 @@ __global__ void __launch_bounds__(256) k_kinetic(const C_t<R>* __restrict__ coef
   }
 }
 
+// per band: FP64 sum of the kinetic block partials (precision R) of the
+// forward rotation -> ekin[band], slot[band] = occ[band] * ekin[band]
+template <typename R>
+__global__ void k_kin_reduce(const R* __restrict__ part, int nblk, int nb, int nbt,
+                             const double* __restrict__ occ, double* __restrict__ slot,
+                             double* __restrict__ ekin) {
+  // one warp per band: lanes take every 32nd block partial, then a shuffle sum
+  const int band = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (band >= nbt) return;
+  const int sk = band / nb, b = band - sk * nb;
+  const R* p = part + (size_t)sk * nblk * nb + b;
+  double acc = 0.0;
+  for (int i = lane; i < nblk; i += 32) acc += (double)p[(size_t)i * nb];
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if (lane == 0) {
+    slot[band] = acc * occ[band];
+    if (ekin) ekin[band] = acc;
+  }
+}
+
 // energies[t] = sum of its slots, t = 0..3; energies[4] = total
 __global__ void k_sum_slots(const double* __restrict__ slots, const int* __restrict__ slot_begin,
                             double* __restrict__ energies, int nterms, const int* __restrict__ flags) {
@@ -665,6 +686,18 @@ int launch_potential_gga(const void* vri, double vscale, void* vr, const void* d
                                                   reinterpret_cast<R*>(vr),
                                                   reinterpret_cast<const C_t<R>*>(div), n);
   JRG_LAUNCH_CHECK("k_potential_gga");
+  return JRG_OK;
+}
+
+int launch_kin_reduce(int prec, const void* part, int nblk, int nb, int nbt, const double* occ,
+                      double* slot, double* ekin, cudaStream_t st) {
+  if (prec == 64)
+    k_kin_reduce<double><<<(nbt * 32 + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double*>(part), nblk,
+                                                            nb, nbt, occ, slot, ekin);
+  else
+    k_kin_reduce<float><<<(nbt * 32 + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float*>(part), nblk, nb,
+                                                           nbt, occ, slot, ekin);
+  JRG_LAUNCH_CHECK("k_kin_reduce");
   return JRG_OK;
 }
 

@@ -596,7 +596,8 @@ template <typename R, int LX0, int OUT, int NBP>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
 k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const double2* __restrict__ M0,
             const void* __restrict__ X1, const double2* __restrict__ M1, void* out0, void* out1,
-            int ng, int nb, R fac, AdamArgs adam) {
+            int ng, int nb, R fac, AdamArgs adam, const double* __restrict__ tk, int nk,
+            void* __restrict__ kin_part, int sk0) {
   using C = C_t<R>;
   constexpr int KC = kRbKC, GT = kRbGT, TG = 4, TJ = NBP / 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -713,6 +714,36 @@ k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const do
         const int j = wj * TJ + b;
         if (g < ng && j < nb) o[(size_t)j * ng + g] = acc[a][b];
       }
+    }
+    if (kin_part) {
+      // kinetic partials of this block: sum over its G vectors of
+      // |G+k|^2/2 |c_j(G)|^2 per band j, in precision R (the blocks are
+      // summed in FP64)
+      const double* tkk = tk + ((sk0 + sk) % nk) * (size_t)ng;
+      R kp[TJ];
+#pragma unroll
+      for (int b = 0; b < TJ; ++b) kp[b] = (R)0;
+#pragma unroll
+      for (int a = 0; a < TG; ++a) {
+        const int g = g0 + wg * 128 + (a / 2) * 64 + 2 * lane + (a % 2);
+        const R tg = g < ng ? (R)tkk[g] : (R)0;
+#pragma unroll
+        for (int b = 0; b < TJ; ++b)
+          kp[b] += tg * (acc[a][b].x * acc[a][b].x + acc[a][b].y * acc[a][b].y);
+      }
+#pragma unroll
+      for (int b = 0; b < TJ; ++b)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) kp[b] += __shfl_xor_sync(0xffffffffu, kp[b], off);
+      R* red = reinterpret_cast<R*>(xs);   // [2][NBP], the staging ring is free now
+      if (lane == 0) {
+#pragma unroll
+        for (int b = 0; b < TJ; ++b) red[wg * NBP + wj * TJ + b] = kp[b];
+      }
+      __syncthreads();
+      if (t < nb)
+        reinterpret_cast<R*>(kin_part)[((size_t)sk * gridDim.x + blockIdx.x) * nb + t] =
+            red[t] + red[NBP + t];
     }
   } else if constexpr (OUT == ROT_GMAJOR_SPLIT) {
     // (S,K,G,B) split real/imag times fac, one part at a time through shared
@@ -980,7 +1011,8 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate_rb)");
       }
       kern<<<dim3((ng + kRbGT - 1) / kRbGT, nsk), 256, sm, st>>>(X0a, X0b, M0, X1, M1, out0, out1, ng,
-                                                                 nb, (R)fac, AdamArgs{});
+                                                                 nb, (R)fac, AdamArgs{}, nullptr, 1,
+                                                                 nullptr, 0);
       JRG_LAUNCH_CHECK("k_rotate_rb");
       return JRG_OK;
     };
@@ -1006,6 +1038,34 @@ int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const
   return rotate_out<R, ROT_GMAJOR_SPLIT>(lx0, X0a, X0b, M0, LAYOUT_BAND, X1, nullptr, M1, out0, out1, nsk, ng, nb, fac, st);
 }
 
+// C = W R^{-1} (parameter layout in, band-major out) with the kinetic
+// partials of each block written to kin_part [nsk][nblk][nb] (precision R); returns the
+// block count per (s,k) (> 0), 0 when not applicable, or -error.
+template <typename R>
+int launch_rotate_kinetic(const void* Wre, const void* Wim, const double2* Ri, void* C, int nsk,
+                          int ng, int nb, const double* tk, int nk, void* kin_part,
+                          cudaStream_t st, int sk0) {
+  if (nb > 32 || !g_rotate_rb || (sizeof(R) == 4 && g_tc_mode == 1)) return 0;
+  auto go = [&](auto kern, int nbp) -> int {
+    const size_t sm = rotate_rb_smem<R>(nb, nbp);
+    if (sm > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return -cuda_fail(e, "cudaFuncSetAttribute(rotate_rb kinetic)");
+    }
+    const int nblk = (ng + kRbGT - 1) / kRbGT;
+    kern<<<dim3(nblk, nsk), 256, sm, st>>>(Wre, Wim, Ri, nullptr, nullptr, C, nullptr, ng, nb,
+                                           (R)1.0, AdamArgs{}, tk, nk, kin_part, sk0);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return -cuda_fail(e, "k_rotate_rb(kinetic)");
+    return nblk;
+  };
+  if (nb <= 8) return go(k_rotate_rb<R, LAYOUT_SPLIT, ROT_BANDMAJOR, 8>, 8);
+  if (nb <= 16) return go(k_rotate_rb<R, LAYOUT_SPLIT, ROT_BANDMAJOR, 16>, 16);
+  if (nb <= 24) return go(k_rotate_rb<R, LAYOUT_SPLIT, ROT_BANDMAJOR, 24>, 24);
+  return go(k_rotate_rb<R, LAYOUT_SPLIT, ROT_BANDMAJOR, 32>, 32);
+}
+
 template <typename R>
 int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const double2* M1,
                        const AdamArgs& a, int nsk, int ng, int nb, double fac, cudaStream_t st) {
@@ -1017,7 +1077,8 @@ int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const 
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(rotate_rb adam)");
     }
     kern<<<dim3((ng + kRbGT - 1) / kRbGT, nsk), 256, sm, st>>>(X0, nullptr, M0, X1, M1, nullptr,
-                                                               nullptr, ng, nb, (R)fac, a);
+                                                               nullptr, ng, nb, (R)fac, a, nullptr, 1,
+                                                               nullptr, 0);
     JRG_LAUNCH_CHECK("k_rotate_rb(adam)");
     return JRG_OK;
   };
@@ -1028,6 +1089,8 @@ int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const 
 }
 
 #define JRG_INST_ORTH(R)                                                                        \
+  template int launch_rotate_kinetic<R>(const void*, const void*, const double2*, void*, int, int,  \
+                                        int, const double*, int, void*, cudaStream_t, int);     \
   template int launch_rotate_adam<R>(const void*, const double2*, const void*, const double2*,    \
                                      const AdamArgs&, int, int, int, double, cudaStream_t);       \
   template int launch_pack_params<R>(const void*, const void*, void*, int, int, int, bool,         \

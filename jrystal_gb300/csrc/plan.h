@@ -76,7 +76,7 @@ struct AdamArgs {
 // Workspace offsets (bytes) of one plan.
 struct Workspace {
   size_t wc, c, gram_part, gram, rmat, rinv, t, u, rho_part, rho, rhog, fft_scratch, vr,
-      gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, total;
+      gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, kin_part, total;
   int gram_splits;
   int ngroups;    // density partial groups
   int nepart;     // energy partial slots
@@ -102,5 +102,7 @@ struct jrg_plan {
   double* d_cell = nullptr;   // cell (9) then reciprocal vectors (9)
   double* d_atoms = nullptr;  // positions [natom][3] then charges [natom]
   double* d_ones = nullptr;   // [S*K*B] ones: unweighted band weights
+  cudaStream_t side = nullptr;   // second stream of the two-way k-point pipeline
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   jrg::Profiler* prof = nullptr;
 };

@@ -213,3 +213,42 @@ def test_tensor_core_and_cuda_core_contractions_agree(nb, nocc, grid, kgrid):
     for i, name in enumerate(["kinetic", "external", "hartree", "xc", "total"]):
       assert abs(e[i] - terms[name]) <= tol["e_rel"] * max(1.0, abs(terms[name])), (tc, name)
     assert max(np.abs(g1 - gr).max(), np.abs(g2 - gi).max()) <= tol["g_rel"] * scale, tc
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("case", [dict(kind="si2", grid=(16, 16, 16), kgrid=(2, 2, 2), nb=8, nocc=4),
+                                  dict(kind="si8", grid=(24, 24, 24), kgrid=(3, 1, 1), nb=12, nocc=8),
+                                  dict(kind="si2", grid=(27, 27, 27), kgrid=(1, 1, 2), nb=5, nocc=3)])
+def test_two_stream_pipeline_matches_serial_and_oracle(prec, case):
+  """jrg_pipeline(1) splits the k-points over two streams; results equal the
+  single-stream path to summation order and the oracle to the usual tolerance."""
+  torch = _torch()
+  from jrystal_gb300 import _lib
+  lib = _lib.load()
+  sysm = make_system(**case)
+  wr, wi = random_params(sysm, seed=41)
+  terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+  plan = _plan(sysm, prec)
+  dt = torch.float64 if prec == 64 else torch.float32
+  twr = torch.tensor(wr, dtype=dt, device="cuda")
+  twi = torch.tensor(wi, dtype=dt, device="cuda")
+  out = {}
+  prev = lib.jrg_pipeline(-1)
+  try:
+    for pipe in (1, 0):
+      lib.jrg_pipeline(pipe)
+      e, g1, g2 = plan.energy_and_grad(twr, twi, sysm.occupation)
+      out[pipe] = (e.cpu().numpy().copy(), g1.cpu().numpy(), g2.cpu().numpy())
+  finally:
+    lib.jrg_pipeline(prev)
+  tol = TOL[prec]
+  scale = max(np.abs(gr).max(), np.abs(gi).max())
+  for pipe in (1, 0):
+    e, g1, g2 = out[pipe]
+    assert e[6] == 0.0
+    for i, name in enumerate(["kinetic", "external", "hartree", "xc", "total"]):
+      assert abs(e[i] - terms[name]) <= tol["e_rel"] * max(1.0, abs(terms[name])), (pipe, name)
+    assert max(np.abs(g1 - gr).max(), np.abs(g2 - gi).max()) <= tol["g_rel"] * scale, pipe
+  same = 1e-12 if prec == 64 else 1e-5
+  np.testing.assert_allclose(out[1][0][:5], out[0][0][:5], rtol=same)
+  assert np.abs(out[1][1] - out[0][1]).max() <= same * scale
