@@ -701,9 +701,12 @@ static int phase_forward_range(const jrg_plan* P, const void* w_re, const void* 
                                 occ, 1.0 / P->vol, k0 * P->nb, n * P->nb, P->nb, st);
 }
 
+// With adam given, the gradient of the half goes to adam->grad (when set) or
+// into the half's own, now dead, plane-buffer range, and the half's
+// parameters take their Adam step right there, in the half's stream.
 template <typename R>
 static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re, void* g_im, void* ws,
-                               int k0, int n, cudaStream_t st) {
+                               int k0, int n, cudaStream_t st, const AdamArgs* adam = nullptr) {
   using C = C_t<R>;
   const Workspace& w = P->ws;
   const int nsk = P->ns * P->nk;
@@ -728,9 +731,24 @@ static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re,
   if ((rc = launch_adjoint_small((double2*)wsp(ws, w.adj) + k0 * nb2, (double2*)wsp(ws, w.rinv) + k0 * nb2,
                                  rh + k0 * nb2, negm2 + k0 * nb2, n, P->nb, st)))
     return rc;
-  return launch_rotate<R>(kRotGSplit, kBand, gc, nullptr, rh + k0 * nb2, c, negm2 + k0 * nb2,
-                          reinterpret_cast<R*>(g_re) + po, reinterpret_cast<R*>(g_im) + po, n, P->ng,
-                          P->nb, 2.0, wsp(ws, w.rot_scratch), st);
+  const size_t cnt = (size_t)n * P->ng * P->nb;
+  R* gr = adam ? (adam->grad[0] ? reinterpret_cast<R*>(adam->grad[0]) + po : reinterpret_cast<R*>(t))
+               : reinterpret_cast<R*>(g_re) + po;
+  R* gi = adam ? (adam->grad[1] ? reinterpret_cast<R*>(adam->grad[1]) + po : reinterpret_cast<R*>(t) + cnt)
+               : reinterpret_cast<R*>(g_im) + po;
+  if ((rc = launch_rotate<R>(kRotGSplit, kBand, gc, nullptr, rh + k0 * nb2, c, negm2 + k0 * nb2, gr, gi,
+                             n, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st)))
+    return rc;
+  if (!adam) return JRG_OK;
+  for (int part = 0; part < 2; ++part) {
+    const float* sc = adam->scale[part] ? adam->scale[part] + po : nullptr;
+    if ((rc = launch_adam<R>(reinterpret_cast<R*>(adam->p[part]) + po, part ? gi : gr,
+                             reinterpret_cast<R*>(adam->m[part]) + po,
+                             reinterpret_cast<R*>(adam->v[part]) + po, sc, (long long)cnt, adam->lr,
+                             adam->b1, adam->b2, adam->c1, adam->c2, adam->eps, st)))
+      return rc;
+  }
+  return JRG_OK;
 }
 
 static bool g_pipeline = true;   // two-way k-point pipeline of jrg_energy_grad
@@ -743,7 +761,7 @@ static bool pipeline_ok(const jrg_plan* P) {
 template <typename R>
 static int energy_grad_pipelined(const jrg_plan* P, const void* w_re, const void* w_im,
                                  const double* occ, double* energies, void* g_re, void* g_im,
-                                 void* ws, cudaStream_t st) {
+                                 void* ws, cudaStream_t st, const AdamArgs* adam = nullptr) {
   using C = C_t<R>;
   const Workspace& w = P->ws;
   const int nsk = P->ns * P->nk;
@@ -769,6 +787,11 @@ static int energy_grad_pipelined(const jrg_plan* P, const void* w_re, const void
   double* slots = (double*)wsp(ws, w.epart);
   if ((rc = launch_kin_reduce(P->prec, wsp(ws, w.kin_part), (P->ng + 255) / 256, P->nb, nbt, occ, slots,
                               (double*)wsp(ws, w.ekin), st)))
+    return rc;
+  if (adam && adam->mlp_w32 &&
+      (rc = launch_precond_scale(adam->mlp_w32, adam->mlp_wb, P->d.tk, (const double*)wsp(ws, w.ekin), occ,
+                                 P->nk, P->ng, P->nb, (long long)nbt * P->ng, adam->t_frac, adam->smax,
+                                 adam->scale[0], st)))
     return rc;
   void* rho = wsp(ws, w.rho);
   if ((rc = launch_reduce_density<R>(wsp(ws, w.rho_part), rho, P->nk, P->ns, P->ngrid, st))) return rc;
@@ -796,11 +819,11 @@ static int energy_grad_pipelined(const jrg_plan* P, const void* w_re, const void
     if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st)))
       return rc;
   }
-  if (!g_re && !g_im) return JRG_OK;
-  if (!g_re || !g_im) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
+  if (!adam && !g_re && !g_im) return JRG_OK;
+  if (!adam && (!g_re || !g_im)) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
   if ((rc = fork())) return rc;
-  if ((rc = phase_adjoint_range<R>(P, occ, g_re, g_im, ws, 0, ka, st))) return rc;
-  if ((rc = phase_adjoint_range<R>(P, occ, g_re, g_im, ws, ka, kb, P->side))) return rc;
+  if ((rc = phase_adjoint_range<R>(P, occ, g_re, g_im, ws, 0, ka, st, adam))) return rc;
+  if ((rc = phase_adjoint_range<R>(P, occ, g_re, g_im, ws, ka, kb, P->side, adam))) return rc;
   return join();
 }
 
@@ -936,8 +959,13 @@ int jrg_energy_grad_adam(const jrg_plan* P, void* params, void* m, void* v, cons
   a.c2 = 1.0 - std::pow(opt->b2, opt->step);
   a.mlp_w32 = opt->mlp_w32; a.mlp_wb = opt->mlp_wb;
   a.t_frac = opt->t_frac; a.smax = opt->smax;
-  int rc = P->prec == 64 ? energy_grad_impl<double>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a)
-                         : energy_grad_impl<float>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a);
+  int rc;
+  if (pipeline_ok(P) && g_pipeline)   // per-half gradient + Adam in the two-stream pipeline
+    rc = P->prec == 64 ? energy_grad_pipelined<double>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a)
+                       : energy_grad_pipelined<float>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a);
+  else   // Adam in the epilogue of the adjoint rotation
+    rc = P->prec == 64 ? energy_grad_impl<double>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a)
+                       : energy_grad_impl<float>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a);
   profile_call_done(P);
   return rc;
 }
