@@ -26,6 +26,10 @@
  *   jrg_adam_update    optax.adam update + apply_updates,
  *                      calc/opt_utils.py:153-168, calc driver :179-180
  *   jrg_ewald          ewald.ewald_coulomb_repulsion, jrystal/_src/ewald.py:21-86
+ *   jrg_plan_set_pseudopotential  normcons.potential_local_reciprocal /
+ *                      potential_nonlocal_psi_reciprocal tables consumed by
+ *                      energy_local / energy_nonlocal in the norm-conserving
+ *                      driver, calc/calc_ground_state_energy_normcons.py:115-192
  *   jrg_precond_*      learned diagonal preconditioner (no jrystal counterpart)
  */
 #ifndef JRYSTAL_GB300_H_
@@ -87,6 +91,25 @@ int jrg_plan_destroy(jrg_plan* plan);
 /* Caller workspace needed by the entry points below (bytes). */
 int jrg_workspace_size(const jrg_plan* plan, size_t* bytes);
 
+/* Norm-conserving pseudopotential of the plan's atoms (replaces the
+ * all-electron Coulomb external potential; plan setup, allocates and
+ * synchronises like jrg_plan_create):
+ *   v_local     host double [nx][ny][nz] interleaved complex, the local part
+ *               V_loc(G) of potential_local_reciprocal
+ *               (jrystal/pseudopotential/local.py:32-132); NULL keeps the
+ *               current table;
+ *   projectors  host double [K][num_proj][G] interleaved complex, the rows
+ *               of potential_nonlocal_psi_reciprocal on the plane-wave sphere
+ *               (jrystal/pseudopotential/nloc.py:42-139); num_proj = 0
+ *               removes the nonlocal term.
+ * Every energy entry point then adds E_nl = sum f/vol sum_j |sum_G c P_j|^2
+ * (nloc.py:143-157, 238-248) to the external energy (energies[1]; the
+ * nonlocal part alone in energies[7]) and its gradient; jrg_potential's
+ * external part becomes IFFT(V_loc).  The workspace grows: query
+ * jrg_workspace_size again. */
+int jrg_plan_set_pseudopotential(jrg_plan* plan, const double* v_local, int num_proj,
+                                 const double* projectors);
+
 /* Orthonormal coefficients from raw parameters.
  * w_re, w_im: [S][K][G][B] real; coeff: [S][K][G][B] interleaved complex.
  * Columns equal jnp.linalg.qr's Q up to a unit phase per band. */
@@ -101,7 +124,8 @@ int jrg_density(const jrg_plan* plan, const void* coeff, const double* occupatio
 
 /* Loss and gradient of the direct-minimisation path.
  * energies (device double[8]): kinetic, external, hartree, xc, total,
- *   then max |C^H C - I| over k, and two reserved slots.
+ *   then max |C^H C - I| over k, the status word, and the nonlocal
+ *   pseudopotential part of the external energy (0 without projectors).
  * grad_re/grad_im: [S][K][G][B] d total / d w_re, d w_im (may be NULL for
  * energy only). */
 int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,

@@ -34,7 +34,11 @@ template <typename R> int launch_real_part(const void*, void*, long long, double
 template <typename R> int launch_hartree_g(const void*, const double*, void*, long long, double, cudaStream_t);
 template <typename R> int launch_kinetic(const void*, const double*, const double*, double*, double*, int, int, int, int, cudaStream_t);
 int launch_precond_scale(const float*, const void*, const double*, const double*, const double*, int, int, int, long long, float, float, float*, cudaStream_t);
-int launch_sum_slots(const double*, const int*, double*, int, const int*, cudaStream_t);
+int launch_sum_slots(const double*, const int*, double*, int, const int*, int, cudaStream_t);
+int nl_splits(int ng, int nsk, int nb, int np);
+template <typename R> int launch_nl_project(const void*, const void*, double2*, int, int, int, int, int, int, int, cudaStream_t);
+int launch_nl_reduce(const double2*, double2*, const double*, const double*, double*, int, int, int, int, double, cudaStream_t);
+template <typename R> int launch_nl_apply(void*, const void*, const double2*, int, int, int, int, int, int, cudaStream_t);
 int launch_band_trace_sums(const double2*, int, int, const double*, int, double*, cudaStream_t);
 int launch_kin_reduce(int, const void*, int, int, int, const double*, double*, double*, cudaStream_t);
 template <typename R> int launch_rotate_kinetic(const void*, const void*, const double2*, void*, int, int, int, const double*, int, void*, cudaStream_t, int = 0);
@@ -93,7 +97,8 @@ static void layout_workspace(jrg_plan* P) {
   // enough (s,k,split) CTAs to fill the GPU several times over: ~256 G rows each
   w.gram_splits = std::max(1, std::min(512, (int)((P->ng + 255) / 256)));
   w.ngroups = (int)nsk;
-  w.nepart = (int)nbt + 2 * kRecipBlocks + kXcBlocks;
+  // slots: kinetic [nbt], external, Hartree, xc [256 each], nonlocal [nsk]
+  w.nepart = (int)nbt + 2 * kRecipBlocks + kXcBlocks + (int)nsk;
   if (w.nepart < 2 * kEwaldBlocks) w.nepart = 2 * kEwaldBlocks;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t r = o; o += align256(bytes); return r; };
@@ -125,7 +130,32 @@ static void layout_workspace(jrg_plan* P) {
   w.rot_scratch = take(nsk * 2 * 128 * 64 * sizeof(uint32_t));   // split B of the TF32 rotations
   w.gga = (P->xc & kXcGga) ? take(3 * (size_t)P->ngrid * C) : 0;   // gradient / flux grids of PBE
   w.kin_part = take(nbt * (size_t)((P->ng + 255) / 256) * Rz);   // kinetic block partials
+  // beta-projector contraction: G-split partials and the weighted F
+  w.nl_splits = P->nproj > 0 ? nl_splits(P->ng, (int)nsk, P->nb, P->nproj) : 0;
+  w.nl_part = P->nproj > 0 ? take(nsk * w.nl_splits * (size_t)P->nb * P->nproj * sizeof(double2)) : 0;
+  w.nl_fw = P->nproj > 0 ? take(nbt * (size_t)P->nproj * sizeof(double2)) : 0;
   w.total = o;
+}
+
+// first energy slot of the nonlocal (beta-projector) partials, one per (s,k)
+static int nl_slot_begin(const jrg_plan* P) {
+  return P->ns * P->nk * P->nb + 2 * kRecipBlocks + kXcBlocks;
+}
+
+// energy slot boundaries: kinetic, external, Hartree, xc, then the nonlocal
+// range (empty without projectors) that k_sum_slots adds to the external term
+static int upload_slot_layout(jrg_plan* P) {
+  const int nbt = P->ns * P->nk * P->nb;
+  const int nl0 = nl_slot_begin(P);
+  const int sb[6] = {0, nbt, nbt + kRecipBlocks, nbt + 2 * kRecipBlocks, nl0,
+                     nl0 + (P->nproj > 0 ? P->ns * P->nk : 0)};
+  if (!P->slot_begin) {
+    cudaError_t e = cudaMalloc((void**)&P->slot_begin, sizeof(sb));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(slot layout)");
+  }
+  cudaError_t e = cudaMemcpy(P->slot_begin, sb, sizeof(sb), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(slot layout)");
+  return JRG_OK;
 }
 
 }  // namespace jrg
@@ -141,7 +171,7 @@ const char* jrg_last_error(void) { return g_err.c_str(); }
 int jrg_plan_destroy(jrg_plan* P) {
   if (!P) return JRG_OK;
   void* ptrs[] = {P->d.gidx, P->d.sph_yz, P->d.plane_x, P->d.plane_off, P->d.row_off, P->d.rows,
-                  P->d.xact, P->d.tk, P->d.tw, P->d.vext, P->d.ginv, P->d.gvec};
+                  P->d.xact, P->d.tk, P->d.tw, P->d.vext, P->d.ginv, P->d.gvec, P->d.proj};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (P->slot_begin) cudaFree(P->slot_begin);
@@ -345,13 +375,7 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
                                          d->num_atom, P->nx, P->ny, P->nz, P->vol, 0);
   }
   layout_workspace(P);
-  // energy slot boundaries: kinetic, external, hartree, xc
-  if (!rc) {
-    const int nbt = P->ns * P->nk * P->nb;
-    std::vector<int> sb = {0, nbt, nbt + kRecipBlocks, nbt + 2 * kRecipBlocks,
-                           nbt + 2 * kRecipBlocks + kXcBlocks};
-    rc = up((void**)&P->slot_begin, sb.data(), sb.size() * sizeof(int));
-  }
+  if (!rc) rc = upload_slot_layout(P);
   if (!rc) {
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) rc = cuda_fail(e, "plan setup");
@@ -365,6 +389,45 @@ int jrg_workspace_size(const jrg_plan* P, size_t* bytes) {
   if (!P || !bytes) return fail(JRG_ERR_INVALID, "null argument");
   *bytes = P->ws.total;
   return JRG_OK;
+}
+
+int jrg_plan_set_pseudopotential(jrg_plan* P, const double* v_local, int num_proj,
+                                 const double* projectors) {
+  if (!P || num_proj < 0 || (num_proj > 0 && !projectors))
+    return fail(JRG_ERR_INVALID, "jrg_plan_set_pseudopotential: bad argument");
+  // host FP64 interleaved complex -> device complex in the plan's precision
+  auto upload = [&](const double* src, size_t n, void* dst) -> int {
+    cudaError_t e;
+    if (P->prec == 64) {
+      e = cudaMemcpy(dst, src, n * 2 * sizeof(double), cudaMemcpyHostToDevice);
+    } else {
+      std::vector<float> f(2 * n);
+      for (size_t i = 0; i < 2 * n; ++i) f[i] = (float)src[i];
+      e = cudaMemcpy(dst, f.data(), n * 2 * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    return e == cudaSuccess ? JRG_OK : cuda_fail(e, "cudaMemcpy(pseudopotential table)");
+  };
+  int rc;
+  if (v_local && (rc = upload(v_local, (size_t)P->ngrid, P->d.vext))) return rc;
+  if (P->d.proj) {
+    cudaFree(P->d.proj);
+    P->d.proj = nullptr;
+  }
+  P->nproj = 0;
+  if (num_proj > 0) {
+    const size_t n = (size_t)P->nk * num_proj * P->ng;
+    cudaError_t e = cudaMalloc(&P->d.proj, n * csize(P->prec));
+    if (e != cudaSuccess) {
+      P->d.proj = nullptr;
+      return cuda_fail(e, "cudaMalloc(projector table)");
+    }
+    if ((rc = upload(projectors, n, P->d.proj))) return rc;
+    P->nproj = num_proj;
+  }
+  layout_workspace(P);
+  if ((rc = upload_slot_layout(P))) return rc;
+  cudaError_t e = cudaDeviceSynchronize();
+  return e == cudaSuccess ? JRG_OK : cuda_fail(e, "pseudopotential setup");
 }
 
 }  // extern "C"
@@ -477,6 +540,44 @@ static int gga_potential(const jrg_plan* P, const void* rho, const C_t<R>* vri, 
   return launch_potential_gga<R>(vri, vscale, vout, g, P->ngrid, st);
 }
 
+// Nonlocal pseudopotential term of the (s,k) blocks [k0, k0+n): F = C P and
+// its energy partials (weights occ), and the weighted fw = wg / vol F used by
+// nl_adjoint.  No-ops without projectors.
+template <typename R>
+static int nl_forward(const jrg_plan* P, void* ws, int k0, int n, const double* occ, const double* wg,
+                      cudaStream_t st) {
+  if (P->nproj <= 0) return JRG_OK;
+  PHASE(PH_NONLOCAL);
+  const Workspace& w = P->ws;
+  const size_t m = (size_t)P->nb * P->nproj;
+  double2* part = (double2*)wsp(ws, w.nl_part) + (size_t)k0 * w.nl_splits * m;
+  double2* fw = (double2*)wsp(ws, w.nl_fw) + (size_t)k0 * m;
+  const C_t<R>* c = (const C_t<R>*)wsp(ws, w.c) + (size_t)k0 * P->nb * P->ng;
+  double* slot = (double*)wsp(ws, w.epart) + nl_slot_begin(P) + k0;
+  int rc;
+  if ((rc = launch_nl_project<R>(c, P->d.proj, part, k0, n, P->nk, P->ng, P->nb, P->nproj, w.nl_splits,
+                                 st)))
+    return rc;
+  return launch_nl_reduce(part, fw, occ + (size_t)k0 * P->nb, wg + (size_t)k0 * P->nb, slot, n, P->nb,
+                          P->nproj, w.nl_splits, 1.0 / P->vol, st);
+}
+
+// g_C[k0, k0+n) += fw conj(P)
+template <typename R>
+static int nl_adjoint(const jrg_plan* P, void* ws, int k0, int n, cudaStream_t st) {
+  if (P->nproj <= 0) return JRG_OK;
+  PHASE(PH_NONLOCAL);
+  const Workspace& w = P->ws;
+  C_t<R>* gc = (C_t<R>*)wsp(ws, w.gc) + (size_t)k0 * P->nb * P->ng;
+  const double2* fw = (const double2*)wsp(ws, w.nl_fw) + (size_t)k0 * P->nb * P->nproj;
+  return launch_nl_apply<R>(gc, P->d.proj, fw, k0, n, P->nk, P->ng, P->nb, P->nproj, st);
+}
+
+static int sum_energy_slots(const jrg_plan* P, double* slots, double* energies, void* ws, cudaStream_t st) {
+  return launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, P->ws.flags),
+                          P->nproj > 0 ? 1 : -1, st);
+}
+
 // density of the band-major coefficients held in workspace slot c
 template <typename R>
 static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* rho_out,
@@ -530,6 +631,7 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
                                    adam->smax, adam->scale[0], st)))
       return rc;
   }
+  if ((rc = nl_forward<R>(P, ws, 0, nsk, occ, band_e ? P->d_ones : occ, st))) return rc;
   void* rho = wsp(ws, w.rho);
   if ((rc = density_from_c<R>(P, occ, ws, rho, st))) return rc;
   {
@@ -555,8 +657,7 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
                                          kXcBlocks, P->ngrid, P->xc, P->vol / N, st))) {
       return rc;
     }
-    if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st)))
-      return rc;
+    if ((rc = sum_energy_slots(P, slots, energies, ws, st))) return rc;
   }
   if (!adam && !g_re && !g_im) return JRG_OK;
   if (!adam && (!g_re || !g_im)) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
@@ -574,6 +675,7 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
                                          band_e ? P->d_ones : occ, 0, nbt, 1.0 / N, st)))
       return rc;
   }
+  if ((rc = nl_adjoint<R>(P, ws, 0, nsk, st))) return rc;
   // orthonormalisation adjoint
   {
     PHASE(PH_ADJ_GRAM);
@@ -620,6 +722,7 @@ static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im
                                 P->ng, P->nb, P->nk, st)))
       return rc;
   }
+  if ((rc = nl_forward<R>(P, ws, 0, nsk, wts, wts, st))) return rc;
   {
     PHASE(PH_PLANE_INV);
     if ((rc = launch_plane_inv_sphere<R>(P, wsp(ws, w.c), wsp(ws, w.t), nbt, st))) return rc;
@@ -634,6 +737,7 @@ static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im
                                          1.0 / N, st)))
       return rc;
   }
+  if ((rc = nl_adjoint<R>(P, ws, 0, nsk, st))) return rc;
   {
     PHASE(PH_ADJ_GRAM);
     if ((rc = launch_gram<R>(kBand, wsp(ws, w.c), nullptr, kBand, wsp(ws, w.gc), nullptr,
@@ -695,6 +799,7 @@ static int phase_forward_range(const jrg_plan* P, const void* w_re, const void* 
                                           (R*)wsp(ws, w.kin_part) + (size_t)k0 * nblk * P->nb, st, k0);
   if (kb < 0) return -kb;
   if (kb == 0) return fail(JRG_ERR_UNSUPPORTED, "pipelined path needs the fused kinetic rotation");
+  if ((rc = nl_forward<R>(P, ws, k0, n, occ, occ, st))) return rc;
   if ((rc = launch_plane_inv_sphere<R>(P, (C*)wsp(ws, w.c) + co, (C*)wsp(ws, w.t) + to, n * P->nb, st)))
     return rc;
   return launch_line_density<R>(P, (C*)wsp(ws, w.t) + to, (R*)wsp(ws, w.rho_part) + (size_t)k0 * P->ngrid,
@@ -721,6 +826,7 @@ static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re,
   int rc;
   if ((rc = launch_line_apply_v<R>(P, t, t, wsp(ws, w.vr), n * P->nb, P->nb, st))) return rc;
   if ((rc = launch_plane_fwd_sphere<R>(P, t, c, gc, occ, k0 * P->nb, n * P->nb, 1.0 / N, st))) return rc;
+  if ((rc = nl_adjoint<R>(P, ws, k0, n, st))) return rc;
   if ((rc = launch_gram<R>(kBand, c, nullptr, kBand, gc, nullptr,
                            (double2*)wsp(ws, w.adj_part) + (size_t)k0 * w.gram_splits * nb2,
                            (double2*)wsp(ws, w.adj) + k0 * nb2, n, P->ng, P->nb, w.gram_splits, st,
@@ -816,8 +922,7 @@ static int energy_grad_pipelined(const jrg_plan* P, const void* w_re, const void
                                          kXcBlocks, P->ngrid, P->xc, P->vol / N, st))) {
       return rc;
     }
-    if ((rc = launch_sum_slots(slots, P->slot_begin, energies, 4, (int*)wsp(ws, w.flags), st)))
-      return rc;
+    if ((rc = sum_energy_slots(P, slots, energies, ws, st))) return rc;
   }
   if (!adam && !g_re && !g_im) return JRG_OK;
   if (!adam && (!g_re || !g_im)) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
@@ -1081,7 +1186,7 @@ namespace {
 const char* kPhaseNames[jrg::PH_COUNT] = {
   "pack_params", "gram", "cholesky_inv", "rotate", "kinetic", "plane_inv_sphere", "line_density",
   "reduce_density", "grid_terms", "line_apply_v", "plane_fwd_sphere", "adj_gram", "adj_small",
-  "adj_rotate", "precond_scale"};
+  "adj_rotate", "precond_scale", "nonlocal"};
 }
 
 extern "C" {

@@ -362,21 +362,37 @@ __global__ void k_kin_reduce(const R* __restrict__ part, int nblk, int nb, int n
 }
 
 // energies[t] = sum of its slots, t = 0..3; energies[4] = total
+// energies[t] = sum of slots [slot_begin[t], slot_begin[t+1]) for t < nterms;
+// with extra_term >= 0 the range [slot_begin[nterms], slot_begin[nterms+1])
+// (the nonlocal pseudopotential energy) is added to term extra_term and also
+// reported alone in energies[nterms + 3]; energies[nterms] = total.
 __global__ void k_sum_slots(const double* __restrict__ slots, const int* __restrict__ slot_begin,
-                            double* __restrict__ energies, int nterms, const int* __restrict__ flags) {
+                            double* __restrict__ energies, int nterms, const int* __restrict__ flags,
+                            int extra_term) {
   __shared__ double red[32];
-  __shared__ double tot;
-  if (threadIdx.x == 0) tot = 0.0;
+  __shared__ double tot, extra;
+  if (threadIdx.x == 0) { tot = 0.0; extra = 0.0; }
+  if (extra_term >= 0) {
+    double acc = 0.0;
+    for (int i = slot_begin[nterms] + threadIdx.x; i < slot_begin[nterms + 1]; i += blockDim.x) acc += slots[i];
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) extra = acc;
+  }
   for (int t = 0; t < nterms; ++t) {
     double acc = 0.0;
     for (int i = slot_begin[t] + threadIdx.x; i < slot_begin[t + 1]; i += blockDim.x) acc += slots[i];
     acc = block_sum(acc, red);
-    if (threadIdx.x == 0) { energies[t] = acc; tot += acc; }
+    if (threadIdx.x == 0) {
+      if (t == extra_term) acc += extra;
+      energies[t] = acc;
+      tot += acc;
+    }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     energies[nterms] = tot;
     energies[nterms + 2] = flags ? (double)flags[0] : 0.0;
+    energies[nterms + 3] = extra;
   }
 }
 
@@ -709,8 +725,8 @@ int launch_band_trace_sums(const double2* A, int nsk, int nb, const double* slot
 }
 
 int launch_sum_slots(const double* slots, const int* slot_begin, double* energies, int nterms,
-                     const int* flags, cudaStream_t st) {
-  k_sum_slots<<<1, 256, 0, st>>>(slots, slot_begin, energies, nterms, flags);
+                     const int* flags, int extra_term, cudaStream_t st) {
+  k_sum_slots<<<1, 256, 0, st>>>(slots, slot_begin, energies, nterms, flags, extra_term);
   JRG_LAUNCH_CHECK("k_sum_slots");
   return JRG_OK;
 }

@@ -43,13 +43,14 @@ struct PlanTables {
   void* vext = nullptr;       // [ngrid] complex V_ext(G) in precision R
   double* ginv = nullptr;     // [ngrid] 4 pi / |G|^2, 0 at G = 0
   double* gvec = nullptr;     // [ngrid][3] cartesian G vectors
+  void* proj = nullptr;       // [nk][nproj][ng] complex beta-projector table (precision R)
 };
 
 // Per-phase CUDA-event timing of the fused entry points (optional).
 enum Phase {
   PH_PACK = 0, PH_GRAM, PH_CHOL, PH_ROTATE, PH_KINETIC, PH_PLANE_INV, PH_LINE_DENSITY,
   PH_REDUCE_DENSITY, PH_GRID_TERMS, PH_LINE_APPLY_V, PH_PLANE_FWD, PH_ADJ_GRAM, PH_ADJ_SMALL,
-  PH_ADJ_ROTATE, PH_PRECOND, PH_COUNT
+  PH_ADJ_ROTATE, PH_PRECOND, PH_NONLOCAL, PH_COUNT
 };
 struct Profiler {
   int max_calls = 0;
@@ -76,8 +77,10 @@ struct AdamArgs {
 // Workspace offsets (bytes) of one plan.
 struct Workspace {
   size_t wc, c, gram_part, gram, rmat, rinv, t, u, rho_part, rho, rhog, fft_scratch, vr,
-      gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, kin_part, total;
+      gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, kin_part, nl_part, nl_fw,
+      total;
   int gram_splits;
+  int nl_splits;  // G splits of the projector contraction
   int ngroups;    // density partial groups
   int nepart;     // energy partial slots
 };
@@ -94,6 +97,7 @@ struct jrg_plan {
   double cell[9], recip[9], vol;
   std::vector<double> pos, charge, kpts;
   int xc;
+  int nproj = 0;            // beta-projector rows of the pseudopotential (0: all-electron)
   jrg::FftAxis ax[3];
   jrg::PlanTables d;
   jrg::Workspace ws;

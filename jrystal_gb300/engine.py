@@ -103,6 +103,39 @@ class PlaneWavePlan:
     self.workspace_bytes = int(nbytes.value)
     self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=self.device)
     self.energies = torch.zeros(8, dtype=torch.float64, device=self.device)
+    self.num_proj = 0
+
+  def set_pseudopotential(self, v_local=None, projectors=None):
+    """Norm-conserving pseudopotential tables (jrg_plan_set_pseudopotential).
+
+    v_local: complex (nx, ny, nz) V_loc(G) of
+    pseudopotential.local.potential_local_reciprocal, or None to keep the
+    current external table; projectors: complex (K, J, G) beta-projector rows
+    on the sphere (pseudopotential.nloc.projector_table), or None / J = 0 for
+    no nonlocal term.  The workspace is reallocated to the new size."""
+    vl = None
+    if v_local is not None:
+      v = np.asarray(v_local, dtype=np.complex128)
+      if v.shape != self.grid:
+        raise ValueError(f"v_local shape {v.shape} != grid {self.grid}")
+      vl = np.ascontiguousarray(v.reshape(-1).view(np.float64))
+    nproj, pj = 0, None
+    if projectors is not None:
+      p = np.asarray(projectors, dtype=np.complex128)
+      if p.ndim != 3 or p.shape[0] != self.num_kpt or p.shape[2] != self.num_g:
+        raise ValueError(f"projectors shape {p.shape} != (K={self.num_kpt}, J, G={self.num_g})")
+      nproj = int(p.shape[1])
+      pj = np.ascontiguousarray(p.reshape(-1).view(np.float64)) if nproj else None
+    ptr = lambda a: None if a is None else a.ctypes.data_as(ct.c_void_p)
+    torch.cuda.synchronize(self.device)
+    _lib.check(self.lib.jrg_plan_set_pseudopotential(self._h, ptr(vl), nproj, ptr(pj)),
+               "jrg_plan_set_pseudopotential")
+    self.num_proj = nproj
+    nbytes = ct.c_size_t()
+    _lib.check(self.lib.jrg_workspace_size(self._h, ct.byref(nbytes)), "jrg_workspace_size")
+    if int(nbytes.value) != self.workspace_bytes:
+      self.workspace_bytes = int(nbytes.value)
+      self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=self.device)
 
   # -- shapes -------------------------------------------------------------
   @property
@@ -128,7 +161,8 @@ class PlaneWavePlan:
                       grad_re: Optional[torch.Tensor] = None,
                       grad_im: Optional[torch.Tensor] = None, with_grad: bool = True):
     """Energy terms (device float64[8]: kinetic, external, hartree, xc,
-    total, -, cholesky-breakdown flag, -) and d total/d{w_re, w_im}."""
+    total, -, cholesky-breakdown flag, nonlocal pseudopotential part of the
+    external term) and d total/d{w_re, w_im}."""
     self._check_param(w_re, "w_re")
     self._check_param(w_im, "w_im")
     occ = self._occ(occupation)

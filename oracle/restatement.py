@@ -686,6 +686,8 @@ def band_trace_terms(w_re, w_im, v_eff, sysm, weights=None, with_grad=True):
   hpsi = _fftn(v[None, None, None] * wave)[..., mask] * (np.sqrt(vol) / n)
   tk = kinetic_operator(gvec, sysm.kpts)[:, mask]  # (k,g)
   hc = tk[None, :, None, :] * np.swapaxes(c, -1, -2) + hpsi   # (s,k,b,g) = H c_b
+  if sysm.proj is not None:      # + V_nl c_b (nloc.py:251-303)
+    hc = hc + _nonlocal_grad_c(dense, sysm.proj, vol, np.ones(weights.shape), mask)
   g_c = np.swapaxes(weights[..., None] * hc, -1, -2)          # (s,k,g,b)
   a = np.einsum("...gi,...gj->...ij", c.conj(), g_c)
   kin = np.sum(weights * np.einsum("kg,skgb->skb", tk, np.abs(c)**2))
@@ -768,6 +770,10 @@ class System:
   kpts: np.ndarray
   occupation: np.ndarray     # (spin, kpt, band)
   xc: str = "lda_x+lda_c_vwn"
+  # norm-conserving pseudopotential: complex V_loc(G) grid replacing the
+  # Coulomb external potential, and dense beta-projector rows (k, j, x, y, z)
+  v_local: Optional[np.ndarray] = None
+  proj: Optional[np.ndarray] = None
 
   @property
   def vol(self):
@@ -776,6 +782,31 @@ class System:
   @property
   def g_vector_grid(self):
     return g_vectors(self.cell_vectors, self.grid)
+
+
+def nonlocal_projections(coeff_dense, proj):
+  """F[s,k,b,j] = sum_xyz c P (c not conjugated; nloc.py:143-151)."""
+  p = np.asarray(proj).reshape(proj.shape[0], -1, *proj.shape[-3:])
+  return np.einsum("skbxyz,kjxyz->skbj", coeff_dense, p)
+
+
+def hamiltonian_nonlocal(coeff_dense, proj, vol):
+  """H_nl = F^H F / vol per (s, k) (nloc.py:143-157)."""
+  f = nonlocal_projections(coeff_dense, proj)
+  return np.einsum("skbj,skcj->skbc", np.conj(f), f) / vol
+
+
+def energy_nonlocal(coeff_dense, proj, vol, occupation):
+  """sum_{s,k,b} f_skb H_nl[s,k,b,b] (nloc.py:238-248)."""
+  h = hamiltonian_nonlocal(coeff_dense, proj, vol)
+  return float(np.sum(np.einsum("skbb->skb", h) * occupation).real)
+
+
+def _nonlocal_grad_c(coeff_dense, proj, vol, weights, mask):
+  """d E_nl / d conj(c) on the sphere: w_b / vol sum_j F_bj conj(P_j) -> (s,k,b,g)."""
+  p = np.asarray(proj).reshape(proj.shape[0], -1, *proj.shape[-3:])
+  f = nonlocal_projections(coeff_dense, p)
+  return weights[..., None] / vol * np.einsum("skbj,kjg->skbg", f, np.conj(p[..., mask]))
 
 
 def energy_terms(w_re, w_im, sysm: System, with_grad=True):
@@ -799,25 +830,32 @@ def energy_terms(w_re, w_im, sysm: System, with_grad=True):
   rho = wave_to_density(wave, occ)                # (s,x,y,z)
   rho_g = _fftn(rho)
   e_kin = kinetic_energy(gvec, sysm.kpts, dense, occ)
-  e_ext = external_energy(rho_g, sysm.positions, sysm.charges, gvec, vol)
+  if sysm.v_local is not None:     # normcons.energy_local (local.py:163-187)
+    v_ext = np.asarray(sysm.v_local)
+  else:
+    v_ext = external_reciprocal(sysm.positions, sysm.charges, gvec, vol)
+  e_ext = reciprocal_braket(v_ext[None], rho_g, vol)
+  e_nl = energy_nonlocal(dense, sysm.proj, vol, occ) if sysm.proj is not None else 0.0
   e_har = hartree_energy(rho_g, gvec, vol, False)
   if is_gga(sysm.xc):
     e_xc, v_xc_gga, _ = gga_energy_potential(rho[0], gvec, vol, sysm.xc)
   else:
     e_xc = xc_energy(rho, vol, sysm.xc, False)
-  terms = dict(kinetic=e_kin, external=e_ext, hartree=e_har, xc=e_xc)
-  terms["total"] = e_kin + e_ext + e_har + e_xc
+  terms = dict(kinetic=e_kin, external=e_ext + e_nl, hartree=e_har, xc=e_xc,
+               external_local=e_ext, external_nonlocal=e_nl)
+  terms["total"] = e_kin + e_ext + e_nl + e_har + e_xc
   if not with_grad:
     return terms
   # dE/d rho(r) = (vol/N) V(r)
-  v_g = (hartree_reciprocal(rho_g, gvec, kohn_sham=True) +
-         external_reciprocal(sysm.positions, sysm.charges, gvec, vol))
+  v_g = hartree_reciprocal(rho_g, gvec, kohn_sham=True) + v_ext
   v_xc = v_xc_gga if is_gga(sysm.xc) else xc_eps_v(rho[0], sysm.xc)[1]
   v_r = np.real(_ifftn(v_g)) + v_xc
   hpsi = _fftn(v_r[None, None, None] * wave)
   hpsi = hpsi[..., mask] * (np.sqrt(vol) / n)     # (s,k,b,g)
   tk = kinetic_operator(gvec, sysm.kpts)[:, mask]  # (k,g)
   g_c = occ[..., None] * (tk[None, :, None, :] * np.swapaxes(c, -1, -2) + hpsi)
+  if sysm.proj is not None:
+    g_c = g_c + _nonlocal_grad_c(dense, sysm.proj, vol, occ, mask)
   g_c = np.swapaxes(g_c, -1, -2)                   # (s,k,g,b)
   a = np.einsum("...gi,...gj->...ij", c.conj(), g_c)
   up = np.triu(a, 1)

@@ -52,3 +52,30 @@ def random_params(sysm, seed=0, ns=1, dtype=np.float64):
   rng = np.random.default_rng(seed)
   shape = (ns, sysm.kpts.shape[0], int(sysm.mask.sum()), sysm.occupation.shape[-1])
   return rng.normal(size=shape).astype(dtype), rng.normal(size=shape).astype(dtype)
+
+
+def nc_tables(sysm, symbols, upf_dir, kpts=None):
+  """Norm-conserving pseudopotential tables of a system from the UPF files in
+  ``upf_dir``: (container, V_loc(G) grid, dense projector rows
+  [k, beta, m, x, y, z], sphere projector table [k, J, G])."""
+  from types import SimpleNamespace
+  from jrystal_gb300.pseudopotential import NormConservingPseudopotential, local, nloc
+  crystal = SimpleNamespace(symbols=list(symbols), positions=sysm.positions, charges=sysm.charges)
+  pp = NormConservingPseudopotential.create(crystal, upf_dir)
+  g = sysm.g_vector_grid
+  k = sysm.kpts if kpts is None else kpts
+  vloc = local.potential_local_reciprocal(sysm.positions, g, pp.r_grid, pp.local_potential_grid,
+                                          pp.local_potential_charge, sysm.vol)
+  dense = nloc.potential_nonlocal_psi_reciprocal(sysm.positions, g, k, pp.r_grid,
+                                                 pp.nonlocal_beta_grid,
+                                                 pp.nonlocal_angular_momentum,
+                                                 pp.nonlocal_d_matrix)
+  table = nloc.projector_table(sysm.positions, g, k, sysm.mask, pp.r_grid, pp.nonlocal_beta_grid,
+                               pp.nonlocal_angular_momentum, pp.nonlocal_d_matrix)
+  return pp, vloc, dense, table
+
+
+def with_pseudopotential(sysm, vloc, dense, nelec_per_band_pairs=None):
+  """A copy of the oracle system with the pseudopotential tables attached."""
+  import dataclasses
+  return dataclasses.replace(sysm, v_local=vloc, proj=dense)
