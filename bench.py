@@ -40,6 +40,9 @@ def _args():
   p.add_argument("--impl", default="ours", choices=["ours", "reference"])
   p.add_argument("--workload", default="si8_cubic_64")
   p.add_argument("--no-cpu-baseline", action="store_true")
+  p.add_argument("--pseudo", action="store_true",
+                 help="attach the analytic norm-conserving model pseudopotential "
+                      "(local table + beta projectors) to the workload")
   p.add_argument("--no-time-to-tol", action="store_true",
                  help="skip the learned-vs-plain time-to-tolerance runs")
   p.add_argument("--cpu-sample-kpts", type=int, default=1)
@@ -224,6 +227,10 @@ def phase_bytes(plan, fused=False):
     "plane_fwd_sphere": nbt * (planes + 2 * sph) + plan.num_kpt * plan.num_g * 8,
     "adj_gram": 2 * nbt * sph,
     "adj_rotate": 2 * nbt * sph + (6 if fused else 1) * nbt * sph,
+    # beta projectors: C and the table read once; the table again and g_C
+    # read + written by the apply pass
+    "nl_project": nbt * sph + plan.num_kpt * plan.num_proj * sph,
+    "nl_apply": plan.num_kpt * plan.num_proj * sph + 2 * nbt * sph,
   }
 
 
@@ -263,6 +270,9 @@ def run_ours(args, wl):
   lib = _lib.load()
   plan = PlaneWavePlan(wl.cell, wl.positions, wl.charges, wl.grid_sizes, wl.mask, wl.kpts,
                        wl.num_band, 1, wl.precision, wl.xc, device=dev)
+  if args.pseudo:
+    from jrystal_gb300.workloads import model_pseudopotential
+    plan.set_pseudopotential(*model_pseudopotential(wl))
   wr, wi = wl.init_params()
   rdt = plan.rdtype
   params = torch.tensor(np.stack([wr, wi]), dtype=rdt, device=dev).contiguous()
@@ -394,9 +404,18 @@ def run_ours(args, wl):
                    "d2h_bytes_per_step": 64},
            "gpu_launches": int(launches), "roofline": roof,
            "energies_last_step": energies[:5]}
+    if args.pseudo:
+      out["config"]["cell"] = "Si cell with the analytic norm-conserving model pseudopotential"
+      out["config"]["projector_rows"] = int(plan.num_proj)
+      out["energies_last_step"] = energies[:5] + [energies[7]]
+      out["nonlocal"] = {k: {"ms_per_launch": round(phases[k], 5),
+                             "algorithmic_bytes": pb[k],
+                             "achieved_gbs": pb[k] / (phases[k] * 1e-3) / 1e9,
+                             "frac": pb[k] / (phases[k] * 1e-3) / 1e9 / peak}
+                         for k in ("nl_project", "nl_apply") if phases.get(k, 0) > 0}
     if not args.no_time_to_tol:
       out["time_to_1e-5_Ha_per_atom"] = time_to_tolerance()
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and not args.pseudo:
       workers = len(os.sched_getaffinity(0))
       nks = max(1, min(args.cpu_sample_kpts, wl.num_kpt))
       per_eval, t_sample = cpu_sample(wl, nks, workers)

@@ -42,6 +42,9 @@ DEFAULT_CONFIG = {
   "seed": 123,
   "jax_enable_x64": True,
   "verbose": False,
+  "use_pseudopotential": False,
+  "pseudopotential_type": "nc",
+  "pseudopotential_file_dir": None,
 }
 
 
@@ -163,18 +166,35 @@ def create_crystal(cfg) -> Crystal:
   return Crystal.create_from_file(path, spin=cfg.get("spin"))
 
 
-def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
-  """All-electron ground state by direct minimisation with fixed occupations
-  (calc/calc_ground_state_energy_all_electrons.py:63-247)."""
-  cfg = _merge(config)
-  if cfg["optimizer"] != "adam":
-    raise NotImplementedError("only the adam optimiser is implemented on the device")
-  if cfg["occupation"] in ("simplex-projector", "idempotent"):
-    return _energy_learnable_occupation(cfg)
-  if cfg["occupation"] not in ("uniform", "gamma"):
-    raise ValueError(f"Invalid method: {cfg['occupation']}")
-  if not cfg["spin_restricted"]:
-    raise NotImplementedError("spin-polarised LDA is not implemented")
+def create_pseudopotential(cfg, crystal):
+  """NormConservingPseudopotential of the crystal's atoms from the UPF files
+  in ``pseudopotential_file_dir`` (calc/opt_utils.py:117-140); jrystal's
+  bundled files are not shipped, so the directory is required."""
+  from .pseudopotential import NormConservingPseudopotential
+  kind = cfg.get("pseudopotential_type", "nc")
+  if kind not in ("normcons", "normconserving", "nc"):
+    if kind in ("ultrasoft", "us"):
+      raise NotImplementedError("ultrasoft pseudopotentials are not implemented")
+    raise ValueError(f"Pseudopotential type {kind} is not supported.")
+  d = cfg.get("pseudopotential_file_dir")
+  if d is None:
+    raise ValueError("pseudopotential_file_dir must name the directory of the UPF files")
+  return NormConservingPseudopotential.create(crystal, d)
+
+
+@dataclass
+class _Setup:
+  crystal: Crystal
+  pseudo: object          # NormConservingPseudopotential or None (all-electron)
+  precision: int
+  grid_sizes: tuple
+  kpts: np.ndarray
+  mask: np.ndarray
+  nelec: int              # valence electrons with a pseudopotential
+  num_bands: int
+
+
+def _setup(cfg, pseudo: bool) -> _Setup:
   crystal = create_crystal(cfg)
   precision = 64 if cfg["jax_enable_x64"] else 32
   grid_sizes = tuple(int(g) for g in _grid.proper_grid_size(cfg["grid_sizes"]))
@@ -186,8 +206,73 @@ def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
     mask = _grid.cubic_mask(grid_sizes)
   else:
     raise ValueError("freq_mask_method must be either cubic or spherical.")
-  nelec = crystal.num_electron
+  pp = create_pseudopotential(cfg, crystal) if pseudo else None
+  nelec = int(sum(pp.valence_charges)) if pp is not None else int(crystal.num_electron)
   num_bands = math.ceil(nelec / 2) + cfg["empty_bands"]
+  return _Setup(crystal, pp, precision, grid_sizes, kpts, mask, nelec, num_bands)
+
+
+def attach_pseudopotential(plan: PlaneWavePlan, pp, kmax: Optional[float] = None):
+  """Local V_loc(G) and beta-projector tables of ``pp`` on ``plan``
+  (calc/calc_ground_state_energy_normcons.py:115-153): built on the host as
+  the reference builds them, consumed by the device kernels."""
+  from .pseudopotential import local, nloc
+  g = _grid.g_vectors(plan.cell, plan.grid)
+  vloc = local.potential_local_reciprocal(plan.positions, g, pp.r_grid, pp.local_potential_grid,
+                                          pp.local_potential_charge, plan.vol)
+  table = nloc.projector_table(plan.positions, g, plan.kpts, plan.mask, pp.r_grid,
+                               pp.nonlocal_beta_grid, pp.nonlocal_angular_momentum,
+                               pp.nonlocal_d_matrix, kmax=kmax)
+  plan.set_pseudopotential(vloc, table)
+  return plan
+
+
+def _make_plan(su: _Setup, cfg, kpts=None, num_bands=None, kmax=None) -> PlaneWavePlan:
+  c = su.crystal
+  plan = PlaneWavePlan(c.cell_vectors, c.positions, c.charges, su.grid_sizes, su.mask,
+                       su.kpts if kpts is None else kpts, num_bands or su.num_bands, 1,
+                       su.precision, cfg["xc"])
+  if su.pseudo is not None:
+    attach_pseudopotential(plan, su.pseudo, kmax=kmax)
+  return plan
+
+
+def _energy_terms_dict(e, pseudo: bool):
+  terms = dict(kinetic=e[0], external=e[1], hartree=e[2], xc=e[3], total=e[4])
+  if pseudo:
+    terms.update(external_local=e[1] - e[7], external_nonlocal=e[7])
+  return terms
+
+
+def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
+  """All-electron ground state by direct minimisation with fixed occupations
+  (calc/calc_ground_state_energy_all_electrons.py:63-247)."""
+  return _ground_state(_merge(config), pseudo=False)
+
+
+def energy_normcons(config: dict) -> GroundStateEnergyOutput:
+  """Ground state with norm-conserving pseudopotentials
+  (calc/calc_ground_state_energy_normcons.py:68-308): valence electrons only,
+  the local table in place of the Coulomb external potential, the nonlocal
+  beta-projector energy added to the loss (energy_terms carries
+  external_local and external_nonlocal).  The Ewald constant uses the
+  crystal's nuclear charges, as the reference's get_ewald_coulomb_repulsion
+  does (calc/opt_utils.py:186-200)."""
+  return _ground_state(_merge(config), pseudo=True)
+
+
+def _ground_state(cfg, pseudo: bool) -> GroundStateEnergyOutput:
+  if cfg["optimizer"] != "adam":
+    raise NotImplementedError("only the adam optimiser is implemented on the device")
+  if cfg["occupation"] in ("simplex-projector", "idempotent"):
+    return _energy_learnable_occupation(cfg, pseudo)
+  if cfg["occupation"] not in ("uniform", "gamma"):
+    raise ValueError(f"Invalid method: {cfg['occupation']}")
+  if not cfg["spin_restricted"]:
+    raise NotImplementedError("spin-polarised LDA is not implemented")
+  su = _setup(cfg, pseudo)
+  crystal, kpts, mask, nelec = su.crystal, su.kpts, su.mask, su.nelec
+  num_bands = su.num_bands
   K = kpts.shape[0]
   if cfg["occupation"] == "uniform":
     occ = np.zeros((2, K, num_bands))
@@ -201,8 +286,7 @@ def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
   if "occupation_array" in cfg:
     occ = np.asarray(cfg["occupation_array"], dtype=np.float64)
     num_bands = occ.shape[-1]
-  plan = PlaneWavePlan(crystal.cell_vectors, crystal.positions, crystal.charges, grid_sizes, mask,
-                       kpts, num_bands, 1, precision, cfg["xc"])
+  plan = _make_plan(su, cfg, num_bands=num_bands)
   ew = plan.ewald(cfg["ewald_args"]["ewald_eta"], cfg["ewald_args"]["ewald_cutoff"])
   ng = int(mask.sum())
   gen = torch.Generator(device=plan.device)
@@ -231,7 +315,7 @@ def energy_all_electrons(config: dict) -> GroundStateEnergyOutput:
       break
   e, _, _ = plan.energy_and_grad(mini.params[0], mini.params[1], mini.occ, with_grad=False)
   e = e.cpu().numpy()
-  terms = dict(kinetic=e[0], external=e[1], hartree=e[2], xc=e[3], total=e[4])
+  terms = _energy_terms_dict(e, pseudo)
   rho = plan.density(plan.coeff(mini.params[0], mini.params[1]), mini.occ)
   return GroundStateEnergyOutput(config=cfg, crystal=crystal,
                                  params_pw={"w_re": mini.params[0], "w_im": mini.params[1]},
@@ -253,32 +337,23 @@ def temperature_schedule(cfg):
   return lambda i: max(sm, 100.0 * rate ** (i / steps))
 
 
-def _energy_learnable_occupation(cfg) -> GroundStateEnergyOutput:
+def _energy_learnable_occupation(cfg, pseudo: bool = False) -> GroundStateEnergyOutput:
   """Free-energy minimisation F = E - T S over the plane-wave parameters and
   learnable occupations (simplex projector or idempotent), the reference
   driver's path for metals (calc/calc_ground_state_energy_all_electrons.py:
-  103-147 and 150-220): the device returns E, dE/dW and the band energies
-  dE/df (jrg_energy_grad_bands); dF/d(occupation parameters) follows by
-  torch autograd through the occupation map and the Fermi-Dirac entropy;
-  both parameter sets take Adam steps with the same hyper-parameters."""
+  103-147 and 150-220; calc_ground_state_energy_normcons.py:155-257): the
+  device returns E, dE/dW and the band energies dE/df
+  (jrg_energy_grad_bands); dF/d(occupation parameters) follows by torch
+  autograd through the occupation map and the Fermi-Dirac entropy; both
+  parameter sets take Adam steps with the same hyper-parameters."""
   from . import entropy as _entropy
   from . import occupation as _occupation
   if not cfg["spin_restricted"]:
     raise NotImplementedError("spin-polarised LDA is not implemented")
-  crystal = create_crystal(cfg)
-  precision = 64 if cfg["jax_enable_x64"] else 32
-  grid_sizes = tuple(int(g) for g in _grid.proper_grid_size(cfg["grid_sizes"]))
-  k_grid = tuple(int(k) for k in np.broadcast_to(cfg["k_grid_sizes"], 3))
-  kpts = _grid.k_vectors(crystal.cell_vectors, k_grid)
-  if cfg["freq_mask_method"] == "spherical":
-    mask = _grid.spherical_mask(crystal.cell_vectors, grid_sizes, cfg["cutoff_energy"])
-  else:
-    mask = _grid.cubic_mask(grid_sizes)
-  nelec = crystal.num_electron
-  num_bands = math.ceil(nelec / 2) + cfg["empty_bands"]
+  su = _setup(cfg, pseudo)
+  crystal, kpts, mask, nelec, num_bands = su.crystal, su.kpts, su.mask, su.nelec, su.num_bands
   K = kpts.shape[0]
-  plan = PlaneWavePlan(crystal.cell_vectors, crystal.positions, crystal.charges, grid_sizes, mask,
-                       kpts, num_bands, 1, precision, cfg["xc"])
+  plan = _make_plan(su, cfg)
   ew = plan.ewald(cfg["ewald_args"]["ewald_eta"], cfg["ewald_args"]["ewald_cutoff"])
   ng = int(mask.sum())
   gen = torch.Generator(device=plan.device)
@@ -340,8 +415,8 @@ def _energy_learnable_occupation(cfg) -> GroundStateEnergyOutput:
     occ = occ_of().detach()
   e, _, _ = plan.energy_and_grad(params[0], params[1], occ, with_grad=False)
   e = e.cpu().numpy()
-  terms = dict(kinetic=e[0], external=e[1], hartree=e[2], xc=e[3], total=e[4],
-               entropy=float(_entropy.fermi_dirac(occ, eps=ent_eps)), temperature=temp_of(i))
+  terms = _energy_terms_dict(e, pseudo)
+  terms.update(entropy=float(_entropy.fermi_dirac(occ, eps=ent_eps)), temperature=temp_of(i))
   rho = plan.density(plan.coeff(params[0], params[1]), occ)
   return GroundStateEnergyOutput(config=cfg, crystal=crystal,
                                  params_pw={"w_re": params[0], "w_im": params[1]},
@@ -393,27 +468,38 @@ def band_structure_all_electrons(config: dict) -> BandStructureOutput:
   at a time, each starting from the previous one); the eigenvalues of the
   band Hamiltonian H_ij = <psi_i|H|psi_j> at each k-point are returned as
   (spin, k, band)."""
+  return _band_structure(config, pseudo=False)
+
+
+def band_structure_normcons(config: dict) -> BandStructureOutput:
+  """Band structure with norm-conserving pseudopotentials
+  (calc/calc_band_structure_normcons.py:68-299): as the all-electron driver,
+  with v_eff = V_H + v_loc + v_xc of the ground-state density and the
+  nonlocal projector term in the band trace and band Hamiltonian
+  (nloc.hamiltonian_trace / hamiltonian_matrix); the beta transforms use the
+  largest |G+k| over the whole k path, as the reference's pre-computation
+  over the path does."""
+  return _band_structure(config, pseudo=True)
+
+
+def _band_structure(config: dict, pseudo: bool) -> BandStructureOutput:
   from .band import get_k_path
+  from .pseudopotential.beta import max_gk_radius
   cfg = dict(BAND_DEFAULTS)
   cfg.update(_merge(config))
-  gs = energy_all_electrons(cfg)
-  crystal = gs.crystal
-  precision = 64 if cfg["jax_enable_x64"] else 32
-  grid_sizes = tuple(int(g) for g in _grid.proper_grid_size(cfg["grid_sizes"]))
-  if cfg["freq_mask_method"] == "spherical":
-    mask = _grid.spherical_mask(crystal.cell_vectors, grid_sizes, cfg["cutoff_energy"])
-  else:
-    mask = _grid.cubic_mask(grid_sizes)
+  gs = _ground_state(cfg, pseudo)
+  su = _setup(cfg, pseudo)
+  crystal, mask = su.crystal, su.mask
   k_path = get_k_path(crystal.cell_vectors, cfg["k_path_special_points"], int(cfg["num_kpoints"]))
   extra = cfg["band_structure_empty_bands"]
-  num_bands = math.ceil(crystal.num_electron / 2) + (int(extra) if extra is not None else 0)
+  num_bands = math.ceil(su.nelec / 2) + (int(extra) if extra is not None else 0)
   oa = cfg["optimizer_args"]
   lr, b1, b2, eps = (oa.get("learning_rate", 1e-2), oa.get("b1", 0.9), oa.get("b2", 0.999),
                      oa.get("eps", 1e-8))
+  kmax = max_gk_radius(_grid.g_vectors(crystal.cell_vectors, su.grid_sizes), k_path) if pseudo else None
 
   def make_plan(kpts):
-    return PlaneWavePlan(crystal.cell_vectors, crystal.positions, crystal.charges, grid_sizes,
-                         mask, kpts, num_bands, 1, precision, cfg["xc"])
+    return _make_plan(su, cfg, kpts=kpts, num_bands=num_bands, kmax=kmax)
 
   t_start = time.perf_counter()
   plan0 = make_plan(k_path[:1])
@@ -453,5 +539,8 @@ def band_structure_all_electrons(config: dict) -> BandStructureOutput:
   if cfg.get("save_path"):
     np.save(cfg["save_path"], eig)
   return out
+
+
 # the reference's name for the all-electron band driver (jrystal/calc/__init__.py:18)
 band_all_electrons = band_structure_all_electrons
+band_normcons = band_structure_normcons

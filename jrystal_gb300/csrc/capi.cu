@@ -36,6 +36,7 @@ template <typename R> int launch_kinetic(const void*, const double*, const doubl
 int launch_precond_scale(const float*, const void*, const double*, const double*, const double*, int, int, int, long long, float, float, float*, cudaStream_t);
 int launch_sum_slots(const double*, const int*, double*, int, const int*, int, cudaStream_t);
 int nl_splits(int ng, int nsk, int nb, int np);
+int nl_chunks(int nb, int np);
 template <typename R> int launch_nl_project(const void*, const void*, double2*, int, int, int, int, int, int, int, cudaStream_t);
 int launch_nl_reduce(const double2*, double2*, const double*, const double*, double*, int, int, int, int, double, cudaStream_t);
 template <typename R> int launch_nl_apply(void*, const void*, const double2*, int, int, int, int, int, int, cudaStream_t);
@@ -97,8 +98,10 @@ static void layout_workspace(jrg_plan* P) {
   // enough (s,k,split) CTAs to fill the GPU several times over: ~256 G rows each
   w.gram_splits = std::max(1, std::min(512, (int)((P->ng + 255) / 256)));
   w.ngroups = (int)nsk;
-  // slots: kinetic [nbt], external, Hartree, xc [256 each], nonlocal [nsk]
-  w.nepart = (int)nbt + 2 * kRecipBlocks + kXcBlocks + (int)nsk;
+  // slots: kinetic [nbt], external, Hartree, xc [256 each], nonlocal
+  // [nsk * nl_chunks] (one per reduction CTA)
+  w.nepart = (int)nbt + 2 * kRecipBlocks + kXcBlocks +
+             (int)nsk * (P->nproj > 0 ? nl_chunks(P->nb, P->nproj) : 1);
   if (w.nepart < 2 * kEwaldBlocks) w.nepart = 2 * kEwaldBlocks;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t r = o; o += align256(bytes); return r; };
@@ -148,7 +151,7 @@ static int upload_slot_layout(jrg_plan* P) {
   const int nbt = P->ns * P->nk * P->nb;
   const int nl0 = nl_slot_begin(P);
   const int sb[6] = {0, nbt, nbt + kRecipBlocks, nbt + 2 * kRecipBlocks, nl0,
-                     nl0 + (P->nproj > 0 ? P->ns * P->nk : 0)};
+                     nl0 + (P->nproj > 0 ? P->ns * P->nk * nl_chunks(P->nb, P->nproj) : 0)};
   if (!P->slot_begin) {
     cudaError_t e = cudaMalloc((void**)&P->slot_begin, sizeof(sb));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(slot layout)");
@@ -547,13 +550,13 @@ template <typename R>
 static int nl_forward(const jrg_plan* P, void* ws, int k0, int n, const double* occ, const double* wg,
                       cudaStream_t st) {
   if (P->nproj <= 0) return JRG_OK;
-  PHASE(PH_NONLOCAL);
+  PHASE(PH_NL_PROJECT);
   const Workspace& w = P->ws;
   const size_t m = (size_t)P->nb * P->nproj;
   double2* part = (double2*)wsp(ws, w.nl_part) + (size_t)k0 * w.nl_splits * m;
   double2* fw = (double2*)wsp(ws, w.nl_fw) + (size_t)k0 * m;
   const C_t<R>* c = (const C_t<R>*)wsp(ws, w.c) + (size_t)k0 * P->nb * P->ng;
-  double* slot = (double*)wsp(ws, w.epart) + nl_slot_begin(P) + k0;
+  double* slot = (double*)wsp(ws, w.epart) + nl_slot_begin(P) + (size_t)k0 * nl_chunks(P->nb, P->nproj);
   int rc;
   if ((rc = launch_nl_project<R>(c, P->d.proj, part, k0, n, P->nk, P->ng, P->nb, P->nproj, w.nl_splits,
                                  st)))
@@ -566,7 +569,7 @@ static int nl_forward(const jrg_plan* P, void* ws, int k0, int n, const double* 
 template <typename R>
 static int nl_adjoint(const jrg_plan* P, void* ws, int k0, int n, cudaStream_t st) {
   if (P->nproj <= 0) return JRG_OK;
-  PHASE(PH_NONLOCAL);
+  PHASE(PH_NL_APPLY);
   const Workspace& w = P->ws;
   C_t<R>* gc = (C_t<R>*)wsp(ws, w.gc) + (size_t)k0 * P->nb * P->ng;
   const double2* fw = (const double2*)wsp(ws, w.nl_fw) + (size_t)k0 * P->nb * P->nproj;
@@ -1186,7 +1189,7 @@ namespace {
 const char* kPhaseNames[jrg::PH_COUNT] = {
   "pack_params", "gram", "cholesky_inv", "rotate", "kinetic", "plane_inv_sphere", "line_density",
   "reduce_density", "grid_terms", "line_apply_v", "plane_fwd_sphere", "adj_gram", "adj_small",
-  "adj_rotate", "precond_scale", "nonlocal"};
+  "adj_rotate", "precond_scale", "nl_project", "nl_apply"};
 }
 
 extern "C" {

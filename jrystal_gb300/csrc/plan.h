@@ -50,7 +50,7 @@ struct PlanTables {
 enum Phase {
   PH_PACK = 0, PH_GRAM, PH_CHOL, PH_ROTATE, PH_KINETIC, PH_PLANE_INV, PH_LINE_DENSITY,
   PH_REDUCE_DENSITY, PH_GRID_TERMS, PH_LINE_APPLY_V, PH_PLANE_FWD, PH_ADJ_GRAM, PH_ADJ_SMALL,
-  PH_ADJ_ROTATE, PH_PRECOND, PH_NONLOCAL, PH_COUNT
+  PH_ADJ_ROTATE, PH_PRECOND, PH_NL_PROJECT, PH_NL_APPLY, PH_COUNT
 };
 struct Profiler {
   int max_calls = 0;

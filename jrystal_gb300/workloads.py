@@ -102,3 +102,24 @@ def si64_supercell(precision=32):
 
 
 WORKLOADS = {"si2_fcc_48": si2_fcc, "si8_cubic_64": si8_cubic, "si64_supercell_96": si64_supercell}
+
+
+def model_pseudopotential(wl: Workload, z_valence: int = 4):
+  """Tables of an analytic norm-conserving model pseudopotential on every atom
+  of ``wl`` (the timed norm-conserving variant of a workload; the model is not
+  fitted to silicon): local V(r) = -z erf(r / 0.8) / r and two Gaussian
+  projectors beta_l(r) = r^l exp(-(r / 0.9)^2), l = 0, 1, with D = diag(0.8,
+  1.6) Ha, on a logarithmic radial mesh.  Returns (V_loc(G) grid, projector
+  table [K, 4 atoms, G]) for PlaneWavePlan.set_pseudopotential."""
+  from math import erf
+  from .pseudopotential import local, nloc
+  r = 1e-3 * np.exp(0.025 * np.arange(450))
+  vloc = -z_valence * np.array([erf(x / 0.8) for x in r]) / r
+  betas = np.stack([np.exp(-(r / 0.9) ** 2), r * np.exp(-(r / 0.9) ** 2)])
+  nat = wl.positions.shape[0]
+  g = _grid.g_vectors(wl.cell, wl.grid_sizes)
+  vol = float(abs(np.linalg.det(wl.cell)))
+  v = local.potential_local_reciprocal(wl.positions, g, [r] * nat, [vloc] * nat, [z_valence] * nat, vol)
+  table = nloc.projector_table(wl.positions, g, wl.kpts, wl.mask, [r] * nat, [betas] * nat,
+                               [np.array([0, 1])] * nat, [np.diag([0.8, 1.6])] * nat)
+  return v, table

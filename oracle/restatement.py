@@ -715,7 +715,12 @@ def plane_wave_hamiltonian(v_eff, sysm, k_index):
   d = (idx[:, None, :] - idx[None, :, :]) % np.asarray(sysm.grid)
   h = vg[d[..., 0], d[..., 1], d[..., 2]]
   tk = kinetic_operator(sysm.g_vector_grid, sysm.kpts[k_index:k_index + 1])[0][sysm.mask]
-  return h + np.diag(tk)
+  h = h + np.diag(tk)
+  if sysm.proj is not None:
+    # V_nl[G, G'] = sum_j conj(P_j(G)) P_j(G') / vol (nloc.py:143-157)
+    p = np.asarray(sysm.proj).reshape(sysm.proj.shape[0], -1, *sysm.grid)[k_index][:, sysm.mask]
+    h = h + p.conj().T @ p / sysm.vol
+  return h
 
 
 def ewald_coulomb_repulsion(positions, charges, g_vector_grid, vol, ewald_eta,

@@ -221,3 +221,78 @@ def test_set_pseudopotential_rejects_bad_shapes(tmp_path):
     plan.set_pseudopotential(vloc, table[:, :, :-1])
   plan.set_pseudopotential(None, None)      # nonlocal term removed, local table kept
   assert plan.num_proj == 0
+
+
+def _si_crystal():
+  import jrystal_gb300 as jr
+  a = 10.26
+  cell = np.array([[0, a / 2, a / 2], [a / 2, 0, a / 2], [a / 2, a / 2, 0]])
+  pos = np.array([[0, 0, 0], [0.25, 0.25, 0.25]]) @ cell
+  return jr.Crystal(charges=np.array([14.0, 14.0]), positions=pos, cell_vectors=cell,
+                    symbols=["Si", "Si"])
+
+
+def test_energy_normcons_driver(tmp_path):
+  """calc.energy_normcons (calc/calc_ground_state_energy_normcons.py:68-308):
+  valence electrons only (8 -> 4 occupied bands), energy decreasing, the
+  final terms equal the oracle's at the final parameters, Ewald with the
+  nuclear charges."""
+  import jrystal_gb300 as jr
+  d = write_set(str(tmp_path / "pp"), SI)
+  crystal = _si_crystal()
+  grid = 16
+  cfg = {"crystal": crystal, "grid_sizes": grid, "k_grid_sizes": [1, 1, 1], "cutoff_energy": 8.0,
+         "epoch": 80, "convergence_condition": 1e-12, "empty_bands": 2, "use_pseudopotential": True,
+         "pseudopotential_file_dir": d, "xc": "lda_x",
+         "optimizer_args": {"learning_rate": 0.01, "b1": 0.9, "b2": 0.99}}
+  out = jr.calc.energy_normcons(cfg)
+  h = out.total_energy_history
+  assert h[-1] < h[0]
+  p = out.params_pw
+  assert p["w_re"].shape[-1] == 6
+  mask = R.spherical_mask(crystal.cell_vectors, (grid,) * 3, 8.0)
+  kpts = R.k_vectors(crystal.cell_vectors, (1, 1, 1))
+  occ = np.zeros((1, 1, 6))
+  occ[..., :4] = 2.0
+  sysm = R.System(crystal.cell_vectors, crystal.positions, crystal.charges, (grid,) * 3, mask, kpts,
+                  occ, "lda_x")
+  _, vloc, dense, _ = nc_tables(sysm, crystal.symbols, d)
+  nc = with_pseudopotential(sysm, vloc, dense)
+  ref = R.energy_terms(p["w_re"].cpu().numpy(), p["w_im"].cpu().numpy(), nc, with_grad=False)
+  t = out.energy_terms
+  for name in ("kinetic", "external", "hartree", "xc", "total", "external_nonlocal", "external_local"):
+    assert abs(t[name] - ref[name]) < 1e-8 * max(1.0, abs(ref[name])), name
+  ew = R.nuclear_repulsion(crystal.positions, crystal.charges, crystal.cell_vectors,
+                           R.g_vectors(crystal.cell_vectors, (grid,) * 3), nc.vol, 0.1, 2e4)
+  assert abs(out.ewald - ew) < 1e-8 * abs(ew)
+  with pytest.raises(ValueError):
+    jr.calc.energy_normcons(dict(cfg, pseudopotential_file_dir=None))
+
+
+def test_band_normcons_driver_matches_full_diagonalisation(tmp_path):
+  """calc.band_normcons (calc/calc_band_structure_normcons.py:68-299) against
+  the lowest eigenvalues of the full plane-wave Hamiltonian T + v_eff + V_nl
+  at every k-point of the path, with the beta transforms of the whole path."""
+  import jrystal_gb300 as jr
+  d = write_set(str(tmp_path / "pp"), SI)
+  crystal = _si_crystal()
+  grid, nk, nb = 16, 4, 6
+  cfg = {"crystal": crystal, "grid_sizes": grid, "k_grid_sizes": [1, 1, 1], "cutoff_energy": 8.0,
+         "epoch": 300, "use_pseudopotential": True, "pseudopotential_file_dir": d, "xc": "lda_x",
+         "optimizer_args": {"learning_rate": 1e-2, "b1": 0.9, "b2": 0.99},
+         "k_path_special_points": "LGX", "num_kpoints": nk, "band_structure_empty_bands": 2,
+         "band_structure_epoch": 2500, "k_path_fine_tuning_epoch": 1500, "seed": 3,
+         "jax_enable_x64": True}
+  out = jr.calc.band_normcons(cfg)
+  assert out.eigenvalues.shape == (1, nk, nb)
+  v = out.effective_potential.cpu().numpy()
+  mask = R.spherical_mask(crystal.cell_vectors, (grid,) * 3, 8.0)
+  sysm = R.System(crystal.cell_vectors, crystal.positions, crystal.charges, (grid,) * 3, mask,
+                  out.k_path, np.ones((1, nk, nb)), "lda_x")
+  _, vloc, dense, _ = nc_tables(sysm, crystal.symbols, d, kpts=out.k_path)
+  nc = with_pseudopotential(sysm, vloc, dense)
+  exact = np.array([np.linalg.eigvalsh(R.plane_wave_hamiltonian(v, nc, k))[:nb] for k in range(nk)])
+  err = np.abs(out.eigenvalues[0] - exact)
+  print("band energies: max |error| per band", err.max(axis=0))
+  assert np.all(out.eigenvalues[0] >= exact - 1e-8)
+  assert err.max() < 1e-4

@@ -181,3 +181,21 @@ def test_oracle_nc_gradient_central_differences(tmp_path):
       fd = (R.energy_terms(*p, nc, with_grad=False)["total"] -
             R.energy_terms(*m, nc, with_grad=False)["total"]) / (2 * h)
       assert abs(fd - g[idx]) < 1e-6 * max(1.0, abs(fd)), (part, idx, fd, g[idx])
+
+
+def test_oracle_nc_rayleigh_ritz(tmp_path):
+  """With the projector term the exact eigenvectors of the full plane-wave
+  Hamiltonian (T + v + V_nl) make the band trace stationary, and their Ritz
+  values equal the exact eigenvalues."""
+  write_set(str(tmp_path), {"Si": dict(z_valence=4, dij=(0.8, 1.6))})
+  sysm = make_system(kind="si2", grid=(8, 8, 8), kgrid=(1, 1, 1), nb=3, nocc=2)
+  _, vloc, dense, _ = nc_tables(sysm, ["Si", "Si"], str(tmp_path))
+  nc = with_pseudopotential(sysm, vloc, dense)
+  v = np.real(R._ifftn(vloc))
+  hk = R.plane_wave_hamiltonian(v, nc, 0)
+  np.testing.assert_allclose(hk, hk.conj().T, atol=1e-12 * np.abs(hk).max())
+  e, u = np.linalg.eigh(hk)
+  x = u[:, :3][None, None]
+  out = R.band_trace_terms(x.real, x.imag, v, nc)
+  np.testing.assert_allclose(np.linalg.eigvalsh(out["hmat"][0, 0]), e[:3], atol=1e-10 * np.abs(e[:3]).max())
+  assert np.abs(out["grad_re"]).max() < 1e-8 and np.abs(out["grad_im"]).max() < 1e-8
