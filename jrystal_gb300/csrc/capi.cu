@@ -174,7 +174,8 @@ const char* jrg_last_error(void) { return g_err.c_str(); }
 int jrg_plan_destroy(jrg_plan* P) {
   if (!P) return JRG_OK;
   void* ptrs[] = {P->d.gidx, P->d.sph_yz, P->d.plane_x, P->d.plane_off, P->d.row_off, P->d.rows,
-                  P->d.xact, P->d.tk, P->d.tw, P->d.vext, P->d.ginv, P->d.gvec, P->d.proj};
+                  P->d.xact, P->d.tk, P->d.tw, P->d.vext, P->d.ginv, P->d.gvec, P->d.proj,
+                  P->d.rowmap};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (P->slot_begin) cudaFree(P->slot_begin);
@@ -266,7 +267,22 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
   }
   plane_off.push_back(ng);
   row_off.push_back((int)rows.size());
+  // dense map of every active row: sphere index per z, -1 off the sphere
+  std::vector<int> rowmap(rows.size() * (size_t)P->nz, -1);
+  {
+    size_t r = 0;
+    for (int e = 0; e < ng; ++e) {
+      const int x = (int)(gidx[e] / nyz), y = sph_yz[e] / P->nz, z = sph_yz[e] % P->nz;
+      const int pl = xact[x];
+      if (r < (size_t)row_off[pl]) r = row_off[pl];
+      while (rows[r] != y) ++r;    // rows of a plane are increasing, as the sphere order is
+      rowmap[r * P->nz + z] = e;
+    }
+  }
   P->nact = (int)plane_x.size();
+  P->xprune64 = P->nx == 64;
+  for (int x : plane_x)
+    if (x >= 16 && x <= 48) P->xprune64 = false;
   P->max_rows = 0;
   for (int p = 0; p < P->nact; ++p) P->max_rows = std::max(P->max_rows, row_off[p + 1] - row_off[p]);
   // kinetic table |G+k|^2/2
@@ -314,7 +330,7 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
 #define UP(field, vec) \
   if (!rc) rc = up((void**)&P->d.field, vec.data(), vec.size() * sizeof(vec[0]));
   UP(gidx, gidx) UP(sph_yz, sph_yz) UP(plane_x, plane_x) UP(plane_off, plane_off)
-  UP(row_off, row_off) UP(rows, rows) UP(xact, xact) UP(tk, tk)
+  UP(row_off, row_off) UP(rows, rows) UP(xact, xact) UP(tk, tk) UP(rowmap, rowmap)
 #undef UP
   // twiddles (host, double precision): x, y, z tables
   if (!rc) {

@@ -154,6 +154,31 @@ template <int N, int DIR, typename C> __host__ __device__ __forceinline__ void d
   }
 }
 
+// 8-point DFT of v with v[2..5] = 0 (the x lines of a 64^3 plane slab whose
+// active planes lie in x <= 15 and x >= 49): the stages of dft<8> with the
+// additions of the known zeros left out.
+template <int DIR, typename C> __host__ __device__ __forceinline__ void dft8_in0167(C (&v)[8]) {
+  // even and odd halves (v0, 0, 0, v6) and (v1, 0, 0, v7) through dft<4>'s stages
+  const C te = twiddle_mul<DIR, 1, 4>(v[6]);
+  const C to = twiddle_mul<DIR, 1, 4>(v[7]);
+  C y[2][4];
+  y[0][0] = cadd(v[0], v[6]);
+  y[0][2] = csub(v[0], v[6]);
+  y[0][1] = csub(v[0], te);
+  y[0][3] = cadd(v[0], te);
+  y[1][0] = cadd(v[1], v[7]);
+  y[1][2] = csub(v[1], v[7]);
+  y[1][1] = csub(v[1], to);
+  y[1][3] = cadd(v[1], to);
+  sfor<4>([&](auto kk) {
+    constexpr int k = kk.value;
+    C w0 = y[0][k], w1 = twiddle_mul<DIR, k, 8>(y[1][k]);
+    dft2<DIR>(w0, w1);
+    v[k] = w0;
+    v[k + 4] = w1;
+  });
+}
+
 // Split of a line length into N1 values per thread and N2 threads per line.
 template <int N> struct Split;
 template <> struct Split<16> { static constexpr int N1 = 4, N2 = 4; };
@@ -183,6 +208,23 @@ __host__ __device__ __forceinline__ void line_step_a(C (&v)[Split<N>::N1], const
       t = cmul(t, w);
     }
     ex[(k1 * N2 + j2) * L + l] = t;
+  });
+}
+
+// line_step_a for N = 64 with the thread's inputs v[2..5] known to be zero
+template <int DIR, typename C>
+__host__ __device__ __forceinline__ void line_step_a_pruned64(C (&v)[8], const C* __restrict__ tw, int j2,
+                                                     C* ex, int L, int l) {
+  dft8_in0167<DIR>(v);
+  sfor<8>([&](auto kk) {
+    constexpr int k1 = kk.value;
+    C t = v[k1];
+    if constexpr (k1 > 0) {
+      C w = tw[j2 * k1];
+      if (DIR > 0) w.y = -w.y;
+      t = cmul(t, w);
+    }
+    ex[(k1 * 8 + j2) * L + l] = t;
   });
 }
 

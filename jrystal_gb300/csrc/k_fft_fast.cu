@@ -12,6 +12,8 @@
 // buffer keeps the column accesses free of bank conflicts.
 #include "fast_dispatch.h"
 #include "fft_reg.cuh"
+#include <cstdlib>
+
 #include "plan.h"
 
 namespace jrg {
@@ -91,6 +93,85 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere(
   }
 }
 
+// sphere -> y,z-transformed active planes, up to bpc bands per CTA: the
+// gather of band i+1 (zero-filling cp.async through the dense row map: sphere
+// values and zeros for the rest of every active row) runs under the transforms
+// of band i; inactive rows of both [z][y] buffers stay zero.
+template <typename R, int N>
+__global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere_mb(
+    const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ planes, const int* __restrict__ row_off,
+    const int* __restrict__ rows, const int* __restrict__ rowmap, const C_t<R>* __restrict__ tw_g,
+    int ng, int nact, int nbands, int bpc) {
+  using C = C_t<R>;
+  constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2, P = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* A0 = tw + N;                                     // two [z][y] buffers, pitch P
+  C* ex = A0 + 2 * N * P;                             // exchange, N*N
+  int* srows = reinterpret_cast<int*>(ex + N * N);    // [N]
+  int* smap = srows + N;                              // [nr][N]
+  const int p = blockIdx.x, tid = threadIdx.x;
+  const int b_begin = blockIdx.y * bpc, b_end = min(nbands, b_begin + bpc);
+  const int r0 = row_off[p], nr = row_off[p + 1] - r0;
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = tw_g[i];
+  for (int i = tid; i < nr; i += blockDim.x) srows[i] = rows[r0 + i];
+  for (int i = tid; i < nr * N; i += blockDim.x) smap[i] = rowmap[(size_t)r0 * N + i];
+  const C z0 = czero<C>();
+  for (int i = tid; i < 2 * N * P; i += blockDim.x) A0[i] = z0;
+  __syncthreads();
+  auto gather = [&](C* A, int band) {
+    const C* cb = coef + (size_t)band * ng;
+    for (int i = tid; i < nr * N; i += blockDim.x) {
+      const int r = i / N, z = i - r * N;
+      const int e = smap[i];
+      cp_async_zfill<sizeof(C)>(&A[z * P + srows[r]], e >= 0 ? cb + e : cb, e >= 0);
+    }
+    cp_async_commit();
+  };
+  if (b_begin < b_end) gather(A0, b_begin);
+  C v[N1];
+  for (int band = b_begin, it = 0; band < b_end; ++band, ++it) {
+    C* A = A0 + (it & 1) * (N * P);
+    if (band + 1 < b_end) {
+      gather(A0 + ((it + 1) & 1) * (N * P), band + 1);   // last read before the previous exchange
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    // z transforms of the active rows (L = nr lines)
+    {
+      const bool act = tid < nr * N2;
+      const int l = act ? tid % nr : 0, j2 = act ? tid / nr : 0;
+      const int y = srows[l];
+      if (act) {
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[(N2 * j1 + j2) * P + y];
+        reg::line_step_a<N, +1>(v, tw, j2, ex, nr, l);
+      }
+      __syncthreads();
+      if (act) {
+        reg::line_step_b<N, +1>(v, j2, ex, nr, l);
+#pragma unroll
+        for (int j = 0; j < N1; ++j) A[(N2 * j + j2) * P + y] = v[j];
+      }
+      __syncthreads();
+    }
+    // y transforms of all z columns (L = N lines), straight to global memory
+    {
+      const int z = tid % N, j2 = tid / N;
+#pragma unroll
+      for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[z * P + N2 * j1 + j2];
+      reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
+      __syncthreads();
+      reg::line_step_b<N, +1>(v, j2, ex, N, z);
+      C* out = planes + ((size_t)band * nact + p) * (N * N);
+#pragma unroll
+      for (int j = 0; j < N1; ++j) out[(N2 * j + j2) * N + z] = v[j];
+    }
+  }
+}
+
 // Rows [nact][N] of band b for line y go to shared memory with cp.async one
 // band ahead of the transforms (PF, adjoint pass), so that the loads of the
 // next band are in flight while the current one is transformed.
@@ -117,7 +198,8 @@ __device__ __forceinline__ void prefetch_row(const C_t<R>* __restrict__ planes, 
 // inverse x transform + occupation-weighted |psi|^2 of a band group (one
 // transform per band: the row prefetch of the adjoint pass measured slower
 // here, 0.30 vs 0.25 ms on the 64^3 Si8 cell)
-template <typename R, int N>
+// PR (N = 64 only): the thread's inputs v[2..5] (x = 16..47) are known zero
+template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_density(
     const C_t<R>* __restrict__ planes, R* __restrict__ rho_part, const double* __restrict__ wband,
     double wscale, int band0, int nband, int bands_per_group, const int* __restrict__ xact,
@@ -148,9 +230,13 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
     const R w = (R)(wband[band0 + b] * wscale);
     const C* src = planes + (size_t)b * nact * (N * N) + y * N + z;
 #pragma unroll
-    for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : src[(size_t)slot[j1] * (N * N)];
+    for (int j1 = 0; j1 < N1; ++j1) {
+      if (PR && j1 >= 2 && j1 <= 5) continue;
+      v[j1] = slot[j1] < 0 ? z0 : src[(size_t)slot[j1] * (N * N)];
+    }
     C* ex = parity ? ex1 : ex0;
-    reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
+    if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex, N, z);
+    else reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
     __syncthreads();
     reg::line_step_b<N, +1>(v, j2, ex, N, z);
 #pragma unroll
@@ -163,7 +249,9 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
 
 // adjoint line pass: inverse x transform, times V(r), forward x transform,
 // active planes written back in place
-template <typename R, int N, bool PF>
+// PR (N = 64 only): x = 16..47 (the thread's v[2..5]) are known zero on input
+// and not written back
+template <typename R, int N, bool PF, bool PR>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_apply_v(
     C_t<R>* __restrict__ planes, const R* __restrict__ vr, int nband, int bands_per_group,
     const int* __restrict__ xact, const C_t<R>* __restrict__ tw_g, int nact) {
@@ -204,12 +292,19 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
       __syncthreads();
       const C* src = rowbuf + parity * nact * N + z;
 #pragma unroll
-      for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : src[slot[j1] * N];
+      for (int j1 = 0; j1 < N1; ++j1) {
+        if (PR && j1 >= 2 && j1 <= 5) continue;
+        v[j1] = slot[j1] < 0 ? z0 : src[slot[j1] * N];
+      }
     } else {
 #pragma unroll
-      for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : base[(size_t)slot[j1] * (N * N)];
+      for (int j1 = 0; j1 < N1; ++j1) {
+        if (PR && j1 >= 2 && j1 <= 5) continue;
+        v[j1] = slot[j1] < 0 ? z0 : base[(size_t)slot[j1] * (N * N)];
+      }
     }
-    reg::line_step_a<N, +1>(v, tw, j2, ex0, N, z);
+    if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex0, N, z);
+    else reg::line_step_a<N, +1>(v, tw, j2, ex0, N, z);
     __syncthreads();
     reg::line_step_b<N, +1>(v, j2, ex0, N, z);
 #pragma unroll
@@ -218,8 +313,10 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
     __syncthreads();
     reg::line_step_b<N, -1>(v, j2, ex1, N, z);
 #pragma unroll
-    for (int j = 0; j < N1; ++j)
+    for (int j = 0; j < N1; ++j) {
+      if (PR && j >= 2 && j <= 5) continue;   // the outputs left out are never formed
       if (slot[j] >= 0) base[(size_t)slot[j] * (N * N)] = v[j];
+    }
   }
 }
 
@@ -377,6 +474,9 @@ __global__ void __launch_bounds__(threads_for<N>()) k_line_dense(const C_t<R>* _
 template <typename R, int N> size_t plane_smem() {
   return sizeof(C_t<R>) * (size_t)(N + N * (N + 1) + N * N) + sizeof(int) * (N + 1);
 }
+template <typename R, int N> size_t plane_mb_smem(int max_rows) {
+  return sizeof(C_t<R>) * (size_t)(N + 2 * N * (N + 1) + N * N) + sizeof(int) * (size_t)N * (1 + max_rows);
+}
 template <typename R, int N> size_t line_smem() {
   return sizeof(C_t<R>) * (size_t)(N + 2 * N * N) + sizeof(int) * N;
 }
@@ -412,6 +512,56 @@ template <typename K> static int prep(K kernel, size_t bytes) {
 
 static bool g_line_prefetch = true;   // cp.async row prefetch in the adjoint line kernel
 
+// bands per CTA of the inverse plane pass (1: one CTA per (plane, band));
+// JRG_PLANE_BANDS overrides the default for measurements.  At the 64^3 Si8
+// cell: 1 -> 0.253 ms, 4 -> 0.246, 8 -> 0.235, 16 -> 0.239 (best step time,
+// 522.5 vs 512.9 evals/s), 32 -> 0.260.  The same staging in the forward
+// plane pass was slower (0.33 vs 0.28 ms: two CTAs per SM instead of three).
+static int plane_bands_per_cta() {
+  static int v = [] {
+    const char* e = std::getenv("JRG_PLANE_BANDS");
+    const int x = e ? std::atoi(e) : 16;
+    return x < 1 ? 1 : (x > 64 ? 64 : x);
+  }();
+  return v;
+}
+
+template <typename R, int N, bool PR>
+static int line_density_launch(const jrg_plan* P, const Args& a, const C_t<R>* tw, cudaStream_t st) {
+  using C = C_t<R>;
+  constexpr int T = threads_for<N>();
+  int rc;
+  const size_t sm = line_smem<R, N>();
+  if ((rc = prep(k_line_density<R, N, PR>, sm)) <= 0) return rc;
+  const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
+  k_line_density<R, N, PR><<<dim3(N, ngroups), T, sm, st>>>(
+      reinterpret_cast<const C*>(a.in), reinterpret_cast<R*>(a.out), a.w, a.wscale, a.band0,
+      a.nbands, a.bands_per_group, P->d.xact, tw, P->nact);
+  FAST_LAUNCHED("fast::k_line_density");
+}
+
+template <typename R, int N, bool PR>
+static int line_apply_v_launch(const jrg_plan* P, const Args& a, const C_t<R>* tw, cudaStream_t st) {
+  using C = C_t<R>;
+  constexpr int T = threads_for<N>();
+  int rc;
+  const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
+  const size_t smp = line_pf_smem<R, N>(P->nact);
+  if (g_line_prefetch && (long long)smp <= optin_smem()) {
+    if ((rc = prep(k_line_apply_v<R, N, true, PR>, smp)) <= 0) return rc;
+    k_line_apply_v<R, N, true, PR><<<dim3(N, ngroups), T, smp, st>>>(
+        reinterpret_cast<C*>(a.out), reinterpret_cast<const R*>(a.aux), a.nbands, a.bands_per_group,
+        P->d.xact, tw, P->nact);
+    FAST_LAUNCHED("fast::k_line_apply_v");
+  }
+  const size_t sm = line_smem<R, N>();
+  if ((rc = prep(k_line_apply_v<R, N, false, PR>, sm)) <= 0) return rc;
+  k_line_apply_v<R, N, false, PR><<<dim3(N, ngroups), T, sm, st>>>(
+      reinterpret_cast<C*>(a.out), reinterpret_cast<const R*>(a.aux), a.nbands, a.bands_per_group,
+      P->d.xact, tw, P->nact);
+  FAST_LAUNCHED("fast::k_line_apply_v");
+}
+
 template <typename R, int N>
 static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
   using C = C_t<R>;
@@ -420,6 +570,15 @@ static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
   int rc;
   switch (op) {
     case OP_PLANE_INV: {
+      const int bpc = plane_bands_per_cta();
+      const size_t smb = plane_mb_smem<R, N>(P->max_rows);
+      if (bpc > 1 && (long long)smb <= optin_smem()) {
+        if ((rc = prep(k_plane_inv_sphere_mb<R, N>, smb)) <= 0) return rc;
+        k_plane_inv_sphere_mb<R, N><<<dim3(P->nact, (a.nbands + bpc - 1) / bpc), T, smb, st>>>(
+            reinterpret_cast<const C*>(a.in), reinterpret_cast<C*>(a.out), P->d.row_off, P->d.rows,
+            P->d.rowmap, tw, P->ng, P->nact, a.nbands, bpc);
+        FAST_LAUNCHED("fast::k_plane_inv_sphere_mb");
+      }
       const size_t sm = plane_smem<R, N>();
       if ((rc = prep(k_plane_inv_sphere<R, N>, sm)) <= 0) return rc;
       k_plane_inv_sphere<R, N><<<dim3(P->nact, a.nbands), T, sm, st>>>(
@@ -428,30 +587,16 @@ static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
       FAST_LAUNCHED("fast::k_plane_inv_sphere");
     }
     case OP_LINE_DENSITY: {
-      const size_t sm = line_smem<R, N>();
-      if ((rc = prep(k_line_density<R, N>, sm)) <= 0) return rc;
-      const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
-      k_line_density<R, N><<<dim3(N, ngroups), T, sm, st>>>(
-          reinterpret_cast<const C*>(a.in), reinterpret_cast<R*>(a.out), a.w, a.wscale, a.band0,
-          a.nbands, a.bands_per_group, P->d.xact, tw, P->nact);
-      FAST_LAUNCHED("fast::k_line_density");
+      if constexpr (N == 64) {
+        if (P->xprune64) return line_density_launch<R, N, true>(P, a, tw, st);
+      }
+      return line_density_launch<R, N, false>(P, a, tw, st);
     }
     case OP_LINE_APPLY_V: {
-      const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
-      const size_t smp = line_pf_smem<R, N>(P->nact);
-      if (g_line_prefetch && (long long)smp <= optin_smem()) {
-        if ((rc = prep(k_line_apply_v<R, N, true>, smp)) <= 0) return rc;
-        k_line_apply_v<R, N, true><<<dim3(N, ngroups), T, smp, st>>>(
-            reinterpret_cast<C*>(a.out), reinterpret_cast<const R*>(a.aux), a.nbands,
-            a.bands_per_group, P->d.xact, tw, P->nact);
-        FAST_LAUNCHED("fast::k_line_apply_v");
+      if constexpr (N == 64) {
+        if (P->xprune64) return line_apply_v_launch<R, N, true>(P, a, tw, st);
       }
-      const size_t sm = line_smem<R, N>();
-      if ((rc = prep(k_line_apply_v<R, N, false>, sm)) <= 0) return rc;
-      k_line_apply_v<R, N, false><<<dim3(N, ngroups), T, sm, st>>>(
-          reinterpret_cast<C*>(a.out), reinterpret_cast<const R*>(a.aux), a.nbands,
-          a.bands_per_group, P->d.xact, tw, P->nact);
-      FAST_LAUNCHED("fast::k_line_apply_v");
+      return line_apply_v_launch<R, N, false>(P, a, tw, st);
     }
     default: {
       const size_t sm = plane_smem<R, N>();

@@ -25,16 +25,6 @@ constexpr int kJT = 32;    // largest projector tile of the projection
 constexpr int kMinG = 256;   // fewest sphere points per projection split
 template <typename R> __host__ __device__ constexpr int tg_of() { return sizeof(R) == 4 ? 32 : 16; }
 template <typename R> __host__ __device__ constexpr int jc_of() { return sizeof(R) == 4 ? 32 : 16; }
-// cp.async of BYTES bytes into shared memory, zero-filled when !pred (no
-// bytes are read then; gmem must still be a valid address)
-template <int BYTES>
-__device__ __forceinline__ void cp_async_zfill(void* smem, const void* gmem, bool pred) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  const int n = pred ? BYTES : 0;
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(sa), "l"(gmem), "n"(BYTES),
-               "r"(n) : "memory");
-}
-
 constexpr int kReduceThreads = 128;   // F entries per reduction CTA
 }  // namespace
 

@@ -37,6 +37,7 @@ struct PlanTables {
   int* plane_off = nullptr;   // [nact+1] sphere offsets per plane
   int* row_off = nullptr;     // [nact+1] offsets into rows
   int* rows = nullptr;        // active y rows per plane
+  int* rowmap = nullptr;      // [total active rows][nz]: sphere index of (row, z), or -1
   int* xact = nullptr;        // [nx] active-plane slot of x, or -1
   double* tk = nullptr;       // [nk][ng] |G+k|^2 / 2
   void* tw = nullptr;         // twiddles: x table, y table, z table (C_t<R>)
@@ -94,6 +95,7 @@ struct jrg_plan {
   int ns, nk, nb, ng;
   int nact;                 // active x planes
   int max_rows;             // max active rows in a plane
+  bool xprune64 = false;    // 64^3 grid with every active x plane in x <= 15 or x >= 49
   double cell[9], recip[9], vol;
   std::vector<double> pos, charge, kpts;
   int xc;
