@@ -97,7 +97,9 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere(
 // gather of band i+1 (zero-filling cp.async through the dense row map: sphere
 // values and zeros for the rest of every active row) runs under the transforms
 // of band i; inactive rows of both [z][y] buffers stay zero.
-template <typename R, int N>
+// PR (N = 64 only): active rows y and sphere z lie outside 16..48, so the
+// inputs v[2..5] of the z and y transforms are zero
+template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere_mb(
     const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ planes, const int* __restrict__ row_off,
     const int* __restrict__ rows, const int* __restrict__ rowmap, const C_t<R>* __restrict__ tw_g,
@@ -146,8 +148,12 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere_mb(
       const int y = srows[l];
       if (act) {
 #pragma unroll
-        for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[(N2 * j1 + j2) * P + y];
-        reg::line_step_a<N, +1>(v, tw, j2, ex, nr, l);
+        for (int j1 = 0; j1 < N1; ++j1) {
+          if (PR && j1 >= 2 && j1 <= 5) continue;
+          v[j1] = A[(N2 * j1 + j2) * P + y];
+        }
+        if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex, nr, l);
+        else reg::line_step_a<N, +1>(v, tw, j2, ex, nr, l);
       }
       __syncthreads();
       if (act) {
@@ -161,8 +167,12 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere_mb(
     {
       const int z = tid % N, j2 = tid / N;
 #pragma unroll
-      for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[z * P + N2 * j1 + j2];
-      reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
+      for (int j1 = 0; j1 < N1; ++j1) {
+        if (PR && j1 >= 2 && j1 <= 5) continue;
+        v[j1] = A[z * P + N2 * j1 + j2];
+      }
+      if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex, N, z);
+      else reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
       __syncthreads();
       reg::line_step_b<N, +1>(v, j2, ex, N, z);
       C* out = planes + ((size_t)band * nact + p) * (N * N);
@@ -322,7 +332,9 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
 
 // forward: y, z transforms of an active plane, sphere gather and gradient
 //   g[b][e] = f_b * (tk[k][e] * c[b][e] + scale * FFT(V psi_b)[e])
-template <typename R, int N>
+// PR (N = 64 only): only rows y and sphere z outside 16..48 are needed, so
+// the y and z transforms do not form the outputs v[2..5]
+template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
     const C_t<R>* __restrict__ planes, const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ gcoef,
     const double* __restrict__ wband, const double* __restrict__ tk, int nb_per_k, int band0,
@@ -352,7 +364,10 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
     __syncthreads();
     reg::line_step_b<N, -1>(v, j2, ex, N, z);
 #pragma unroll
-    for (int j = 0; j < N1; ++j) A[z * P + N2 * j + j2] = v[j];
+    for (int j = 0; j < N1; ++j) {
+      if (PR && j >= 2 && j <= 5) continue;   // inactive rows are never read
+      A[z * P + N2 * j + j2] = v[j];
+    }
     __syncthreads();
   }
   // z transforms of the active rows
@@ -369,7 +384,10 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
     if (act) {
       reg::line_step_b<N, -1>(v, j2, ex, nr, l);
 #pragma unroll
-      for (int j = 0; j < N1; ++j) A[(N2 * j + j2) * P + y] = v[j];
+      for (int j = 0; j < N1; ++j) {
+        if (PR && j >= 2 && j <= 5) continue;   // off-sphere z are never gathered
+        A[(N2 * j + j2) * P + y] = v[j];
+      }
     }
     __syncthreads();
   }
@@ -527,6 +545,33 @@ static int plane_bands_per_cta() {
 }
 
 template <typename R, int N, bool PR>
+static int plane_inv_mb_launch(const jrg_plan* P, const Args& a, const C_t<R>* tw, int bpc, size_t smb,
+                               cudaStream_t st) {
+  using C = C_t<R>;
+  constexpr int T = threads_for<N>();
+  int rc;
+  if ((rc = prep(k_plane_inv_sphere_mb<R, N, PR>, smb)) <= 0) return rc;
+  k_plane_inv_sphere_mb<R, N, PR><<<dim3(P->nact, (a.nbands + bpc - 1) / bpc), T, smb, st>>>(
+      reinterpret_cast<const C*>(a.in), reinterpret_cast<C*>(a.out), P->d.row_off, P->d.rows,
+      P->d.rowmap, tw, P->ng, P->nact, a.nbands, bpc);
+  FAST_LAUNCHED("fast::k_plane_inv_sphere_mb");
+}
+
+template <typename R, int N, bool PR>
+static int plane_fwd_launch(const jrg_plan* P, const Args& a, const C_t<R>* tw, cudaStream_t st) {
+  using C = C_t<R>;
+  constexpr int T = threads_for<N>();
+  int rc;
+  const size_t sm = plane_smem<R, N>();
+  if ((rc = prep(k_plane_fwd_sphere<R, N, PR>, sm)) <= 0) return rc;
+  k_plane_fwd_sphere<R, N, PR><<<dim3(P->nact, a.nbands), T, sm, st>>>(
+      reinterpret_cast<const C*>(a.in), reinterpret_cast<const C*>(a.aux), reinterpret_cast<C*>(a.out),
+      a.w, P->d.tk, P->nb, a.band0, P->d.plane_off, P->d.sph_yz, P->d.row_off, P->d.rows, tw, P->ng,
+      P->nact, P->nk, a.wscale);
+  FAST_LAUNCHED("fast::k_plane_fwd_sphere");
+}
+
+template <typename R, int N, bool PR>
 static int line_density_launch(const jrg_plan* P, const Args& a, const C_t<R>* tw, cudaStream_t st) {
   using C = C_t<R>;
   constexpr int T = threads_for<N>();
@@ -573,11 +618,10 @@ static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
       const int bpc = plane_bands_per_cta();
       const size_t smb = plane_mb_smem<R, N>(P->max_rows);
       if (bpc > 1 && (long long)smb <= optin_smem()) {
-        if ((rc = prep(k_plane_inv_sphere_mb<R, N>, smb)) <= 0) return rc;
-        k_plane_inv_sphere_mb<R, N><<<dim3(P->nact, (a.nbands + bpc - 1) / bpc), T, smb, st>>>(
-            reinterpret_cast<const C*>(a.in), reinterpret_cast<C*>(a.out), P->d.row_off, P->d.rows,
-            P->d.rowmap, tw, P->ng, P->nact, a.nbands, bpc);
-        FAST_LAUNCHED("fast::k_plane_inv_sphere_mb");
+        if constexpr (N == 64) {
+          if (P->yzprune64) return plane_inv_mb_launch<R, N, true>(P, a, tw, bpc, smb, st);
+        }
+        return plane_inv_mb_launch<R, N, false>(P, a, tw, bpc, smb, st);
       }
       const size_t sm = plane_smem<R, N>();
       if ((rc = prep(k_plane_inv_sphere<R, N>, sm)) <= 0) return rc;
@@ -599,13 +643,10 @@ static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
       return line_apply_v_launch<R, N, false>(P, a, tw, st);
     }
     default: {
-      const size_t sm = plane_smem<R, N>();
-      if ((rc = prep(k_plane_fwd_sphere<R, N>, sm)) <= 0) return rc;
-      k_plane_fwd_sphere<R, N><<<dim3(P->nact, a.nbands), T, sm, st>>>(
-          reinterpret_cast<const C*>(a.in), reinterpret_cast<const C*>(a.aux),
-          reinterpret_cast<C*>(a.out), a.w, P->d.tk, P->nb, a.band0, P->d.plane_off, P->d.sph_yz,
-          P->d.row_off, P->d.rows, tw, P->ng, P->nact, P->nk, a.wscale);
-      FAST_LAUNCHED("fast::k_plane_fwd_sphere");
+      if constexpr (N == 64) {
+        if (P->yzprune64) return plane_fwd_launch<R, N, true>(P, a, tw, st);
+      }
+      return plane_fwd_launch<R, N, false>(P, a, tw, st);
     }
   }
 }

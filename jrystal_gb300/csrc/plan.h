@@ -96,6 +96,7 @@ struct jrg_plan {
   int nact;                 // active x planes
   int max_rows;             // max active rows in a plane
   bool xprune64 = false;    // 64^3 grid with every active x plane in x <= 15 or x >= 49
+  bool yzprune64 = false;   // 64^3 grid with every active row y and sphere z outside 16..48
   double cell[9], recip[9], vol;
   std::vector<double> pos, charge, kpts;
   int xc;
