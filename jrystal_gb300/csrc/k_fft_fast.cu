@@ -235,14 +235,28 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
   const int b_end = min(nband, b_begin + bands_per_group);
   const C z0 = czero<C>();
   C v[N1];
+  // PR: the four non-zero inputs of the next band are loaded while the
+  // current band is transformed
+  C nxt[4];
+  auto load4 = [&](int b) {
+    const C* src = planes + (size_t)b * nact * (N * N) + y * N + z;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j1 = q < 2 ? q : q + 4;
+      nxt[q] = slot[j1] < 0 ? z0 : src[(size_t)slot[j1] * (N * N)];
+    }
+  };
+  if (PR && b_begin < b_end) load4(b_begin);
   int parity = 0;
   for (int b = b_begin; b < b_end; ++b, parity ^= 1) {
     const R w = (R)(wband[band0 + b] * wscale);
-    const C* src = planes + (size_t)b * nact * (N * N) + y * N + z;
+    if constexpr (PR) {
+      v[0] = nxt[0]; v[1] = nxt[1]; v[6] = nxt[2]; v[7] = nxt[3];
+      if (b + 1 < b_end) load4(b + 1);
+    } else {
+      const C* src = planes + (size_t)b * nact * (N * N) + y * N + z;
 #pragma unroll
-    for (int j1 = 0; j1 < N1; ++j1) {
-      if (PR && j1 >= 2 && j1 <= 5) continue;
-      v[j1] = slot[j1] < 0 ? z0 : src[(size_t)slot[j1] * (N * N)];
+      for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : src[(size_t)slot[j1] * (N * N)];
     }
     C* ex = parity ? ex1 : ex0;
     if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex, N, z);
@@ -615,7 +629,11 @@ static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
   int rc;
   switch (op) {
     case OP_PLANE_INV: {
-      const int bpc = plane_bands_per_cta();
+      // several bands per CTA only while the grid still fills the GPU twice
+      // over at two CTAs per SM (152 SMs); a smaller call runs one band per CTA
+      int bpc = plane_bands_per_cta();
+      while (bpc > 1 && (long long)a.nbands * P->nact < 2LL * 2 * 152 * bpc) bpc /= 2;
+      if (bpc < 4) bpc = 1;
       const size_t smb = plane_mb_smem<R, N>(P->max_rows);
       if (bpc > 1 && (long long)smb <= optin_smem()) {
         if constexpr (N == 64) {
