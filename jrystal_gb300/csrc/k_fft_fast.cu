@@ -303,10 +303,26 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
   }
   const C z0 = czero<C>();
   C v[N1];
+  // RP (pruned, no row buffer): the four non-zero inputs of the next band are
+  // loaded into registers while the current band is transformed
+  constexpr bool RP = PR && !PF;
+  C nxt[4];
+  auto load4 = [&](int b) {
+    const C* src = planes + (size_t)b * nact * (N * N) + y * N + z;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j1 = q < 2 ? q : q + 4;
+      nxt[q] = slot[j1] < 0 ? z0 : src[(size_t)slot[j1] * (N * N)];
+    }
+  };
+  if (RP && b_begin < b_end) load4(b_begin);
   int parity = 0;
   for (int b = b_begin; b < b_end; ++b, parity ^= 1) {
     C* base = planes + (size_t)b * nact * (N * N) + y * N + z;
-    if constexpr (PF) {
+    if constexpr (RP) {
+      v[0] = nxt[0]; v[1] = nxt[1]; v[6] = nxt[2]; v[7] = nxt[3];
+      if (b + 1 < b_end) load4(b + 1);
+    } else if constexpr (PF) {
       if (b + 1 < b_end) {
         prefetch_row<R, N>(planes, rowbuf + (parity ^ 1) * nact * N, b + 1, y, nact);
         cp_async_wait<1>();
@@ -544,6 +560,16 @@ template <typename K> static int prep(K kernel, size_t bytes) {
 
 static bool g_line_prefetch = true;   // cp.async row prefetch in the adjoint line kernel
 
+// the pruned adjoint line kernel prefetches the next band into registers
+// unless JRG_LINE_ROWBUF=1 selects the shared-memory row buffer (measurements)
+static bool line_rowbuf() {
+  static bool v = [] {
+    const char* e = std::getenv("JRG_LINE_ROWBUF");
+    return e && std::atoi(e) != 0;
+  }();
+  return v;
+}
+
 // bands per CTA of the inverse plane pass (1: one CTA per (plane, band));
 // JRG_PLANE_BANDS overrides the default for measurements.  At the 64^3 Si8
 // cell: 1 -> 0.253 ms, 4 -> 0.246, 8 -> 0.235, 16 -> 0.239 (best step time,
@@ -606,7 +632,7 @@ static int line_apply_v_launch(const jrg_plan* P, const Args& a, const C_t<R>* t
   int rc;
   const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
   const size_t smp = line_pf_smem<R, N>(P->nact);
-  if (g_line_prefetch && (long long)smp <= optin_smem()) {
+  if (g_line_prefetch && !(PR && !line_rowbuf()) && (long long)smp <= optin_smem()) {
     if ((rc = prep(k_line_apply_v<R, N, true, PR>, smp)) <= 0) return rc;
     k_line_apply_v<R, N, true, PR><<<dim3(N, ngroups), T, smp, st>>>(
         reinterpret_cast<C*>(a.out), reinterpret_cast<const R*>(a.aux), a.nbands, a.bands_per_group,
