@@ -83,8 +83,8 @@ bool factor_axis(int n, FftAxis* ax) {
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // energy slot layout
-constexpr int kRecipBlocks = 256;
-constexpr int kXcBlocks = 256;
+constexpr int kRecipBlocks = 256;   // CTAs (and energy slots) of the reciprocal-space terms
+constexpr int kXcBlocks = 256;      // CTAs (and energy slots) of the xc terms (1024: 0.093 vs 0.081 ms)
 constexpr int kEwaldBlocks = 512;
 
 static int csize(int prec) { return prec == 64 ? 16 : 8; }
@@ -946,14 +946,16 @@ static int energy_grad_pipelined(const jrg_plan* P, const void* w_re, const void
                                          kXcBlocks, P->ngrid, P->xc, P->vol / N, st))) {
       return rc;
     }
-    if ((rc = sum_energy_slots(P, slots, energies, ws, st))) return rc;
   }
-  if (!adam && !g_re && !g_im) return JRG_OK;
+  // the energy sums feed only the energies output: they run after the adjoint
+  // halves, off the path between the two forks
+  if (!adam && !g_re && !g_im) return sum_energy_slots(P, slots, energies, ws, st);
   if (!adam && (!g_re || !g_im)) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
   if ((rc = fork())) return rc;
   if ((rc = phase_adjoint_range<R>(P, occ, g_re, g_im, ws, 0, ka, st, adam))) return rc;
   if ((rc = phase_adjoint_range<R>(P, occ, g_re, g_im, ws, ka, kb, P->side, adam))) return rc;
-  return join();
+  if ((rc = join())) return rc;
+  return sum_energy_slots(P, slots, energies, ws, st);
 }
 
 template <typename R>
