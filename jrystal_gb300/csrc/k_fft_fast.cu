@@ -441,6 +441,94 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
   }
 }
 
+// forward plane pass, up to bpc bands per CTA: each thread loads its eight
+// values of the next band's plane into registers while the current band is
+// transformed, gathered and weighted (PR as in k_plane_fwd_sphere).
+template <typename R, int N, bool PR>
+__global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere_rp(
+    const C_t<R>* __restrict__ planes, const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ gcoef,
+    const double* __restrict__ wband, const double* __restrict__ tk, int nb_per_k, int band0,
+    const int* __restrict__ plane_off, const int* __restrict__ sph_yz, const int* __restrict__ row_off,
+    const int* __restrict__ rows, const C_t<R>* __restrict__ tw_g, int ng, int nact, int nk,
+    double scale, int nbands, int bpc) {
+  using C = C_t<R>;
+  constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2, P = N + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw = reinterpret_cast<C*>(smem_raw);
+  C* A = tw + N;
+  C* ex = A + N * P;
+  int* srows = reinterpret_cast<int*>(ex + N * N);
+  const int p = blockIdx.x, tid = threadIdx.x;
+  const int b_begin = blockIdx.y * bpc, b_end = min(nbands, b_begin + bpc);
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = tw_g[i];
+  const int r0 = row_off[p], nr = row_off[p + 1] - r0;
+  for (int i = tid; i < nr; i += blockDim.x) srows[i] = rows[r0 + i];
+  const int zc = tid % N, jc = tid / N;   // column z and thread index j2 of the y transforms
+  C nxt[N1];
+  auto load = [&](int band) {
+    const C* in = planes + ((size_t)band * nact + p) * (N * N) + zc;
+#pragma unroll
+    for (int j1 = 0; j1 < N1; ++j1) nxt[j1] = in[(N2 * j1 + jc) * N];
+  };
+  if (b_begin < b_end) load(b_begin);
+  __syncthreads();
+  const R sc = (R)scale;
+  C v[N1];
+  for (int band = b_begin; band < b_end; ++band) {
+    // y transforms of all z columns
+#pragma unroll
+    for (int j1 = 0; j1 < N1; ++j1) v[j1] = nxt[j1];
+    if (band + 1 < b_end) load(band + 1);
+    reg::line_step_a<N, -1>(v, tw, jc, ex, N, zc);
+    __syncthreads();
+    reg::line_step_b<N, -1>(v, jc, ex, N, zc);
+#pragma unroll
+    for (int j = 0; j < N1; ++j) {
+      if (PR && j >= 2 && j <= 5) continue;   // inactive rows are never read
+      A[zc * P + N2 * j + jc] = v[j];
+    }
+    __syncthreads();
+    // z transforms of the active rows
+    {
+      const bool act = tid < nr * N2;
+      const int l = act ? tid % nr : 0, j2 = act ? tid / nr : 0;
+      const int y = srows[l];
+      if (act) {
+#pragma unroll
+        for (int j1 = 0; j1 < N1; ++j1) v[j1] = A[(N2 * j1 + j2) * P + y];
+        reg::line_step_a<N, -1>(v, tw, j2, ex, nr, l);
+      }
+      __syncthreads();
+      if (act) {
+        reg::line_step_b<N, -1>(v, j2, ex, nr, l);
+#pragma unroll
+        for (int j = 0; j < N1; ++j) {
+          if (PR && j >= 2 && j <= 5) continue;   // off-sphere z are never gathered
+          A[(N2 * j + j2) * P + y] = v[j];
+        }
+      }
+      __syncthreads();
+    }
+    const int gb = band0 + band;
+    const int kidx = (gb / nb_per_k) % nk;
+    const R w = (R)wband[gb];
+    const double* tkk = tk + (size_t)kidx * ng;
+    const C* cb = coef + (size_t)band * ng;
+    C* gout = gcoef + (size_t)band * ng;
+    for (int e = plane_off[p] + tid; e < plane_off[p + 1]; e += blockDim.x) {
+      const int yz = sph_yz[e];
+      const int y = yz / N, z = yz - y * N;
+      const C val = A[z * P + y];
+      const C c = cb[e];
+      const R t = (R)tkk[e];
+      C g;
+      g.x = w * (t * c.x + sc * val.x);
+      g.y = w * (t * c.y + sc * val.y);
+      gout[e] = g;
+    }
+  }
+}
+
 // dense plane pass of whole grids [batch][x][y][z]: z then y transforms of
 // plane x (input real or complex), result to `out` in the same layout
 template <typename R, int N, int DIR, bool REAL_IN>
@@ -560,6 +648,17 @@ template <typename K> static int prep(K kernel, size_t bytes) {
 
 static bool g_line_prefetch = true;   // cp.async row prefetch in the adjoint line kernel
 
+// bands per CTA of the forward plane pass (register prefetch of the next
+// band); JRG_PLANE_FWD_BANDS overrides the default for measurements
+static int plane_fwd_bands_per_cta() {
+  static int v = [] {
+    const char* e = std::getenv("JRG_PLANE_FWD_BANDS");
+    const int x = e ? std::atoi(e) : 8;
+    return x < 1 ? 1 : (x > 64 ? 64 : x);
+  }();
+  return v;
+}
+
 // the pruned adjoint line kernel prefetches the next band into registers
 // unless JRG_LINE_ROWBUF=1 selects the shared-memory row buffer (measurements)
 static bool line_rowbuf() {
@@ -605,6 +704,16 @@ static int plane_fwd_launch(const jrg_plan* P, const Args& a, const C_t<R>* tw, 
   constexpr int T = threads_for<N>();
   int rc;
   const size_t sm = plane_smem<R, N>();
+  int bpc = plane_fwd_bands_per_cta();
+  while (bpc > 1 && (long long)a.nbands * P->nact < 2LL * 2 * 152 * bpc) bpc /= 2;
+  if (bpc >= 2) {
+    if ((rc = prep(k_plane_fwd_sphere_rp<R, N, PR>, sm)) <= 0) return rc;
+    k_plane_fwd_sphere_rp<R, N, PR><<<dim3(P->nact, (a.nbands + bpc - 1) / bpc), T, sm, st>>>(
+        reinterpret_cast<const C*>(a.in), reinterpret_cast<const C*>(a.aux), reinterpret_cast<C*>(a.out),
+        a.w, P->d.tk, P->nb, a.band0, P->d.plane_off, P->d.sph_yz, P->d.row_off, P->d.rows, tw, P->ng,
+        P->nact, P->nk, a.wscale, a.nbands, bpc);
+    FAST_LAUNCHED("fast::k_plane_fwd_sphere_rp");
+  }
   if ((rc = prep(k_plane_fwd_sphere<R, N, PR>, sm)) <= 0) return rc;
   k_plane_fwd_sphere<R, N, PR><<<dim3(P->nact, a.nbands), T, sm, st>>>(
       reinterpret_cast<const C*>(a.in), reinterpret_cast<const C*>(a.aux), reinterpret_cast<C*>(a.out),

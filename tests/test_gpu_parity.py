@@ -252,3 +252,42 @@ def test_two_stream_pipeline_matches_serial_and_oracle(prec, case):
   same = 1e-12 if prec == 64 else 1e-5
   np.testing.assert_allclose(out[1][0][:5], out[0][0][:5], rtol=same)
   assert np.abs(out[1][1] - out[0][1]).max() <= same * scale
+
+
+MULTIBAND_CASES = [
+  # 64^3, 4 k-points x 24 bands: single stream 96 bands x 31 planes selects the
+  # multi-band inverse plane pass (4 bands per CTA) and the register-prefetch
+  # forward plane pass, both with the pruned 64-point transforms
+  dict(kind="si8", grid=(64, 64, 64), kgrid=(2, 2, 1), nb=24, nocc=16),
+  # 48^3 (not pruned), 4 k-points x 30 bands
+  dict(kind="si8", grid=(48, 48, 48), kgrid=(2, 2, 1), nb=30, nocc=16),
+]
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("pipe", [0, 1])
+@pytest.mark.parametrize("case", range(len(MULTIBAND_CASES)))
+def test_multiband_plane_passes(prec, pipe, case):
+  """Several bands per CTA in the plane passes (chosen only when the call
+  fills the GPU) against the oracle, with and without the two-stream pipeline."""
+  torch = _torch()
+  from jrystal_gb300 import _lib
+  lib = _lib.load()
+  sysm = make_system(**MULTIBAND_CASES[case])
+  wr, wi = random_params(sysm, seed=77 + case)
+  terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+  plan = _plan(sysm, prec)
+  dt = torch.float64 if prec == 64 else torch.float32
+  prev = lib.jrg_pipeline(pipe)
+  try:
+    e, g1, g2 = plan.energy_and_grad(torch.tensor(wr, dtype=dt, device="cuda"),
+                                     torch.tensor(wi, dtype=dt, device="cuda"), sysm.occupation)
+  finally:
+    lib.jrg_pipeline(prev)
+  e = e.cpu().numpy()
+  tol = TOL[prec]
+  for i, name in enumerate(["kinetic", "external", "hartree", "xc", "total"]):
+    assert abs(e[i] - terms[name]) <= tol["e_rel"] * max(1.0, abs(terms[name])), (name, e[i], terms[name])
+  scale = max(np.abs(gr).max(), np.abs(gi).max())
+  err = max(np.abs(g1.cpu().numpy() - gr).max(), np.abs(g2.cpu().numpy() - gi).max())
+  assert err <= tol["g_rel"] * scale, (err, scale)
