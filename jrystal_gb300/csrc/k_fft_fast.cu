@@ -672,10 +672,11 @@ static bool line_rowbuf() {
 // bands per CTA of the inverse plane pass (1: one CTA per (plane, band));
 // JRG_PLANE_BANDS overrides the default for measurements.  At the 64^3 Si8
 // cell: 1 -> 0.253 ms, 4 -> 0.246, 8 -> 0.235, 16 -> 0.239 (best step time,
-// 522.5 vs 512.9 evals/s), 32 -> 0.260.  In the forward plane pass neither a
-// staged next plane (0.33 vs 0.28 ms) nor a register prefetch of it (0.266 -
-// 0.292 vs 0.265 ms at 2 - 8 bands per CTA) paid off: both cost a third of the
-// resident CTAs.
+// 522.5 vs 512.9 evals/s), 32 -> 0.260.  In the forward plane pass a staged
+// next plane (shared memory) was slower (0.33 vs 0.28 ms); the register
+// prefetch (k_plane_fwd_sphere_rp) leaves the single-stream phase time as it
+// was (0.266 vs 0.265 ms) but, with fewer CTAs per launch, overlaps the other
+// pipeline stream better: 581.4 vs 576.7 evals/s over three runs each.
 static int plane_bands_per_cta() {
   static int v = [] {
     const char* e = std::getenv("JRG_PLANE_BANDS");
