@@ -195,10 +195,10 @@ def _config(wl, n):
 
 
 # DRAM bytes (read + write) per band of one k_line_apply_v<float, 64> launch,
-# from the ncu --set full capture of the 64^3 Si8 cell at 2x2x2 k-points (331 MB
-# for 192 bands, profiles/hot_kernels_si8_cubic_64_k8.md); a full launch is
-# scaled by its band count
-LINE_APPLY_V_DRAM_PER_BAND = (196.706304e6 + 133.798656e6) / 192
+# from the ncu --set full capture of the 64^3 Si8 cell at 2x2x2 k-points (135 MB
+# for the 96 bands of one pipeline half, profiles/hot_kernels_si8_cubic_64_k8.md);
+# a full launch is scaled by its band count
+LINE_APPLY_V_DRAM_PER_BAND = (98.57996e6 + 36.56985e6) / 96
 
 
 # algorithmic bytes per call of each phase of jrg_energy_grad (fused: the
