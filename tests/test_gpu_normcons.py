@@ -296,3 +296,36 @@ def test_band_normcons_driver_matches_full_diagonalisation(tmp_path):
   print("band energies: max |error| per band", err.max(axis=0))
   assert np.all(out.eigenvalues[0] >= exact - 1e-8)
   assert err.max() < 1e-4
+
+
+def test_nc_functional_hamiltonian_matrix_and_trace(tmp_path):
+  """normcons.hamiltonian_matrix / hamiltonian_trace (nloc.py:160-303) on
+  dense coefficients against the same sums of the oracle's dense pieces: the
+  nonlocal F^H F / vol, the local and Hartree potentials as ifftn of their
+  reciprocal tables (complex, as the reference keeps them), v_xc and T."""
+  import jrystal_gb300 as jr
+  from jrystal_gb300.pseudopotential import normcons
+  jr.set_precision(64)
+  sysm, nc, vloc, table = _setup(tmp_path, kind="si2", grid=(12, 12, 12), kgrid=(2, 1, 1), nb=4,
+                                 nocc=2)
+  g = nc.g_vector_grid
+  wr0, wi0 = random_params(nc, seed=12)
+  c0, _ = R.cholesky_qr(wr0, wi0)
+  rho_h = R.density_grid(R.expand_coefficient(c0, nc.mask), nc.vol, nc.occupation)  # (1,x,y,z)
+  wr, wi = random_params(nc, seed=13)
+  c, _ = R.cholesky_qr(wr, wi)
+  dense_c = R.expand_coefficient(c, nc.mask)
+  wave = R.wave_grid(dense_c, nc.vol)
+  v_h = R._ifftn(R.hartree_reciprocal(R._fftn(rho_h), g, kohn_sham=True))
+  v_xc = R.xc_eps_v(rho_h[0], nc.xc)[1]
+  h_ref = (R.hamiltonian_nonlocal(dense_c, nc.proj, nc.vol)
+           + R.expectation(wave, R._ifftn(vloc), nc.vol, diagonal=False, mode="real")
+           + R.expectation(wave, v_h + v_xc, nc.vol, diagonal=False, mode="real")
+           + R.expectation(dense_c, R.kinetic_operator(g, nc.kpts), nc.vol, diagonal=False,
+                           mode="kinetic"))
+  h = normcons.hamiltonian_matrix(dense_c, rho_h, vloc, nc.proj, g, nc.kpts, nc.vol,
+                                  xc=nc.xc, kohn_sham=True).cpu().numpy()
+  np.testing.assert_allclose(h, h_ref, atol=1e-9 * np.abs(h_ref).max())
+  tr = float(normcons.hamiltonian_trace(dense_c, rho_h, vloc, nc.proj, g, nc.kpts, nc.vol,
+                                        xc=nc.xc, kohn_sham=True))
+  assert abs(tr - np.einsum("skii->", h_ref).real) < 1e-9 * abs(tr)
