@@ -473,8 +473,25 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere_rp(
   if (b_begin < b_end) load(b_begin);
   __syncthreads();
   const R sc = (R)scale;
+  // first gather element of this thread: its map entry is band-independent,
+  // its coefficient and kinetic value are loaded at the top of each band so
+  // that their latency falls under the transforms
+  const int e_lo = plane_off[p], e_hi = plane_off[p + 1];
+  const int e0 = e_lo + tid;
+  const bool has0 = e0 < e_hi;
+  const int yz0 = has0 ? sph_yz[e0] : 0;
   C v[N1];
   for (int band = b_begin; band < b_end; ++band) {
+    const int gb = band0 + band;
+    const int kidx = (gb / nb_per_k) % nk;
+    const double* tkk = tk + (size_t)kidx * ng;
+    const C* cb = coef + (size_t)band * ng;
+    C c0 = czero<C>();
+    R t0 = (R)0;
+    if (has0) {
+      c0 = cb[e0];
+      t0 = (R)tkk[e0];
+    }
     // y transforms of all z columns
 #pragma unroll
     for (int j1 = 0; j1 < N1; ++j1) v[j1] = nxt[j1];
@@ -509,13 +526,17 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere_rp(
       }
       __syncthreads();
     }
-    const int gb = band0 + band;
-    const int kidx = (gb / nb_per_k) % nk;
     const R w = (R)wband[gb];
-    const double* tkk = tk + (size_t)kidx * ng;
-    const C* cb = coef + (size_t)band * ng;
     C* gout = gcoef + (size_t)band * ng;
-    for (int e = plane_off[p] + tid; e < plane_off[p + 1]; e += blockDim.x) {
+    if (has0) {
+      const int y = yz0 / N, z = yz0 - y * N;
+      const C val = A[z * P + y];
+      C g;
+      g.x = w * (t0 * c0.x + sc * val.x);
+      g.y = w * (t0 * c0.y + sc * val.y);
+      gout[e0] = g;
+    }
+    for (int e = e0 + blockDim.x; e < e_hi; e += blockDim.x) {
       const int yz = sph_yz[e];
       const int y = yz / N, z = yz - y * N;
       const C val = A[z * P + y];
