@@ -85,7 +85,11 @@ long long jrg_launch_count(void);
 
 /* Plans: geometry tables (sphere maps, twiddles, kinetic and external
  * potential tables) on the current device.  Creating a plan allocates its
- * tables and synchronises the device; all other calls only enqueue work. */
+ * tables and synchronises the device; all other calls only enqueue work.
+ * Concurrency: a plan serves one host thread at a time (its second stream,
+ * fork/join events and phase profiler belong to the plan); threads that call
+ * concurrently use a plan each.  Calls that may overlap on the device need
+ * separate workspaces.  Distinct plans share no mutable state. */
 int jrg_plan_create(const jrg_plan_desc* desc, jrg_plan** out);
 int jrg_plan_destroy(jrg_plan* plan);
 /* Caller workspace needed by the entry points below (bytes). */
