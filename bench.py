@@ -395,12 +395,27 @@ def run_ours(args, wl):
     traffic = None
     if top == "line_apply_v" and plan.grid == (64, 64, 64) and plan.precision == 32:
       traffic = LINE_APPLY_V_DRAM_PER_BAND * plan.num_spin * plan.num_kpt * plan.num_band
+    # whole-evaluation models: the grid-streaming byte model 6 P G c + 10 P n_g c
+    # (each band's grid crossing HBM once per FFT pass) and the compulsory
+    # traffic (2 + 4) P n_g r 2 (parameters, gradient and Adam state), against
+    # the measured step time; FFT flops 3 P 5 G log2 G
+    c_b = 8 if wl.precision == 32 else 16
+    P_b = plan.num_spin * plan.num_kpt * plan.num_band
+    G_b = int(np.prod(plan.grid))
+    model_bytes = 6 * P_b * G_b * c_b + 10 * P_b * plan.num_g * c_b
+    compulsory = (2 + 4) * P_b * plan.num_g * (c_b // 2) * 2
+    fft_flops = 3 * P_b * 5 * G_b * np.log2(G_b)
+    step_model = {"model_bytes": int(model_bytes), "model_gbs": model_bytes / (ms * 1e-3) / 1e9,
+                  "model_frac": model_bytes / (ms * 1e-3) / 1e9 / peak,
+                  "compulsory_bytes": int(compulsory),
+                  "compulsory_frac": compulsory / (ms * 1e-3) / 1e9 / peak,
+                  "fft_tflops": fft_flops / (ms * 1e-3) / 1e12}
     roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
             "traffic_source": None if traffic is None else
             "ncu dram bytes per band (2x2x2 k-point capture) x bands of this launch",
             "algorithmic_bytes": pb[top], "ms_per_launch": phases[top],
-            "phase_ms": {k: round(v, 4) for k, v in phases.items()}}
+            "phase_ms": {k: round(v, 4) for k, v in phases.items()}, "step_model": step_model}
     out = {"metric": METRIC, "value": 1000.0 / ms * ws, "unit": UNIT, "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
