@@ -61,6 +61,18 @@ def _dist():
   return ws, rank, local
 
 
+def _max_over_ranks(x, device):
+  """The maximum of x over the ranks of the process group (x itself without
+  one): the job's time is its slowest rank's."""
+  import torch
+  import torch.distributed as dist
+  if not dist.is_initialized() or dist.get_world_size() == 1:
+    return float(x)
+  t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+  dist.all_reduce(t, op=dist.ReduceOp.MAX)
+  return float(t.item())
+
+
 def _peaks():
   path = os.path.join(ROOT, "MEASURED_PEAKS.json")
   try:
@@ -339,10 +351,7 @@ def run_ours(args, wl):
   _lib.check(lib.jrg_profile_read(plan._h, arr, ct.byref(ncalls), nph), "jrg_profile_read")
   lib.jrg_profile_enable(plan._h, 0)
   phases = {lib.jrg_profile_phase_name(i).decode(): arr[i] / max(1, ncalls.value) for i in range(nph)}
-  if ws > 1:
-    tt = torch.tensor([ms], dtype=torch.float64, device=dev)
-    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    ms = float(tt.item())
+  ms = _max_over_ranks(ms, dev)
   energies = e.cpu().numpy().tolist()
 
   # end to end through the public API with host buffers: H2D of the step's
@@ -382,10 +391,7 @@ def run_ours(args, wl):
   e1.record(stream)
   barrier()
   e2e_ms = e0.elapsed_time(e1) / args.steps
-  if ws > 1:
-    tt = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
-    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    e2e_ms = float(tt.item())
+  e2e_ms = _max_over_ranks(e2e_ms, dev)
 
   if rank == 0:
     peak, peak_kind = _peaks()
