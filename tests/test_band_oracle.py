@@ -77,3 +77,59 @@ def test_rayleigh_ritz_against_full_plane_wave_hamiltonian():
   np.testing.assert_allclose(ritz, exact, atol=1e-10 * np.abs(exact).max())
   # and the trace is stationary there
   assert np.abs(out["grad_re"]).max() < 1e-8 and np.abs(out["grad_im"]).max() < 1e-8
+
+
+def _wirtinger_hessian(f, n, h=1e-3):
+  """2 d^2 f / (d conj(u_i) d u_j) at u = 1 by central differences, u = a + i b:
+  d/d conj(u) = (d/da + i d/db) / 2, d/du = (d/da - i d/db) / 2."""
+  u0 = np.ones(n, dtype=np.complex128)
+
+  def d2(i, si, j, sj):   # second difference along the real directions si e_i, sj e_j
+    ei = np.zeros(n, complex)
+    ej = np.zeros(n, complex)
+    ei[i] = si * h
+    ej[j] = sj * h
+    return (f(u0 + ei + ej) - f(u0 + ei - ej) - f(u0 - ei + ej) + f(u0 - ei - ej)) / (4 * h * h)
+
+  out = np.zeros((n, n), dtype=np.complex128)
+  for i in range(n):
+    for j in range(n):
+      faa, fab = d2(i, 1, j, 1), d2(i, 1, j, 1j)
+      fba, fbb = d2(i, 1j, j, 1), d2(i, 1j, j, 1j)
+      out[i, j] = 2 * 0.25 * (faa - 1j * fab + 1j * fba + fbb)
+  return out
+
+
+def test_complex_hessian_convention_and_band_hamiltonian():
+  """jrystal builds H_ij as complex_hessian of efun(u) = 1/2 E(sum_i u_i psi_i)
+  (jrystal/_src/hamiltonian.py:211-232) in the convention that
+  _src/hessian_test.py:29-45 pins: the Hessian of 1/2 x^H H x is H, i.e.
+  2 d^2 f / (d conj(x_i) d x_j).  The oracle's band Hamiltonian (the form the
+  device returns) equals that construction."""
+  rng = np.random.default_rng(3)
+  a = rng.normal(size=(5, 5)) + 1j * rng.normal(size=(5, 5))
+  hq = a + a.conj().T
+  q = lambda x: float(np.real(0.5 * x.conj() @ hq @ x))
+  np.testing.assert_allclose(_wirtinger_hessian(q, 5), hq, atol=1e-7)
+
+  sysm = make_system(kind="si2", grid=(8, 8, 8), kgrid=(1, 1, 1), nb=3, nocc=2)
+  rho, _ = _veff(sysm)
+  wr, wi = random_params(sysm, seed=9)
+  c, _ = R.cholesky_qr(wr, wi)
+  dense = R.expand_coefficient(c, sysm.mask)                      # (1,1,b,x,y,z)
+
+  def efun(u):
+    psi = np.einsum("i,ixyz->xyz", u, dense[0, 0])[None, None, None]
+    return 0.5 * float(R.hamiltonian_matrix_trace(psi, sysm.positions, sysm.charges, rho,
+                                                  sysm.g_vector_grid, sysm.kpts, sysm.vol,
+                                                  sysm.xc, True))
+
+  h_fd = _wirtinger_hessian(efun, 3)
+  h = R.hamiltonian_matrix(dense, sysm.positions, sysm.charges, rho, sysm.g_vector_grid,
+                           sysm.kpts, sysm.vol, sysm.xc, True)[0, 0]
+  np.testing.assert_allclose(h, h_fd, atol=1e-6 * np.abs(h).max())
+  ref = R.band_trace_terms(wr, wi, np.real(R.effective(rho, sysm.positions, sysm.charges,
+                                                       sysm.g_vector_grid, sysm.vol, False,
+                                                       sysm.xc, True)[0]), sysm,
+                           with_grad=False)["hmat"][0, 0]
+  np.testing.assert_allclose(ref, h_fd, atol=1e-6 * np.abs(h).max())
