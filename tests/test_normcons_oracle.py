@@ -199,3 +199,27 @@ def test_oracle_nc_rayleigh_ritz(tmp_path):
   out = R.band_trace_terms(x.real, x.imag, v, nc)
   np.testing.assert_allclose(np.linalg.eigvalsh(out["hmat"][0, 0]), e[:3], atol=1e-10 * np.abs(e[:3]).max())
   assert np.abs(out["grad_re"]).max() < 1e-8 and np.abs(out["grad_im"]).max() < 1e-8
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_UPF), reason="reference UPF files absent")
+def test_numerical_sbt_accuracy_on_reference_betas():
+  """jrystal/sbt/sbt_test.py:42-71 holds its two transforms of the bundled Si
+  betas (kmax 100, delta_r = PP_RAB, 2000 points up to 100) within 5e-3 of
+  each other; the numerical transform restated here stays within that of an
+  independent Simpson quadrature over the mesh (measured 8.9e-4)."""
+  from types import SimpleNamespace
+  from scipy.integrate import simpson
+  from scipy.interpolate import CubicSpline
+  from scipy.special import spherical_jn
+  from jrystal_gb300.pseudopotential import NormConservingPseudopotential
+  from jrystal_gb300.pseudopotential.sbt import sbt
+  cr = SimpleNamespace(symbols=["Si"], positions=np.zeros((1, 3)), charges=np.array([14]))
+  pp = NormConservingPseudopotential.create(cr, REF_UPF + "/")
+  r, rab = pp.r_grid[0], pp.r_ab[0]
+  beta, ls = pp.nonlocal_beta_grid[0], pp.nonlocal_angular_momentum[0]
+  g, out = sbt(r, beta, l=list(ls), kmax=100, delta_r=rab)
+  xx = np.linspace(0, 100, 2000)
+  got = CubicSpline(g, out, axis=-1)(xx)
+  ref = np.stack([[simpson(beta[b] * spherical_jn(int(ls[b]), k * r) * r * r * rab, dx=1.0)
+                   for k in xx] for b in range(len(ls))])
+  np.testing.assert_allclose(got, ref, rtol=0, atol=5e-3)
