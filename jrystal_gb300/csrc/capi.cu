@@ -280,13 +280,17 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
     }
   }
   P->nact = (int)plane_x.size();
-  P->xprune64 = P->nx == 64;
-  for (int x : plane_x)
-    if (x >= 16 && x <= 48) P->xprune64 = false;
-  P->yzprune64 = P->ny == 64 && P->nz == 64;
-  for (int e = 0; e < ng; ++e) {
-    const int y = sph_yz[e] / P->nz, z = sph_yz[e] % P->nz;
-    if ((y >= 16 && y <= 48) || (z >= 16 && z <= 48)) P->yzprune64 = false;
+  {
+    auto mid = [](int i, int n) { return i >= n / 4 && i < 3 * n / 4; };   // the zero blocks
+    auto eight = [](int n) { return n == 32 || n == 64; };                 // 8 values per thread
+    P->xprune = eight(P->nx);
+    for (int x : plane_x)
+      if (mid(x, P->nx)) P->xprune = false;
+    P->yzprune = eight(P->ny) && P->ny == P->nz;
+    for (int e = 0; e < ng; ++e) {
+      const int y = sph_yz[e] / P->nz, z = sph_yz[e] % P->nz;
+      if (mid(y, P->ny) || mid(z, P->nz)) P->yzprune = false;
+    }
   }
   P->max_rows = 0;
   for (int p = 0; p < P->nact; ++p) P->max_rows = std::max(P->max_rows, row_off[p + 1] - row_off[p]);

@@ -154,9 +154,10 @@ template <int N, int DIR, typename C> __host__ __device__ __forceinline__ void d
   }
 }
 
-// 8-point DFT of v with v[2..5] = 0 (the x lines of a 64^3 plane slab whose
-// active planes lie in x <= 15 and x >= 49): the stages of dft<8> with the
-// additions of the known zeros left out.
+// 8-point DFT of v with v[2..5] = 0 (a line of N = 32 or 64 points whose
+// non-zero entries lie below N/4 and at or above 3N/4, held as 8 values per
+// thread: x = N2 j1 + j2): the stages of dft<8> with the additions of the
+// known zeros left out.
 template <int DIR, typename C> __host__ __device__ __forceinline__ void dft8_in0167(C (&v)[8]) {
   // even and odd halves (v0, 0, 0, v6) and (v1, 0, 0, v7) through dft<4>'s stages
   const C te = twiddle_mul<DIR, 1, 4>(v[6]);
@@ -211,10 +212,13 @@ __host__ __device__ __forceinline__ void line_step_a(C (&v)[Split<N>::N1], const
   });
 }
 
-// line_step_a for N = 64 with the thread's inputs v[2..5] known to be zero
-template <int DIR, typename C>
-__host__ __device__ __forceinline__ void line_step_a_pruned64(C (&v)[8], const C* __restrict__ tw, int j2,
-                                                     C* ex, int L, int l) {
+// line_step_a for the lengths held as 8 values per thread (N = 32, 64) with
+// the thread's inputs v[2..5] known to be zero
+template <int N, int DIR, typename C>
+__host__ __device__ __forceinline__ void line_step_a_pruned8(C (&v)[8], const C* __restrict__ tw, int j2,
+                                                    C* ex, int L, int l) {
+  static_assert(Split<N>::N1 == 8, "pruned step for eight values per thread");
+  constexpr int N2 = Split<N>::N2;
   dft8_in0167<DIR>(v);
   sfor<8>([&](auto kk) {
     constexpr int k1 = kk.value;
@@ -224,7 +228,7 @@ __host__ __device__ __forceinline__ void line_step_a_pruned64(C (&v)[8], const C
       if (DIR > 0) w.y = -w.y;
       t = cmul(t, w);
     }
-    ex[(k1 * 8 + j2) * L + l] = t;
+    ex[(k1 * N2 + j2) * L + l] = t;
   });
 }
 

@@ -97,8 +97,8 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere(
 // gather of band i+1 (zero-filling cp.async through the dense row map: sphere
 // values and zeros for the rest of every active row) runs under the transforms
 // of band i; inactive rows of both [z][y] buffers stay zero.
-// PR (N = 64 only): active rows y and sphere z lie outside 16..48, so the
-// inputs v[2..5] of the z and y transforms are zero
+// PR (8 values per thread: N = 32, 64): active rows y and sphere z lie below
+// N/4 or at or above 3N/4, so the inputs v[2..5] of the z and y transforms are zero
 template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere_mb(
     const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ planes, const int* __restrict__ row_off,
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere_mb(
           if (PR && j1 >= 2 && j1 <= 5) continue;
           v[j1] = A[(N2 * j1 + j2) * P + y];
         }
-        if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex, nr, l);
+        if constexpr (PR) reg::line_step_a_pruned8<N, +1>(v, tw, j2, ex, nr, l);
         else reg::line_step_a<N, +1>(v, tw, j2, ex, nr, l);
       }
       __syncthreads();
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_inv_sphere_mb(
         if (PR && j1 >= 2 && j1 <= 5) continue;
         v[j1] = A[z * P + N2 * j1 + j2];
       }
-      if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex, N, z);
+      if constexpr (PR) reg::line_step_a_pruned8<N, +1>(v, tw, j2, ex, N, z);
       else reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
       __syncthreads();
       reg::line_step_b<N, +1>(v, j2, ex, N, z);
@@ -208,7 +208,7 @@ __device__ __forceinline__ void prefetch_row(const C_t<R>* __restrict__ planes, 
 // inverse x transform + occupation-weighted |psi|^2 of a band group (one
 // transform per band: the row prefetch of the adjoint pass measured slower
 // here, 0.30 vs 0.25 ms on the 64^3 Si8 cell)
-// PR (N = 64 only): the thread's inputs v[2..5] (x = 16..47) are known zero
+// PR (N = 32, 64): the thread's inputs v[2..5] (x = N/4 .. 3N/4 - 1) are known zero
 template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_density(
     const C_t<R>* __restrict__ planes, R* __restrict__ rho_part, const double* __restrict__ wband,
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
       for (int j1 = 0; j1 < N1; ++j1) v[j1] = slot[j1] < 0 ? z0 : src[(size_t)slot[j1] * (N * N)];
     }
     C* ex = parity ? ex1 : ex0;
-    if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex, N, z);
+    if constexpr (PR) reg::line_step_a_pruned8<N, +1>(v, tw, j2, ex, N, z);
     else reg::line_step_a<N, +1>(v, tw, j2, ex, N, z);
     __syncthreads();
     reg::line_step_b<N, +1>(v, j2, ex, N, z);
@@ -273,8 +273,8 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
 
 // adjoint line pass: inverse x transform, times V(r), forward x transform,
 // active planes written back in place
-// PR (N = 64 only): x = 16..47 (the thread's v[2..5]) are known zero on input
-// and not written back
+// PR (N = 32, 64): x = N/4 .. 3N/4 - 1 (the thread's v[2..5]) are known zero
+// on input and not written back
 template <typename R, int N, bool PF, bool PR>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_apply_v(
     C_t<R>* __restrict__ planes, const R* __restrict__ vr, int nband, int bands_per_group,
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
         v[j1] = slot[j1] < 0 ? z0 : base[(size_t)slot[j1] * (N * N)];
       }
     }
-    if constexpr (PR) reg::line_step_a_pruned64<+1>(v, tw, j2, ex0, N, z);
+    if constexpr (PR) reg::line_step_a_pruned8<N, +1>(v, tw, j2, ex0, N, z);
     else reg::line_step_a<N, +1>(v, tw, j2, ex0, N, z);
     __syncthreads();
     reg::line_step_b<N, +1>(v, j2, ex0, N, z);
@@ -362,8 +362,8 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
 
 // forward: y, z transforms of an active plane, sphere gather and gradient
 //   g[b][e] = f_b * (tk[k][e] * c[b][e] + scale * FFT(V psi_b)[e])
-// PR (N = 64 only): only rows y and sphere z outside 16..48 are needed, so
-// the y and z transforms do not form the outputs v[2..5]
+// PR (N = 32, 64): only rows y and sphere z below N/4 or at or above 3N/4 are
+// needed, so the y and z transforms do not form the outputs v[2..5]
 template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
     const C_t<R>* __restrict__ planes, const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ gcoef,
@@ -795,8 +795,8 @@ static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
       if (bpc < 4) bpc = 1;
       const size_t smb = plane_mb_smem<R, N>(P->max_rows);
       if (bpc > 1 && (long long)smb <= optin_smem()) {
-        if constexpr (N == 64) {
-          if (P->yzprune64) return plane_inv_mb_launch<R, N, true>(P, a, tw, bpc, smb, st);
+        if constexpr (Split<N>::N1 == 8) {
+          if (P->yzprune) return plane_inv_mb_launch<R, N, true>(P, a, tw, bpc, smb, st);
         }
         return plane_inv_mb_launch<R, N, false>(P, a, tw, bpc, smb, st);
       }
@@ -808,20 +808,20 @@ static int run(const jrg_plan* P, int op, const Args& a, cudaStream_t st) {
       FAST_LAUNCHED("fast::k_plane_inv_sphere");
     }
     case OP_LINE_DENSITY: {
-      if constexpr (N == 64) {
-        if (P->xprune64) return line_density_launch<R, N, true>(P, a, tw, st);
+      if constexpr (Split<N>::N1 == 8) {
+        if (P->xprune) return line_density_launch<R, N, true>(P, a, tw, st);
       }
       return line_density_launch<R, N, false>(P, a, tw, st);
     }
     case OP_LINE_APPLY_V: {
-      if constexpr (N == 64) {
-        if (P->xprune64) return line_apply_v_launch<R, N, true>(P, a, tw, st);
+      if constexpr (Split<N>::N1 == 8) {
+        if (P->xprune) return line_apply_v_launch<R, N, true>(P, a, tw, st);
       }
       return line_apply_v_launch<R, N, false>(P, a, tw, st);
     }
     default: {
-      if constexpr (N == 64) {
-        if (P->yzprune64) return plane_fwd_launch<R, N, true>(P, a, tw, st);
+      if constexpr (Split<N>::N1 == 8) {
+        if (P->yzprune) return plane_fwd_launch<R, N, true>(P, a, tw, st);
       }
       return plane_fwd_launch<R, N, false>(P, a, tw, st);
     }

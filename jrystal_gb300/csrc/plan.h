@@ -95,8 +95,11 @@ struct jrg_plan {
   int ns, nk, nb, ng;
   int nact;                 // active x planes
   int max_rows;             // max active rows in a plane
-  bool xprune64 = false;    // 64^3 grid with every active x plane in x <= 15 or x >= 49
-  bool yzprune64 = false;   // 64^3 grid with every active row y and sphere z outside 16..48
+  // N = 32 or 64 (8 values per thread in the slab transforms) with every
+  // active x plane (xprune) / active row y and sphere z (yzprune) below N/4 or
+  // at or above 3N/4: the x (y, z) transforms skip the known zeros
+  bool xprune = false;
+  bool yzprune = false;
   double cell[9], recip[9], vol;
   std::vector<double> pos, charge, kpts;
   int xc;

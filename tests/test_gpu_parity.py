@@ -42,6 +42,8 @@ CASES = [
   dict(kind="si8", grid=(16, 16, 16), kgrid=(2, 1, 1), nb=30, nocc=16),
   # more than 32 bands: tiled Gram, 32-wide rotation tiles, global-memory Cholesky
   dict(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 2), nb=40, nocc=20),
+  # 32^3 sphere: the pruned eight-values-per-thread transforms
+  dict(kind="si8", grid=(32, 32, 32), kgrid=(2, 1, 1), nb=4, nocc=2),
 ]
 
 
