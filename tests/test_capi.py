@@ -52,3 +52,32 @@ def test_invalid_arguments_are_rejected_on_the_host():
 def test_build_recipe_targets_sm_103a():
   assert "arch=compute_103a,code=sm_103a" in " ".join(build.ARCH)
   assert os.path.exists(build.LIB)
+
+
+def test_plan_refuses_a_cpu_device():
+  """There is no CPU fallback: a plan on the CPU is refused before any work."""
+  import numpy as np
+  from jrystal_gb300.engine import PlaneWavePlan
+  mask = np.zeros((8, 8, 8), dtype=bool)
+  mask[0, 0, 0] = mask[0, 0, 1] = True
+  with pytest.raises(RuntimeError, match="CUDA"):
+    PlaneWavePlan(np.eye(3) * 5.0, np.zeros((1, 3)), np.array([1.0]), (8, 8, 8), mask,
+                  np.zeros((1, 3)), 1, 1, 64, "lda_x", device="cpu")
+
+
+def test_pseudopotential_setter_rejects_bad_arguments_on_the_host():
+  lib = _lib.load()
+  assert lib.jrg_plan_set_pseudopotential(None, None, 0, None) == _lib.JRG_ERR_INVALID
+  assert lib.jrg_plan_set_pseudopotential(None, None, 4, None) == _lib.JRG_ERR_INVALID
+
+
+def test_pseudopotential_types():
+  from types import SimpleNamespace
+  from jrystal_gb300 import calc
+  cr = SimpleNamespace(symbols=["Si"], positions=[[0, 0, 0]], charges=[14])
+  with pytest.raises(NotImplementedError):
+    calc.create_pseudopotential({"pseudopotential_type": "us", "pseudopotential_file_dir": "."}, cr)
+  with pytest.raises(ValueError):
+    calc.create_pseudopotential({"pseudopotential_type": "paw", "pseudopotential_file_dir": "."}, cr)
+  with pytest.raises(ValueError):
+    calc.create_pseudopotential({"pseudopotential_type": "nc", "pseudopotential_file_dir": None}, cr)
