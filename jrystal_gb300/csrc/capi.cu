@@ -13,7 +13,7 @@ namespace jrg {
 
 // ---- launchers implemented in the kernel files ----
 template <typename R> int launch_plane_inv_sphere(const jrg_plan*, const void*, void*, int, cudaStream_t);
-template <typename R> int launch_line_density(const jrg_plan*, const void*, void*, const double*, double, int, int, int, cudaStream_t);
+template <typename R> int launch_line_density(const jrg_plan*, const void*, void*, const double*, double, int, int, int, double*, cudaStream_t);
 template <typename R> int launch_line_apply_v(const jrg_plan*, const void*, void*, const void*, int, int, cudaStream_t);
 template <typename R> int launch_plane_fwd_sphere(const jrg_plan*, const void*, const void*, void*, const double*, int, int, double, cudaStream_t);
 template <typename R> int launch_fft3d_dense(const FftAxis*, const C_t<R>*, int, int, bool, const void*, C_t<R>*, C_t<R>*, double, cudaStream_t);
@@ -26,9 +26,9 @@ int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int
 template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t);
 constexpr int kSplit = 0, kBand = 1;           // tall-operand layouts (k_orth.cu)
 constexpr int kRotBand = 0, kRotGC = 1, kRotGSplit = 2;
-template <typename R> int launch_reduce_density(const void*, void*, int, int, long long, cudaStream_t);
-template <typename R> int launch_recip_terms(const void*, const double*, const void*, void*, double*, double*, int, long long, double, cudaStream_t);
-template <typename R> int launch_potential(const void*, const void*, double, void*, double*, int, long long, int, double, cudaStream_t);
+template <typename R> int launch_reduce_density(const void*, void*, int, int, long long, const double*, double*, cudaStream_t);
+template <typename R> int launch_recip_terms(const void*, const double*, void*, double*, int, long long, double, const ChargeFix&, cudaStream_t);
+template <typename R> int launch_potential(const void*, const void*, double, void*, double*, int, long long, int, double, const double*, const double*, double*, cudaStream_t);
 template <typename R> int launch_xc_field(const void*, void*, long long, int, int, cudaStream_t);
 template <typename R> int launch_real_part(const void*, void*, long long, double, cudaStream_t);
 template <typename R> int launch_hartree_g(const void*, const double*, void*, long long, double, cudaStream_t);
@@ -44,14 +44,15 @@ int launch_band_trace_sums(const double2*, int, int, const double*, int, double*
 int launch_kin_reduce(int, const void*, int, int, int, const double*, double*, double*, cudaStream_t);
 template <typename R> int launch_rotate_kinetic(const void*, const void*, const double2*, void*, int, int, int, const double*, int, void*, cudaStream_t, int = 0);
 template <typename R> int launch_mul_ig(const void*, const double*, void*, int, long long, double, cudaStream_t);
-template <typename R> int launch_gga_local(const void*, void*, void*, void*, void*, double*, int, long long, int, double, int, cudaStream_t);
+template <typename R> int launch_gga_local(const void*, void*, void*, void*, void*, double*, int, long long, int, double, int, const double*, const double*, double*, cudaStream_t);
 template <typename R> int launch_div_g(void*, const void*, const void*, const double*, long long, double, cudaStream_t);
-template <typename R> int launch_potential_gga(const void*, double, void*, const void*, long long, cudaStream_t);
+template <typename R> int launch_potential_gga(const void*, double, void*, const void*, long long, const double*, cudaStream_t);
 constexpr int kXcGga = JRG_XC_GGA_X_PBE | JRG_XC_GGA_C_PBE;
-template <typename R> int launch_geometry_tables(double*, double*, void*, const double*, const double*, const double*, int, int, int, int, double, cudaStream_t);
+template <typename R> int launch_geometry_tables(double*, double*, void*, double2*, const double*, const double*, const double*, int, int, int, int, double, cudaStream_t);
 int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
 template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t);
 int launch_twiddles(int n, int prec, void* out, cudaStream_t st);
+int launch_dft_axis_inv_f64(const double2*, double2*, int, int, int, int, const double2*, cudaStream_t);
 template <typename R> int launch_rotate_adam(const void*, const double2*, const void*, const double2*, const AdamArgs&, int, int, int, double, cudaStream_t);
 int launch_lda(int prec, long long n, int xc, int ks, const void* rho, void* out, cudaStream_t st);
 
@@ -120,6 +121,8 @@ static void layout_workspace(jrg_plan* P) {
   w.t = take(nbt * P->nact * (size_t)P->ny * P->nz * C);
   w.u = w.t;                            // adjoint line pass works in place
   w.rho_part = take((size_t)w.ngroups * P->ngrid * Rz);
+  w.rho_scale = take((size_t)w.ngroups * sizeof(double));
+  w.rho_q = take((kQParts + 1) * sizeof(double));
   w.rho = take((size_t)P->ns * P->ngrid * Rz);
   w.rhog = take((size_t)P->ngrid * C);
   w.fft_scratch = take((size_t)P->ngrid * C);
@@ -138,6 +141,39 @@ static void layout_workspace(jrg_plan* P) {
   w.nl_part = P->nproj > 0 ? take(nsk * w.nl_splits * (size_t)P->nb * P->nproj * sizeof(double2)) : 0;
   w.nl_fw = P->nproj > 0 ? take(nbt * (size_t)P->nproj * sizeof(double2)) : 0;
   w.total = o;
+}
+
+// V_ext(r) = Re IFFT(V_ext(G)) in FP64 from the FP64 table (plan setup; the
+// external energy and potential of the energy path use it in real space).
+// Three direct DFTs along the axes: N (nx + ny + nz) FP64 products once per
+// table, with no shared-memory limit on the grid size.
+static int make_vext_real(jrg_plan* P) {
+  const size_t n = (size_t)P->ngrid;
+  double2* tw = nullptr;
+  double2* buf = nullptr;
+  int rc = JRG_OK;
+  cudaError_t e = cudaSuccess;
+  if (!P->d.vext_r) e = cudaMalloc((void**)&P->d.vext_r, n * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&tw, (size_t)(P->nx + P->ny + P->nz) * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&buf, 2 * n * sizeof(double2));
+  if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(external potential table)");
+  double2* twx = tw;
+  double2* twy = tw + P->nx;
+  double2* twz = tw + P->nx + P->ny;
+  if (!rc) rc = launch_twiddles(P->nx, 64, twx, 0);
+  if (!rc) rc = launch_twiddles(P->ny, 64, twy, 0);
+  if (!rc) rc = launch_twiddles(P->nz, 64, twz, 0);
+  if (!rc) rc = launch_dft_axis_inv_f64(P->d.vext64, buf, P->nx, P->ny, P->nz, 2, twz, 0);
+  if (!rc) rc = launch_dft_axis_inv_f64(buf, buf + n, P->nx, P->ny, P->nz, 1, twy, 0);
+  if (!rc) rc = launch_dft_axis_inv_f64(buf + n, buf, P->nx, P->ny, P->nz, 0, twx, 0);
+  if (!rc) rc = launch_real_part<double>(buf, P->d.vext_r, (long long)n, 1.0 / (double)P->ngrid, 0);
+  if (!rc) {
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) rc = cuda_fail(e, "external potential table");
+  }
+  if (tw) cudaFree(tw);
+  if (buf) cudaFree(buf);
+  return rc;
 }
 
 // first energy slot of the nonlocal (beta-projector) partials, one per (s,k)
@@ -178,6 +214,8 @@ int jrg_plan_destroy(jrg_plan* P) {
                   P->d.rowmap};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (P->prec == 32 && P->d.vext64) cudaFree(P->d.vext64);
+  if (P->d.vext_r) cudaFree(P->d.vext_r);
   if (P->slot_begin) cudaFree(P->slot_begin);
   if (P->d_cell) cudaFree(P->d_cell);
   if (P->d_atoms) cudaFree(P->d_atoms);
@@ -358,7 +396,12 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
     if (P->prec == 64) {
       rc = up(&P->d.tw, tw.data(), tw.size() * sizeof(double));
     } else {
-      std::vector<float> twf(tw.begin(), tw.end());
+      std::vector<float> twf(tw.size());
+      for (size_t t = 0; t < tw.size() / 2; ++t) {
+        const float2 w = balanced_twiddle(tw[2 * t], tw[2 * t + 1]);
+        twf[2 * t] = w.x;
+        twf[2 * t + 1] = w.y;
+      }
       rc = up(&P->d.tw, twf.data(), twf.size() * sizeof(float));
     }
   }
@@ -392,16 +435,19 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
     cudaError_t e = cudaMalloc((void**)&P->d.gvec, 3 * P->ngrid * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc((void**)&P->d.ginv, P->ngrid * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&P->d.vext, P->ngrid * csize(P->prec));
+    if (e == cudaSuccess && P->prec == 32) e = cudaMalloc((void**)&P->d.vext64, P->ngrid * sizeof(double2));
+    if (e == cudaSuccess && P->prec == 64) P->d.vext64 = (double2*)P->d.vext;
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaMalloc(geometry tables)");
   }
   if (!rc) {
     if (P->prec == 64)
-      rc = launch_geometry_tables<double>(P->d.gvec, P->d.ginv, P->d.vext, d_recip, d_pos, d_chg,
+      rc = launch_geometry_tables<double>(P->d.gvec, P->d.ginv, P->d.vext, nullptr, d_recip, d_pos, d_chg,
                                           d->num_atom, P->nx, P->ny, P->nz, P->vol, 0);
     else
-      rc = launch_geometry_tables<float>(P->d.gvec, P->d.ginv, P->d.vext, d_recip, d_pos, d_chg,
+      rc = launch_geometry_tables<float>(P->d.gvec, P->d.ginv, P->d.vext, P->d.vext64, d_recip, d_pos, d_chg,
                                          d->num_atom, P->nx, P->ny, P->nz, P->vol, 0);
   }
+  if (!rc) rc = make_vext_real(P);
   layout_workspace(P);
   if (!rc) rc = upload_slot_layout(P);
   if (!rc) {
@@ -437,6 +483,11 @@ int jrg_plan_set_pseudopotential(jrg_plan* P, const double* v_local, int num_pro
   };
   int rc;
   if (v_local && (rc = upload(v_local, (size_t)P->ngrid, P->d.vext))) return rc;
+  if (v_local && P->prec == 32) {
+    cudaError_t e = cudaMemcpy(P->d.vext64, v_local, (size_t)P->ngrid * sizeof(double2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(pseudopotential table)");
+  }
+  if (v_local && (rc = make_vext_real(P))) return rc;
   if (P->d.proj) {
     cudaFree(P->d.proj);
     P->d.proj = nullptr;
@@ -541,11 +592,15 @@ static int gga_gradients(const jrg_plan* P, const C_t<R>* rhog, void* ws, cudaSt
 }
 
 // Step 2: local terms (E_xc partials into slot_x, f_rho into vout) and, for the
-// potential, vout = Re(vri) vscale + f_rho - 2 div(f_sigma grad rho); with
-// eps_only, vout = eps(rho, sigma) per particle instead.
+// potential, vout = Re(vri) vscale + f_rho - 2 div(f_sigma grad rho) (+ V_ext(r)
+// and its energy partials into slot_e when vext_r is given); with eps_only,
+// vout = eps(rho, sigma) per particle instead.  qscale: the density factor of
+// ChargeFix (null: 1).
 template <typename R>
 static int gga_potential(const jrg_plan* P, const void* rho, const C_t<R>* vri, double vscale,
-                         void* vout, double* slot_x, int eps_only, void* ws, cudaStream_t st) {
+                         void* vout, double* slot_x, int eps_only, void* ws, cudaStream_t st,
+                         const double* qscale = nullptr, const double* vext_r = nullptr,
+                         double* slot_e = nullptr) {
   using C = C_t<R>;
   const Workspace& w = P->ws;
   C* g = (C*)wsp(ws, w.gga);
@@ -556,7 +611,7 @@ static int gga_potential(const jrg_plan* P, const void* rho, const C_t<R>* vri, 
   const double N = (double)P->ngrid;
   int rc;
   if ((rc = launch_gga_local<R>(rho, g, g1, g2, vout, slot_x, kXcBlocks, P->ngrid, P->xc,
-                                P->vol / N, eps_only, st)))
+                                P->vol / N, eps_only, qscale, vext_r, slot_e, st)))
     return rc;
   if (eps_only) return JRG_OK;
   for (int a = 0; a < 3; ++a) {
@@ -565,7 +620,7 @@ static int gga_potential(const jrg_plan* P, const void* rho, const C_t<R>* vri, 
   }
   if ((rc = launch_div_g<R>(g, g1, g2, P->d.gvec, P->ngrid, 1.0 / N, st))) return rc;
   if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, g, scratch, g, 1.0, st))) return rc;
-  return launch_potential_gga<R>(vri, vscale, vout, g, P->ngrid, st);
+  return launch_potential_gga<R>(vri, vscale, vout, g, P->ngrid, vext_r, st);
 }
 
 // Nonlocal pseudopotential term of the (s,k) blocks [k0, k0+n): F = C P and
@@ -606,10 +661,11 @@ static int sum_energy_slots(const jrg_plan* P, double* slots, double* energies, 
                           P->nproj > 0 ? 1 : -1, st);
 }
 
-// density of the band-major coefficients held in workspace slot c
+// density of the band-major coefficients held in workspace slot c (qpart:
+// the charge partials of ChargeFix, or null)
 template <typename R>
 static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* rho_out,
-                          cudaStream_t st) {
+                          cudaStream_t st, double* qpart = nullptr) {
   const Workspace& w = P->ws;
   const int nbt = P->ns * P->nk * P->nb;
   int rc;
@@ -620,11 +676,54 @@ static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* 
   {
     PHASE(PH_LINE_DENSITY);
     if ((rc = launch_line_density<R>(P, wsp(ws, w.t), wsp(ws, w.rho_part), occ, 1.0 / P->vol, 0,
-                                     nbt, P->nb, st)))
+                                     nbt, P->nb, (double*)wsp(ws, w.rho_scale), st)))
       return rc;
   }
   PHASE(PH_REDUCE_DENSITY);
-  return launch_reduce_density<R>(wsp(ws, w.rho_part), rho_out, P->nk, P->ns, P->ngrid, st);
+  return launch_reduce_density<R>(wsp(ws, w.rho_part), rho_out, P->nk, P->ns, P->ngrid,
+                                  (const double*)wsp(ws, w.rho_scale), qpart, st);
+}
+
+// Grid phase of the energy path on the density in workspace slot rho (with
+// its charge partials in rho_q): rho(G); the charge factor s (ChargeFix);
+// Hartree energy and potential in G space; xc and external energies and
+// V(r) = V_H + v_xc + V_ext on the grid (external from the FP64 V_ext(r)
+// table).  Energy partials go to the external, Hartree and xc slots.
+template <typename R>
+static int grid_phase(const jrg_plan* P, const double* occ, double* slots, void* ws, cudaStream_t st) {
+  using C = C_t<R>;
+  static_assert(kRecipBlocks == kXcBlocks, "external partials are written by the xc kernels");
+  const Workspace& w = P->ws;
+  const int nbt = P->ns * P->nk * P->nb;
+  const double N = (double)P->ngrid;
+  void* rho = wsp(ws, w.rho);
+  C* rhog = (C*)wsp(ws, w.rhog);
+  C* scratch = (C*)wsp(ws, w.fft_scratch);
+  const C* tw = (const C*)P->d.tw;
+  double* q = (double*)wsp(ws, w.rho_q);
+  ChargeFix cf;
+  cf.qpart = q;
+  cf.occ = occ;
+  cf.nocc = nbt;
+  cf.dv = P->vol / N;
+  cf.scale = q + kQParts;
+  double* slot_e = slots + nbt;
+  double* slot_h = slots + nbt + kRecipBlocks;
+  double* slot_x = slots + nbt + 2 * kRecipBlocks;
+  int rc;
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+  const bool gga = (P->xc & kXcGga) != 0;
+  if (gga && (rc = gga_gradients<R>(P, rhog, ws, st))) return rc;
+  // Hartree energy and V_H(G) (in place)
+  if ((rc = launch_recip_terms<R>(rhog, P->d.ginv, rhog, slot_h, kRecipBlocks, P->ngrid, P->vol / (N * N),
+                                  cf, st)))
+    return rc;
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st))) return rc;
+  if (gga)
+    return gga_potential<R>(P, rho, rhog, 1.0, wsp(ws, w.vr), slot_x, 0, ws, st, cf.scale, P->d.vext_r,
+                            slot_e);
+  return launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slot_x, kXcBlocks, P->ngrid, P->xc, P->vol / N,
+                             cf.scale, P->d.vext_r, slot_e, st);
 }
 
 template <typename R>
@@ -660,31 +759,10 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
       return rc;
   }
   if ((rc = nl_forward<R>(P, ws, 0, nsk, occ, band_e ? P->d_ones : occ, st))) return rc;
-  void* rho = wsp(ws, w.rho);
-  if ((rc = density_from_c<R>(P, occ, ws, rho, st))) return rc;
+  if ((rc = density_from_c<R>(P, occ, ws, wsp(ws, w.rho), st, (double*)wsp(ws, w.rho_q)))) return rc;
   {
     PHASE(PH_GRID_TERMS);
-    C* rhog = (C*)wsp(ws, w.rhog);
-    C* scratch = (C*)wsp(ws, w.fft_scratch);
-    const C* tw = (const C*)P->d.tw;
-    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
-    const bool gga = (P->xc & kXcGga) != 0;
-    if (gga && (rc = gga_gradients<R>(P, rhog, ws, st))) return rc;
-    // Hartree / external (slots after the kinetic ones) and dE/drho in G space (in place)
-    const double pref = P->vol / (N * N);
-    if ((rc = launch_recip_terms<R>(rhog, P->d.ginv, P->d.vext, rhog, slots + nbt + kRecipBlocks,
-                                    slots + nbt, kRecipBlocks, P->ngrid, pref, st)))
-      return rc;
-    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st)))
-      return rc;
-    if (gga) {
-      if ((rc = gga_potential<R>(P, rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks, 0,
-                                 ws, st)))
-        return rc;
-    } else if ((rc = launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks,
-                                         kXcBlocks, P->ngrid, P->xc, P->vol / N, st))) {
-      return rc;
-    }
+    if ((rc = grid_phase<R>(P, occ, slots, ws, st))) return rc;
     if ((rc = sum_energy_slots(P, slots, energies, ws, st))) return rc;
   }
   if (!adam && !g_re && !g_im) return JRG_OK;
@@ -831,7 +909,8 @@ static int phase_forward_range(const jrg_plan* P, const void* w_re, const void* 
   if ((rc = launch_plane_inv_sphere<R>(P, (C*)wsp(ws, w.c) + co, (C*)wsp(ws, w.t) + to, n * P->nb, st)))
     return rc;
   return launch_line_density<R>(P, (C*)wsp(ws, w.t) + to, (R*)wsp(ws, w.rho_part) + (size_t)k0 * P->ngrid,
-                                occ, 1.0 / P->vol, k0 * P->nb, n * P->nb, P->nb, st);
+                                occ, 1.0 / P->vol, k0 * P->nb, n * P->nb, P->nb,
+                                (double*)wsp(ws, w.rho_scale) + k0, st);
 }
 
 // With adam given, the gradient of the half goes to adam->grad (when set) or
@@ -927,30 +1006,10 @@ static int energy_grad_pipelined(const jrg_plan* P, const void* w_re, const void
                                  P->nk, P->ng, P->nb, (long long)nbt * P->ng, adam->t_frac, adam->smax,
                                  adam->scale[0], st)))
     return rc;
-  void* rho = wsp(ws, w.rho);
-  if ((rc = launch_reduce_density<R>(wsp(ws, w.rho_part), rho, P->nk, P->ns, P->ngrid, st))) return rc;
-  {
-    C* rhog = (C*)wsp(ws, w.rhog);
-    C* scratch = (C*)wsp(ws, w.fft_scratch);
-    const C* tw = (const C*)P->d.tw;
-    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
-    const bool gga = (P->xc & kXcGga) != 0;
-    if (gga && (rc = gga_gradients<R>(P, rhog, ws, st))) return rc;
-    const double pref = P->vol / (N * N);
-    if ((rc = launch_recip_terms<R>(rhog, P->d.ginv, P->d.vext, rhog, slots + nbt + kRecipBlocks,
-                                    slots + nbt, kRecipBlocks, P->ngrid, pref, st)))
-      return rc;
-    if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st)))
-      return rc;
-    if (gga) {
-      if ((rc = gga_potential<R>(P, rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks, 0,
-                                 ws, st)))
-        return rc;
-    } else if ((rc = launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slots + nbt + 2 * kRecipBlocks,
-                                         kXcBlocks, P->ngrid, P->xc, P->vol / N, st))) {
-      return rc;
-    }
-  }
+  if ((rc = launch_reduce_density<R>(wsp(ws, w.rho_part), wsp(ws, w.rho), P->nk, P->ns, P->ngrid,
+                                     (const double*)wsp(ws, w.rho_scale), (double*)wsp(ws, w.rho_q), st)))
+    return rc;
+  if ((rc = grid_phase<R>(P, occ, slots, ws, st))) return rc;
   // the energy sums feed only the energies output: they run after the adjoint
   // halves, off the path between the two forks
   if (!adam && !g_re && !g_im) return sum_energy_slots(P, slots, energies, ws, st);

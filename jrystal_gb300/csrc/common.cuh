@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <math.h>
 
 namespace jrg {
 
@@ -34,6 +35,50 @@ __host__ __device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
 __host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 __host__ __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 template <typename C> __host__ __device__ __forceinline__ C czero() { C r; r.x = 0; r.y = 0; return r; }
+
+// FP32 twiddle for the FP64 pair (c, s) = (cos, sin): of the floats next to c
+// and next to s (one each side, or the value itself when exact), the pair
+// whose squared norm c^2 + s^2 is closest to 1, the nearest pair on ties.
+// Nearest rounding alone leaves every |w|^2 - 1 at up to 1e-7 with a sum over
+// a table that does not cancel, i.e. a fixed norm loss or gain of every
+// transform that uses the table.
+__host__ __device__ inline float2 balanced_twiddle(double c, double s) {
+  const float c0 = (float)c, s0 = (float)s;
+  const float c1 = (double)c0 == c ? c0 : nextafterf(c0, (double)c0 < c ? 2.f : -2.f);
+  const float s1 = (double)s0 == s ? s0 : nextafterf(s0, (double)s0 < s ? 2.f : -2.f);
+  float2 best = make_float2(c0, s0);
+  double be = fabs((double)c0 * c0 + (double)s0 * s0 - 1.0);
+  const float cs[2] = {c0, c1}, ss[2] = {s0, s1};
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      const double e = fabs((double)cs[i] * cs[i] + (double)ss[j] * ss[j] - 1.0);
+      if (e < be) { be = e; best = make_float2(cs[i], ss[j]); }
+    }
+  return best;
+}
+
+// Weights of a band group for the density partials, formed by warp 0 of the
+// block (the FP64 work stays off the other warps): sw[b - b_begin] = w[b] /
+// w_ref with w_ref the largest |w| of w[b_begin, b_end) (ratios 0 when all are
+// zero), and, in x-block 0, gscale[grp] = w_ref * wscale.  Partials are
+// accumulated with the ratios and scaled by gscale in FP64 when reduced.
+// The caller synchronises the block before reading sw.
+template <typename R>
+__device__ __forceinline__ void group_weights(const double* __restrict__ w, int b_begin, int b_end,
+                                              double wscale, double* __restrict__ gscale, int grp,
+                                              R* sw) {
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  double wref = 0.0;
+  for (int b = b_begin + lane; b < b_end; b += 32) wref = fmax(wref, fabs(w[b]));
+  for (int o = 16; o > 0; o >>= 1) wref = fmax(wref, __shfl_xor_sync(0xffffffffu, wref, o));
+  const double winv = wref > 0.0 ? 1.0 / wref : 0.0;
+  for (int b = b_begin + lane; b < b_end; b += 32) sw[b - b_begin] = (R)(w[b] * winv);
+  if (lane == 0 && blockIdx.x == 0) gscale[grp] = wref * wscale;
+}
+
+// bytes of the group-weight array of the density kernels (16-byte aligned start)
+__host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 // Block-wide sum of a double (all threads get the result).  blockDim.x must
 // be a multiple of 32 and at most 1024.

@@ -12,6 +12,7 @@ struct Args {
   const double* w;
   double wscale;        // density weight scale, or the FFT scale of plane fwd
   int band0, nbands, bands_per_group;
+  double* gscale;       // density: per band group, the FP64 factor of its partial
 };
 // 1: launched, 0: grid not covered (use the generic kernels), <0: -status
 template <typename R> int dispatch(const jrg_plan* P, int op, const Args& a, cudaStream_t st);

@@ -92,11 +92,33 @@ template <int DIR, int K, int N, typename C> __host__ __device__ __forceinline__
     constexpr double c = cos2pi(k, N);
     constexpr double s = DIR * sin2pi(k, N);
     C r;
-    r.x = (R)c * a.x - (R)s * a.y;
-    r.y = (R)c * a.y + (R)s * a.x;
+    if constexpr (sizeof(R) == 8) {
+      r.x = c * a.x - s * a.y;
+      r.y = c * a.y + s * a.x;
+    } else {
+      // FP32: each constant as hi + lo.  A constant rounded to float scales
+      // every product it touches by the same factor (sqrt(2)/2 rounds 1.7e-8
+      // low, so |w|^2 = 1 - 3.4e-8): the transform loses norm by a fixed
+      // fraction and the density by a fixed charge, which the energy sums
+      // see at first order.  With the lo part the products carry only the
+      // unbiased rounding of the arithmetic.
+      constexpr float ch = (float)c, cl = (float)(c - (double)ch);
+      constexpr float sh = (float)s, sl = (float)(s - (double)sh);
+      if constexpr (ch == sh || ch == -sh) {
+        // |cos| = |sin| (odd multiples of pi/4): w = ch (1 + i sign) (1 + lo/hi)
+        constexpr float sg = ch == sh ? 1.f : -1.f;
+        const float tx = a.x - sg * a.y, ty = a.y + sg * a.x;
+        r.x = fmaf(ch, tx, cl * tx);
+        r.y = fmaf(ch, ty, cl * ty);
+      } else {
+        r.x = fmaf(ch, a.x, fmaf(-sh, a.y, fmaf(cl, a.x, -sl * a.y)));
+        r.y = fmaf(ch, a.y, fmaf(sh, a.x, fmaf(cl, a.y, sl * a.x)));
+      }
+    }
     return r;
   }
 }
+
 
 // ---- register DFTs ----------------------------------------------------------
 template <int N, int DIR, typename C> __host__ __device__ __forceinline__ void dft(C (&v)[N]);
@@ -118,9 +140,18 @@ template <int N, int DIR, typename C> __host__ __device__ __forceinline__ void d
     C t1 = cadd(v[1], v[2]);
     C d = csub(v[1], v[2]);
     C t2 = csub(v[0], cscale(t1, (R)0.5));
-    C id;   // DIR * i * sqrt(3)/2 * d
-    if (DIR > 0) { id.x = -(R)s3 * d.y; id.y = (R)s3 * d.x; }
-    else { id.x = (R)s3 * d.y; id.y = -(R)s3 * d.x; }
+    if constexpr (sizeof(R) == 4) {
+      // sqrt(3)/2 as hi + lo (see twiddle_mul)
+      constexpr float h = (float)s3, l = (float)(s3 - (double)h);
+      d.x = fmaf(h, d.x, l * d.x);
+      d.y = fmaf(h, d.y, l * d.y);
+    } else {
+      d.x *= s3;
+      d.y *= s3;
+    }
+    C id;   // DIR * i * sqrt(3)/2 * (v1 - v2)
+    if (DIR > 0) { id.x = -d.y; id.y = d.x; }
+    else { id.x = d.y; id.y = -d.x; }
     v[0] = cadd(v[0], t1);
     v[1] = cadd(t2, id);
     v[2] = csub(t2, id);

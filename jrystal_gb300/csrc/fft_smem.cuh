@@ -50,11 +50,21 @@ __device__ __forceinline__ void small_dft(C (&v)[RAD], const C* tw, int n) {
     v[0] = cadd(a, b); v[1] = csub(a, b);
   } else if constexpr (RAD == 3) {
     using R = decltype(v[0].x);
-    const R s3 = (R)0.86602540378443864676;   // sqrt(3)/2
+    constexpr double s3 = 0.86602540378443864676;   // sqrt(3)/2
     C t1 = cadd(v[1], v[2]);
     C d = csub(v[1], v[2]);
     C t2 = csub(v[0], cscale(t1, (R)0.5));
-    C id = cscale(mul_pm_i<DIR>(d), s3);      // DIR*i*sqrt(3)/2*(v1-v2)
+    if constexpr (sizeof(R) == 4) {
+      // sqrt(3)/2 as hi + lo: a constant rounded to float would scale the
+      // norm of every transform by the same factor
+      constexpr float h = (float)s3, l = (float)(s3 - (double)h);
+      d.x = fmaf(h, d.x, l * d.x);
+      d.y = fmaf(h, d.y, l * d.y);
+    } else {
+      d.x *= s3;
+      d.y *= s3;
+    }
+    C id = mul_pm_i<DIR>(d);                  // DIR*i*sqrt(3)/2*(v1-v2)
     v[0] = cadd(v[0], t1);
     v[1] = cadd(t2, id);
     v[2] = csub(t2, id);

@@ -56,6 +56,12 @@ __global__ void __launch_bounds__(256) k_plane_inv_sphere(
 // ------------------------------------------------------------------------
 // inverse x transform + occupation-weighted |psi|^2 of a band group
 // ------------------------------------------------------------------------
+// shared memory of the line kernels: twiddles, two slabs, extra reals and ints
+template <typename R> __host__ __device__ size_t line_smem(int nx, int nz, int extra_real, int extra_int) {
+  return sizeof(C_t<R>) * (size_t)(nx + 2 * nx * nz) + sizeof(R) * (size_t)extra_real +
+         sizeof(int) * (size_t)extra_int;
+}
+
 constexpr int kLineThreads = 256;
 constexpr int kMaxPtsPerThread = 48;   // nx*nz <= 256*48 (up to 96 x 128)
 
@@ -64,7 +70,7 @@ __global__ void __launch_bounds__(kLineThreads) k_line_density(
     const C_t<R>* __restrict__ planes, R* __restrict__ rho_part, const double* __restrict__ wband,
     double wscale, int band0, int nband, int bands_per_group, const int* __restrict__ plane_x,
     const int* __restrict__ xact, const C_t<R>* __restrict__ tw_x, FftAxis axx, int nx, int ny,
-    int nz, int nact) {
+    int nz, int nact, double* __restrict__ gscale) {
   using C = C_t<R>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int slab = nx * nz;
@@ -72,18 +78,21 @@ __global__ void __launch_bounds__(kLineThreads) k_line_density(
   C* A = twx + nx;
   C* B = A + slab;
   int* sxact = reinterpret_cast<int*>(B + slab);
+  // weights relative to the group's largest (see the fast kernel)
+  R* sw = reinterpret_cast<R*>(smem_raw + align16(line_smem<R>(nx, nz, 0, nx)));
   const int y = blockIdx.x;
   const int grp = blockIdx.y;
+  const int b_begin = grp * bands_per_group;
+  const int b_end = min(nband, b_begin + bands_per_group);
   for (int i = threadIdx.x; i < nx; i += blockDim.x) { twx[i] = tw_x[i]; sxact[i] = xact[i]; }
+  group_weights<R>(wband + band0, b_begin, b_end, wscale, gscale, grp, sw);
   R acc[kMaxPtsPerThread];
 #pragma unroll
   for (int k = 0; k < kMaxPtsPerThread; ++k) acc[k] = (R)0;
   __syncthreads();
-  const int b_begin = grp * bands_per_group;
-  const int b_end = min(nband, b_begin + bands_per_group);
   const C z0 = czero<C>();
   for (int b = b_begin; b < b_end; ++b) {
-    const double w = wband[band0 + b] * wscale;
+    const R w = sw[b - b_begin];
     // inactive x rows are zero; active rows come from the plane buffer
     for (int i = threadIdx.x; i < slab; i += blockDim.x) {
       const int x = i / nz, z = i - x * nz;
@@ -97,7 +106,7 @@ __global__ void __launch_bounds__(kLineThreads) k_line_density(
       const int i = threadIdx.x + k * blockDim.x;
       if (i < slab) {
         const C v = res[i];
-        acc[k] += (R)w * (v.x * v.x + v.y * v.y);
+        acc[k] += w * (v.x * v.x + v.y * v.y);
       }
     }
     __syncthreads();
@@ -280,10 +289,6 @@ __global__ void __launch_bounds__(kLineThreads) k_line_dense(const C_t<R>* __res
 template <typename R> size_t plane_smem(int ny, int nz, int max_rows) {
   return sizeof(C_t<R>) * (size_t)(ny + nz + 2 * ny * nz) + sizeof(int) * (size_t)(max_rows + 1);
 }
-template <typename R> size_t line_smem(int nx, int nz, int extra_real, int extra_int) {
-  return sizeof(C_t<R>) * (size_t)(nx + 2 * nx * nz) + sizeof(R) * (size_t)extra_real +
-         sizeof(int) * (size_t)extra_int;
-}
 
 template <typename K> static int set_smem(K kernel, size_t bytes) {
   if (bytes > 48 * 1024) {
@@ -318,23 +323,24 @@ int launch_plane_inv_sphere(const jrg_plan* P, const void* coef, void* planes, i
 
 template <typename R>
 int launch_line_density(const jrg_plan* P, const void* planes, void* rho_part, const double* wband,
-                        double wscale, int band0, int nbands, int bands_per_group, cudaStream_t st) {
+                        double wscale, int band0, int nbands, int bands_per_group, double* gscale,
+                        cudaStream_t st) {
   using C = C_t<R>;
   {
-    fast::Args a{planes, rho_part, nullptr, wband, wscale, band0, nbands, bands_per_group};
+    fast::Args a{planes, rho_part, nullptr, wband, wscale, band0, nbands, bands_per_group, gscale};
     const int f = fast::dispatch<R>(P, fast::OP_LINE_DENSITY, a, st);
     if (f < 0) return -f;
     if (f > 0) return JRG_OK;
   }
   const C* tw = reinterpret_cast<const C*>(P->d.tw);
-  size_t sm = line_smem<R>(P->nx, P->nz, 0, P->nx);
+  size_t sm = align16(line_smem<R>(P->nx, P->nz, 0, P->nx)) + sizeof(R) * (size_t)bands_per_group;
   int rc = set_smem(k_line_density<R>, sm);
   if (rc) return rc;
   const int ngroups = (nbands + bands_per_group - 1) / bands_per_group;
   dim3 grid(P->ny, ngroups);
   k_line_density<R><<<grid, kLineThreads, sm, st>>>(
       reinterpret_cast<const C*>(planes), reinterpret_cast<R*>(rho_part), wband, wscale, band0, nbands,
-      bands_per_group, P->d.plane_x, P->d.xact, tw, P->ax[0], P->nx, P->ny, P->nz, P->nact);
+      bands_per_group, P->d.plane_x, P->d.xact, tw, P->ax[0], P->nx, P->ny, P->nz, P->nact, gscale);
   JRG_LAUNCH_CHECK("k_line_density");
   return JRG_OK;
 }
@@ -436,7 +442,7 @@ int launch_fft3d_dense(const FftAxis* ax, const C_t<R>* tw, int batch, int dir, 
 #define JRG_INST(R)                                                                              \
   template int launch_plane_inv_sphere<R>(const jrg_plan*, const void*, void*, int, cudaStream_t); \
   template int launch_line_density<R>(const jrg_plan*, const void*, void*, const double*, double, \
-                                      int, int, int, cudaStream_t);                              \
+                                      int, int, int, double*, cudaStream_t);                     \
   template int launch_line_apply_v<R>(const jrg_plan*, const void*, void*, const void*, int, int,   \
                                       cudaStream_t);                                             \
   template int launch_plane_fwd_sphere<R>(const jrg_plan*, const void*, const void*, void*,        \

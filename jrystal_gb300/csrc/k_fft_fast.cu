@@ -29,6 +29,10 @@ template <typename R, int N> constexpr int min_blocks_for() {
 }
 
 // byte offset of the prefetch row buffers in a line kernel's shared memory
+// group weights of k_line_density, after the twiddles, exchange buffers and xact
+template <typename R, int N> __host__ __device__ constexpr size_t line_w_offset() {
+  return align16(sizeof(C_t<R>) * (size_t)(N + 2 * N * N) + sizeof(int) * N);
+}
 template <typename R, int N> __host__ __device__ constexpr size_t line_pf_offset() {
   return (sizeof(C_t<R>) * (size_t)(N + 2 * N * N) + sizeof(int) * N + 15) / 16 * 16;
 }
@@ -207,13 +211,18 @@ __device__ __forceinline__ void prefetch_row(const C_t<R>* __restrict__ planes, 
 
 // inverse x transform + occupation-weighted |psi|^2 of a band group (one
 // transform per band: the row prefetch of the adjoint pass measured slower
-// here, 0.30 vs 0.25 ms on the 64^3 Si8 cell)
+// here, 0.30 vs 0.25 ms on the 64^3 Si8 cell).  The partial of a group holds
+// sum_b (w_b / w_ref) |psi_b|^2 with w_ref the group's largest weight, and
+// gscale[grp] = w_ref * wscale (FP64) is applied by the density reduction: a
+// weight rounded to FP32 would scale the whole group's charge (the usual
+// case, every occupied band of a k-point has the same weight) by one
+// rounding error; the ratio of equal weights is exactly 1.
 // PR (N = 32, 64): the thread's inputs v[2..5] (x = N/4 .. 3N/4 - 1) are known zero
 template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_line_density(
     const C_t<R>* __restrict__ planes, R* __restrict__ rho_part, const double* __restrict__ wband,
     double wscale, int band0, int nband, int bands_per_group, const int* __restrict__ xact,
-    const C_t<R>* __restrict__ tw_g, int nact) {
+    const C_t<R>* __restrict__ tw_g, int nact, double* __restrict__ gscale) {
   using C = C_t<R>;
   constexpr int N1 = Split<N>::N1, N2 = Split<N>::N2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -221,9 +230,13 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
   C* ex0 = tw + N;
   C* ex1 = ex0 + N * N;
   int* sxact = reinterpret_cast<int*>(ex1 + N * N);
+  R* sw = reinterpret_cast<R*>(smem_raw + line_w_offset<R, N>());   // [bands_per_group]
   const int y = blockIdx.x, grp = blockIdx.y, tid = threadIdx.x;
   const int z = tid % N, j2 = tid / N;
+  const int b_begin = grp * bands_per_group;
+  const int b_end = min(nband, b_begin + bands_per_group);
   for (int i = tid; i < N; i += blockDim.x) { tw[i] = tw_g[i]; sxact[i] = xact[i]; }
+  group_weights<R>(wband + band0, b_begin, b_end, wscale, gscale, grp, sw);
   __syncthreads();
   int slot[N1];
 #pragma unroll
@@ -231,8 +244,6 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
   R acc[N1];
 #pragma unroll
   for (int j = 0; j < N1; ++j) acc[j] = (R)0;
-  const int b_begin = grp * bands_per_group;
-  const int b_end = min(nband, b_begin + bands_per_group);
   const C z0 = czero<C>();
   C v[N1];
   // PR: the four non-zero inputs of the next band are loaded while the
@@ -249,7 +260,7 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
   if (PR && b_begin < b_end) load4(b_begin);
   int parity = 0;
   for (int b = b_begin; b < b_end; ++b, parity ^= 1) {
-    const R w = (R)(wband[band0 + b] * wscale);
+    const R w = sw[b - b_begin];
     if constexpr (PR) {
       v[0] = nxt[0]; v[1] = nxt[1]; v[6] = nxt[2]; v[7] = nxt[3];
       if (b + 1 < b_end) load4(b + 1);
@@ -749,12 +760,12 @@ static int line_density_launch(const jrg_plan* P, const Args& a, const C_t<R>* t
   using C = C_t<R>;
   constexpr int T = threads_for<N>();
   int rc;
-  const size_t sm = line_smem<R, N>();
+  const size_t sm = line_w_offset<R, N>() + sizeof(R) * (size_t)a.bands_per_group;
   if ((rc = prep(k_line_density<R, N, PR>, sm)) <= 0) return rc;
   const int ngroups = (a.nbands + a.bands_per_group - 1) / a.bands_per_group;
   k_line_density<R, N, PR><<<dim3(N, ngroups), T, sm, st>>>(
       reinterpret_cast<const C*>(a.in), reinterpret_cast<R*>(a.out), a.w, a.wscale, a.band0,
-      a.nbands, a.bands_per_group, P->d.xact, tw, P->nact);
+      a.nbands, a.bands_per_group, P->d.xact, tw, P->nact, a.gscale);
   FAST_LAUNCHED("fast::k_line_density");
 }
 

@@ -6,49 +6,114 @@
 
 namespace jrg {
 
-// rho[s][i] = sum over the groups of spin s of part[g][i] (FP64 sum)
+// rho[s][i] = sum over the groups g of spin s of gscale[g] part[g][i] (FP64
+// sum; gscale = the group's reference weight over the cell volume); with
+// qpart, block b also stores the FP64 sum of the rho values it wrote
+// (kQParts blocks)
+// FP32 partials are summed in float-float arithmetic (each gscale as hi + lo,
+// exact products by FMA, two-sum accumulation: about 2^-44 relative, with
+// FP32 instructions instead of the GPU's slow FP64 pipe); FP64 partials in
+// FP64.  Group factors are staged in shared memory (groups_per_spin * ns <=
+// kMaxReduceGroups, else read from global memory).
+constexpr int kMaxReduceGroups = 1024;
 template <typename R>
-__global__ void k_reduce_density(const R* __restrict__ part, R* __restrict__ rho, int groups_per_spin,
-                                 int ns, long long ngrid) {
+__global__ void __launch_bounds__(256) k_reduce_density(const R* __restrict__ part, R* __restrict__ rho,
+                                                        int groups_per_spin, int ns, long long ngrid,
+                                                        const double* __restrict__ gscale,
+                                                        double* __restrict__ qpart) {
+  __shared__ double red[32];
+  __shared__ float2 sg[kMaxReduceGroups];   // gscale as (hi, lo)
+  const int ngr = groups_per_spin * ns;
+  const bool staged = ngr <= kMaxReduceGroups;
+  if (staged)
+    for (int g = threadIdx.x; g < ngr; g += blockDim.x) {
+      const float h = (float)gscale[g];
+      sg[g] = make_float2(h, (float)(gscale[g] - (double)h));
+    }
+  __syncthreads();
   const long long n = (long long)ns * ngrid;
+  double q = 0.0;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
        e += (long long)gridDim.x * blockDim.x) {
     const long long s = e / ngrid, i = e % ngrid;
-    double acc = 0.0;
-    for (int g = 0; g < groups_per_spin; ++g) acc += (double)part[((long long)s * groups_per_spin + g) * ngrid + i];
-    rho[e] = (R)acc;
+    R r;
+    if constexpr (sizeof(R) == 4) {
+      float sh = 0.f, sl = 0.f;
+      for (int g = 0; g < groups_per_spin; ++g) {
+        const long long gg = (long long)s * groups_per_spin + g;
+        float2 f;
+        if (staged) {
+          f = sg[gg];
+        } else {
+          f.x = (float)gscale[gg];
+          f.y = (float)(gscale[gg] - (double)f.x);
+        }
+        const float x = part[gg * ngrid + i];
+        const float p = x * f.x;
+        const float pe = fmaf(x, f.y, fmaf(x, f.x, -p));   // exact low part of x*hi, plus x*lo
+        const float t = sh + p;                            // two-sum of sh and p
+        const float bb = t - sh;
+        const float te = (sh - (t - bb)) + (p - bb);
+        sh = t;
+        sl += te + pe;
+      }
+      r = (R)((double)sh + (double)sl);
+    } else {
+      double acc = 0.0;
+      for (int g = 0; g < groups_per_spin; ++g) {
+        const long long gg = (long long)s * groups_per_spin + g;
+        acc += gscale[gg] * (double)part[gg * ngrid + i];
+      }
+      r = (R)acc;
+    }
+    rho[e] = r;
+    q += (double)r;
+  }
+  if (qpart) {
+    q = block_sum(q, red);
+    if (threadIdx.x == 0) qpart[blockIdx.x] = q;
   }
 }
 
-// Reciprocal-space terms of a single (spin-summed) density transform rhog:
-//   E_H  = vol/N^2 * sum 1/2 ginv |rho_G|^2          (ginv = 4 pi/|G|^2, 0 at G=0)
-//   E_ext= vol/N^2 * sum Re(conj(Vext_G) rho_G)
-//   vg   = ginv * rho_G + Vext_G   (dE/d rho, reciprocal form, before the 1/N of the IFFT)
+// the charge factor s of ChargeFix (every thread of the block gets it)
+__device__ __forceinline__ double charge_scale(const ChargeFix& cf, double* red) {
+  if (!cf.qpart) return 1.0;
+  double a = 0.0, t = 0.0;
+  for (int i = threadIdx.x; i < kQParts; i += blockDim.x) a += cf.qpart[i];
+  for (int i = threadIdx.x; i < cf.nocc; i += blockDim.x) t += cf.occ[i];
+  a = block_sum(a, red) * cf.dv;
+  t = block_sum(t, red);
+  return (a > 0.0 && t > 0.0) ? t / a : 1.0;
+}
+
+// Hartree term of a single (spin-summed) density transform rhog, for the
+// renormalised density s rho (s from ChargeFix; block 0 stores it):
+//   E_H = vol/N^2 * sum 1/2 ginv |s rho_G|^2          (ginv = 4 pi/|G|^2, 0 at G=0)
+//   vg  = ginv * s rho_G   (the Hartree potential, before the 1/N of the IFFT)
+// The external energy and potential are taken in real space from the FP64
+// V_ext(r) table by the potential kernels (Parseval: the same sum).
 template <typename R>
 __global__ void __launch_bounds__(256) k_recip_terms(const C_t<R>* __restrict__ rhog,
                                                      const double* __restrict__ ginv,
-                                                     const C_t<R>* __restrict__ vext,
                                                      C_t<R>* __restrict__ vg, double* __restrict__ slot_h,
-                                                     double* __restrict__ slot_e, long long ngrid,
-                                                     double pref) {
+                                                     long long ngrid, double pref, ChargeFix cf) {
   __shared__ double red[32];
-  double eh = 0.0, ee = 0.0;
+  const double s = charge_scale(cf, red);
+  if (cf.scale && blockIdx.x == 0 && threadIdx.x == 0) *cf.scale = s;
+  double eh = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
        i += (long long)gridDim.x * blockDim.x) {
     const C_t<R> r = rhog[i];
-    const C_t<R> v = vext[i];
     const double gi = ginv[i];
     const double rx = r.x, ry = r.y;
     eh += 0.5 * gi * (rx * rx + ry * ry);
-    ee += (double)v.x * rx + (double)v.y * ry;
     C_t<R> o;
-    o.x = (R)(gi * rx + (double)v.x);
-    o.y = (R)(gi * ry + (double)v.y);
+    o.x = (R)(s * gi * rx);
+    o.y = (R)(s * gi * ry);
     if (vg) vg[i] = o;
   }
   eh = block_sum(eh, red);
-  ee = block_sum(ee, red);
-  if (threadIdx.x == 0) { slot_h[blockIdx.x] = eh * pref; slot_e[blockIdx.x] = ee * pref; }
+  if (threadIdx.x == 0) slot_h[blockIdx.x] = eh * pref * s * s;
 }
 
 // LDA: Slater exchange + VWN (1980) paramagnetic correlation fit.
@@ -205,13 +270,19 @@ template <typename R>
 __global__ void __launch_bounds__(256) k_gga_local(const R* __restrict__ rho, C_t<R>* __restrict__ g0,
                                                    C_t<R>* __restrict__ g1, C_t<R>* __restrict__ g2,
                                                    R* __restrict__ vloc, double* __restrict__ slot_x,
-                                                   long long n, int xc, double pref, int eps_only) {
+                                                   long long n, int xc, double pref, int eps_only,
+                                                   const double* __restrict__ qscale,
+                                                   const double* __restrict__ vext_r,
+                                                   double* __restrict__ slot_e) {
   __shared__ double red[32];
-  double ex = 0.0;
+  // renormalised density s rho and its gradients (ChargeFix), 1 without qscale
+  const double s = qscale ? *qscale : 1.0;
+  double ex = 0.0, ee = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const double r = rho[i];
-    const double d0 = g0[i].x, d1 = g1[i].x, d2 = g2[i].x;
+    const double r = s * (double)rho[i];
+    if (vext_r) ee += vext_r[i] * r;
+    const double d0 = s * (double)g0[i].x, d1 = s * (double)g1[i].x, d2 = s * (double)g2[i].x;
     const double sig = d0 * d0 + d1 * d1 + d2 * d2;
     double fr = 0.0, fs = 0.0, fe = 0.0;
     if (r > 1e-15) {
@@ -228,6 +299,10 @@ __global__ void __launch_bounds__(256) k_gga_local(const R* __restrict__ rho, C_
   }
   ex = block_sum(ex, red);
   if (threadIdx.x == 0 && slot_x) slot_x[blockIdx.x] = ex * pref;
+  if (slot_e) {
+    ee = block_sum(ee, red);
+    if (threadIdx.x == 0) slot_e[blockIdx.x] = ee * pref;
+  }
 }
 
 // g0 = scale * sum_a i G_a h_a   (divergence in reciprocal space)
@@ -249,36 +324,56 @@ __global__ void k_div_g(C_t<R>* __restrict__ g0, const C_t<R>* __restrict__ g1,
   }
 }
 
-// vr = Re(vri) * vscale + vr - 2 Re(div)   (vr holds f_rho on entry; vri may be null)
+// vr = Re(vri) * vscale + vr - 2 Re(div) + V_ext(r)   (vr holds f_rho on
+// entry; vri and vext_r may be null)
 template <typename R>
 __global__ void k_potential_gga(const C_t<R>* __restrict__ vri, double vscale, R* __restrict__ vr,
-                                const C_t<R>* __restrict__ div, long long n) {
+                                const C_t<R>* __restrict__ div, long long n,
+                                const double* __restrict__ vext_r) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    const double base = vri ? (double)vri[i].x * vscale : 0.0;
+    double base = vri ? (double)vri[i].x * vscale : 0.0;
+    if (vext_r) base += vext_r[i];
     vr[i] = (R)(base + (double)vr[i] - 2.0 * (double)div[i].x);
   }
 }
 
-// V(r) = Re(vri)*vscale + v_xc(rho) (when vr is given);  E_xc = vol/N * sum eps(rho) rho.
+// For the density s rho (s = *qscale, 1 when null): V(r) = Re(vri)*vscale +
+// v_xc + V_ext(r) (when vr is given), E_xc = vol/N sum eps s rho and, with
+// vext_r, E_ext = vol/N sum V_ext(r) s rho (FP64 table, real-space form).
 template <typename R>
 __global__ void __launch_bounds__(256) k_potential(const R* __restrict__ rho,
                                                    const C_t<R>* __restrict__ vri, double vscale,
                                                    R* __restrict__ vr, double* __restrict__ slot_x,
-                                                   long long ngrid, int xc, double pref) {
+                                                   long long ngrid, int xc, double pref,
+                                                   const double* __restrict__ qscale,
+                                                   const double* __restrict__ vext_r,
+                                                   double* __restrict__ slot_e) {
   __shared__ double red[32];
-  double ex = 0.0;
+  const double s = qscale ? *qscale : 1.0;
+  double ex = 0.0, ee = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
        i += (long long)gridDim.x * blockDim.x) {
-    const R rr = rho[i];
-    const double r = rr;
+    // the energy sums take s rho in FP64 (s - 1 is ~1e-8, below FP32
+    // resolution); eps and v_xc are evaluated at its FP32 rounding
+    const double r = s * (double)rho[i];
+    const R rr = (R)r;
     double eps, v;
     lda_eps_v_t<R>(rr, xc, &eps, &v);
     ex += eps * r;
-    if (vr) vr[i] = (R)((double)vri[i].x * vscale + v);
+    double ve = 0.0;
+    if (vext_r) {
+      ve = vext_r[i];
+      ee += ve * r;
+    }
+    if (vr) vr[i] = (R)((double)vri[i].x * vscale + v + ve);
   }
   ex = block_sum(ex, red);
   if (threadIdx.x == 0) slot_x[blockIdx.x] = ex * pref;
+  if (slot_e) {
+    ee = block_sum(ee, red);
+    if (threadIdx.x == 0) slot_e[blockIdx.x] = ee * pref;
+  }
 }
 
 // xc energy density (kohn_sham = 0) or v_xc (kohn_sham = 1) on the grid
@@ -424,7 +519,8 @@ __device__ __forceinline__ int fftfreq_int(int i, int n) { return (i < (n + 1) /
 
 template <typename R>
 __global__ void k_geometry_tables(double* __restrict__ gvec, double* __restrict__ ginv,
-                                  C_t<R>* __restrict__ vext, const double* __restrict__ recip,
+                                  C_t<R>* __restrict__ vext, double2* __restrict__ vext64,
+                                  const double* __restrict__ recip,
                                   const double* __restrict__ pos, const double* __restrict__ chg,
                                   int natom, int nx, int ny, int nz, double vol) {
   const long long n = (long long)nx * ny * nz;
@@ -453,6 +549,7 @@ __global__ void k_geometry_tables(double* __restrict__ gvec, double* __restrict_
       sx *= f; sy *= f;
     }
     vext[i] = cmk<C_t<R>>(sx, sy);
+    if (vext64) vext64[i] = make_double2(sx, sy);
   }
 }
 
@@ -583,13 +680,45 @@ __global__ void k_adam(R* __restrict__ p, const R* __restrict__ g, R* __restrict
   }
 }
 
-// twiddle table W_n^t = exp(-2 pi i t/n), t < n, evaluated in FP64
+// Direct FP64 inverse DFT along one axis of an [n0][n1][n2] grid (plan setup
+// only, no shared-memory size limit): out[.., k, ..] = sum_j in[.., j, ..]
+// exp(+2 pi i j k / n), tw[t] = exp(-2 pi i t / n) of that axis.
+__global__ void k_dft_axis_inv_f64(const double2* __restrict__ in, double2* __restrict__ out, int n0,
+                                   int n1, int n2, int axis, const double2* __restrict__ tw) {
+  const long long total = (long long)n0 * n1 * n2;
+  const int n = axis == 0 ? n0 : (axis == 1 ? n1 : n2);
+  const long long stride = axis == 0 ? (long long)n1 * n2 : (axis == 1 ? n2 : 1);
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)((idx / stride) % n);
+    const long long base = idx - (long long)k * stride;
+    double ax = 0.0, ay = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const double2 w = tw[(int)(((long long)j * k) % n)];
+      const double2 v = in[base + (long long)j * stride];
+      ax += v.x * w.x + v.y * w.y;    // v * conj(w)
+      ay += v.y * w.x - v.x * w.y;
+    }
+    out[idx] = make_double2(ax, ay);
+  }
+}
+
+int launch_dft_axis_inv_f64(const double2* in, double2* out, int n0, int n1, int n2, int axis,
+                            const double2* tw, cudaStream_t st) {
+  k_dft_axis_inv_f64<<<1024, 256, 0, st>>>(in, out, n0, n1, n2, axis, tw);
+  JRG_LAUNCH_CHECK("k_dft_axis_inv_f64");
+  return JRG_OK;
+}
+
+// twiddle table W_n^t = exp(-2 pi i t/n), t < n, evaluated in FP64 (FP32
+// tables: balanced_twiddle)
 template <typename R>
 __global__ void k_twiddles(int n, C_t<R>* __restrict__ out) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     double s, c;
     sincospi(-2.0 * (double)t / (double)n, &s, &c);
-    out[t] = cmk<C_t<R>>(c, s);
+    if constexpr (sizeof(R) == 4) out[t] = balanced_twiddle(c, s);
+    else out[t] = cmk<C_t<R>>(c, s);
   }
 }
 
@@ -605,30 +734,30 @@ static inline unsigned grid_for(long long n, int per = 256, int cap = 4096) {
 
 template <typename R>
 int launch_reduce_density(const void* part, void* rho, int groups_per_spin, int ns, long long ngrid,
-                          cudaStream_t st) {
-  k_reduce_density<R><<<grid_for(ns * ngrid), 256, 0, st>>>(
-      reinterpret_cast<const R*>(part), reinterpret_cast<R*>(rho), groups_per_spin, ns, ngrid);
+                          const double* gscale, double* qpart, cudaStream_t st) {
+  k_reduce_density<R><<<kQParts, 256, 0, st>>>(reinterpret_cast<const R*>(part), reinterpret_cast<R*>(rho),
+                                               groups_per_spin, ns, ngrid, gscale, qpart);
   JRG_LAUNCH_CHECK("k_reduce_density");
   return JRG_OK;
 }
 
 template <typename R>
-int launch_recip_terms(const void* rhog, const double* ginv, const void* vext, void* vg,
-                       double* slot_h, double* slot_e, int nblocks, long long ngrid, double pref,
-                       cudaStream_t st) {
-  k_recip_terms<R><<<nblocks, 256, 0, st>>>(
-      reinterpret_cast<const C_t<R>*>(rhog), ginv, reinterpret_cast<const C_t<R>*>(vext),
-      reinterpret_cast<C_t<R>*>(vg), slot_h, slot_e, ngrid, pref);
+int launch_recip_terms(const void* rhog, const double* ginv, void* vg, double* slot_h, int nblocks,
+                       long long ngrid, double pref, const ChargeFix& cf, cudaStream_t st) {
+  k_recip_terms<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(rhog), ginv,
+                                            reinterpret_cast<C_t<R>*>(vg), slot_h, ngrid, pref, cf);
   JRG_LAUNCH_CHECK("k_recip_terms");
   return JRG_OK;
 }
 
 template <typename R>
 int launch_potential(const void* rho, const void* vri, double vscale, void* vr, double* slot_x,
-                     int nblocks, long long ngrid, int xc, double pref, cudaStream_t st) {
+                     int nblocks, long long ngrid, int xc, double pref, const double* qscale,
+                     const double* vext_r, double* slot_e, cudaStream_t st) {
   k_potential<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const R*>(rho),
                                           reinterpret_cast<const C_t<R>*>(vri), vscale,
-                                          reinterpret_cast<R*>(vr), slot_x, ngrid, xc, pref);
+                                          reinterpret_cast<R*>(vr), slot_x, ngrid, xc, pref, qscale,
+                                          vext_r, slot_e);
   JRG_LAUNCH_CHECK("k_potential");
   return JRG_OK;
 }
@@ -678,10 +807,12 @@ int launch_mul_ig(const void* in, const double* gvec, void* out, int a, long lon
 
 template <typename R>
 int launch_gga_local(const void* rho, void* g0, void* g1, void* g2, void* vloc, double* slot_x,
-                     int nblocks, long long n, int xc, double pref, int eps_only, cudaStream_t st) {
+                     int nblocks, long long n, int xc, double pref, int eps_only, const double* qscale,
+                     const double* vext_r, double* slot_e, cudaStream_t st) {
   k_gga_local<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const R*>(rho), reinterpret_cast<C_t<R>*>(g0),
                                           reinterpret_cast<C_t<R>*>(g1), reinterpret_cast<C_t<R>*>(g2),
-                                          reinterpret_cast<R*>(vloc), slot_x, n, xc, pref, eps_only);
+                                          reinterpret_cast<R*>(vloc), slot_x, n, xc, pref, eps_only,
+                                          qscale, vext_r, slot_e);
   JRG_LAUNCH_CHECK("k_gga_local");
   return JRG_OK;
 }
@@ -697,10 +828,10 @@ int launch_div_g(void* g0, const void* g1, const void* g2, const double* gvec, l
 
 template <typename R>
 int launch_potential_gga(const void* vri, double vscale, void* vr, const void* div, long long n,
-                         cudaStream_t st) {
+                         const double* vext_r, cudaStream_t st) {
   k_potential_gga<R><<<grid_for(n), 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(vri), vscale,
                                                   reinterpret_cast<R*>(vr),
-                                                  reinterpret_cast<const C_t<R>*>(div), n);
+                                                  reinterpret_cast<const C_t<R>*>(div), n, vext_r);
   JRG_LAUNCH_CHECK("k_potential_gga");
   return JRG_OK;
 }
@@ -732,11 +863,11 @@ int launch_sum_slots(const double* slots, const int* slot_begin, double* energie
 }
 
 template <typename R>
-int launch_geometry_tables(double* gvec, double* ginv, void* vext, const double* recip,
+int launch_geometry_tables(double* gvec, double* ginv, void* vext, double2* vext64, const double* recip,
                            const double* pos, const double* chg, int natom, int nx, int ny, int nz,
                            double vol, cudaStream_t st) {
   k_geometry_tables<R><<<grid_for((long long)nx * ny * nz), 256, 0, st>>>(
-      gvec, ginv, reinterpret_cast<C_t<R>*>(vext), recip, pos, chg, natom, nx, ny, nz, vol);
+      gvec, ginv, reinterpret_cast<C_t<R>*>(vext), vext64, recip, pos, chg, natom, nx, ny, nz, vol);
   JRG_LAUNCH_CHECK("k_geometry_tables");
   return JRG_OK;
 }
@@ -777,27 +908,30 @@ int launch_twiddles(int n, int prec, void* out, cudaStream_t st) {
 }
 
 #define JRG_INST_GRID(R)                                                                        \
-  template int launch_reduce_density<R>(const void*, void*, int, int, long long, cudaStream_t);   \
-  template int launch_recip_terms<R>(const void*, const double*, const void*, void*, double*,     \
-                                     double*, int, long long, double, cudaStream_t);            \
+  template int launch_reduce_density<R>(const void*, void*, int, int, long long, const double*, \
+                                        double*, cudaStream_t);                                  \
+  template int launch_recip_terms<R>(const void*, const double*, void*, double*, int, long long,  \
+                                     double, const ChargeFix&, cudaStream_t);                    \
   template int launch_potential<R>(const void*, const void*, double, void*, double*, int,         \
-                                   long long, int, double, cudaStream_t);                       \
+                                   long long, int, double, const double*, const double*, double*, \
+                                   cudaStream_t);                                               \
   template int launch_xc_field<R>(const void*, void*, long long, int, int, cudaStream_t);         \
   template int launch_real_part<R>(const void*, void*, long long, double, cudaStream_t);          \
   template int launch_hartree_g<R>(const void*, const double*, void*, long long, double,          \
                                    cudaStream_t);                                               \
   template int launch_kinetic<R>(const void*, const double*, const double*, double*, double*, int, \
                                  int, int, int, cudaStream_t);                                  \
-  template int launch_geometry_tables<R>(double*, double*, void*, const double*, const double*,   \
+  template int launch_geometry_tables<R>(double*, double*, void*, double2*, const double*, const double*, \
                                          const double*, int, int, int, int, double, cudaStream_t); \
   template int launch_mul_ig<R>(const void*, const double*, void*, int, long long, double,        \
                                 cudaStream_t);                                                  \
   template int launch_gga_local<R>(const void*, void*, void*, void*, void*, double*, int,          \
-                                   long long, int, double, int, cudaStream_t);                  \
+                                   long long, int, double, int, const double*, const double*,   \
+                                   double*, cudaStream_t);                                      \
   template int launch_div_g<R>(void*, const void*, const void*, const double*, long long, double, \
                                cudaStream_t);                                                   \
   template int launch_potential_gga<R>(const void*, double, void*, const void*, long long,        \
-                                       cudaStream_t);                                           \
+                                       const double*, cudaStream_t);                            \
   template int launch_adam<R>(void*, const void*, void*, void*, const float*, long long, double,  \
                               double, double, double, double, double, cudaStream_t);
 JRG_INST_GRID(float)

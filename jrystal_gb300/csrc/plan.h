@@ -29,6 +29,23 @@ void count_launch();
 
 bool factor_axis(int n, FftAxis* ax);
 
+// Charge renormalisation of the energy path's density.  The exact density of
+// orthonormal coefficients integrates to sum_{s,k,b} occ (Parseval); the FP32
+// density misses that by ~1e-8 (rounding of the coefficients and of the
+// transforms), which the all-electron external energy (hundreds of Ha) turns
+// into ~1e-6 Ha per atom.  k_reduce_density leaves FP64 partial sums of rho
+// in qpart, k_recip_terms forms s = sum occ / (vol/N sum rho) (1 without
+// qpart) and stores it in *scale, and the Hartree, external and xc terms use
+// s rho.
+constexpr int kQParts = 1024;   // CTAs of k_reduce_density, one charge partial each
+struct ChargeFix {
+  const double* qpart = nullptr;  // [kQParts]
+  const double* occ = nullptr;    // [nocc]
+  int nocc = 0;
+  double dv = 0.0;                // vol / N
+  double* scale = nullptr;        // s
+};
+
 // Device tables of one plan.
 struct PlanTables {
   int* gidx = nullptr;        // [ng] flattened grid index
@@ -42,6 +59,8 @@ struct PlanTables {
   double* tk = nullptr;       // [nk][ng] |G+k|^2 / 2
   void* tw = nullptr;         // twiddles: x table, y table, z table (C_t<R>)
   void* vext = nullptr;       // [ngrid] complex V_ext(G) in precision R
+  double2* vext64 = nullptr;  // [ngrid] the same table in FP64 (= vext at FP64)
+  double* vext_r = nullptr;   // [ngrid] real-space V_ext(r) = Re IFFT(V_ext(G)), FP64
   double* ginv = nullptr;     // [ngrid] 4 pi / |G|^2, 0 at G = 0
   double* gvec = nullptr;     // [ngrid][3] cartesian G vectors
   void* proj = nullptr;       // [nk][nproj][ng] complex beta-projector table (precision R)
@@ -77,7 +96,7 @@ struct AdamArgs {
 
 // Workspace offsets (bytes) of one plan.
 struct Workspace {
-  size_t wc, c, gram_part, gram, rmat, rinv, t, u, rho_part, rho, rhog, fft_scratch, vr,
+  size_t wc, c, gram_part, gram, rmat, rinv, t, u, rho_part, rho_scale, rho_q, rho, rhog, fft_scratch, vr,
       gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, kin_part, nl_part, nl_fw,
       total;
   int gram_splits;
