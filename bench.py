@@ -83,8 +83,42 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+class _Nvml:
+  """The few NVML reads the clock record needs (libnvidia-ml from the
+  driver, through ctypes): SM clock, its maximum and the active clock event
+  reasons.  Reads only; nothing is set."""
+  HW_SLOWDOWN, SW_THERMAL, HW_THERMAL, SW_POWER_CAP = 0x8, 0x20, 0x40, 0x4
+
+  def __init__(self, index):
+    import ctypes as ct
+    self.ct = ct
+    self.lib = ct.CDLL("libnvidia-ml.so.1")
+    if self.lib.nvmlInit_v2() != 0:
+      raise RuntimeError("nvmlInit failed")
+    self.h = ct.c_void_p()
+    if self.lib.nvmlDeviceGetHandleByIndex_v2(ct.c_uint(index), ct.byref(self.h)) != 0:
+      raise RuntimeError("nvmlDeviceGetHandleByIndex failed")
+    try:
+      self._reasons = self.lib.nvmlDeviceGetCurrentClocksEventReasons
+    except AttributeError:   # the name of older drivers
+      self._reasons = self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+    mx = ct.c_uint()
+    self.max_mhz = float(mx.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ct.byref(mx)) == 0 \
+        else None
+
+  def sample(self):
+    ct = self.ct
+    mhz, reasons = ct.c_uint(), ct.c_ulonglong()
+    if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(mhz)) != 0:   # NVML_CLOCK_SM
+      return None
+    self._reasons(self.h, ct.byref(reasons))
+    return float(mhz.value), int(reasons.value)
+
+
 class ClockSampler:
-  """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+  """SM clocks and throttle reasons sampled every 2 ms by a host thread
+  through NVML while the region runs (a region of a few tens of ms still
+  gets samples); nvidia-smi every 200 ms where NVML cannot be loaded."""
   Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
        "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
        "clocks_event_reasons.sw_power_cap")
@@ -92,9 +126,20 @@ class ClockSampler:
   def __init__(self, index):
     self.index = index
     self.proc = None
+    self.nvml = None
     self.lines = []
+    self.samples = []
+    self.stop = threading.Event()
 
   def __enter__(self):
+    try:
+      self.nvml = _Nvml(self.index)
+    except Exception:
+      self.nvml = None
+    if self.nvml is not None:
+      self.t = threading.Thread(target=self._poll, daemon=True)
+      self.t.start()
+      return self
     try:
       self.proc = subprocess.Popen(
         ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
@@ -111,11 +156,21 @@ class ClockSampler:
       self.proc = None
     return self
 
+  def _poll(self):
+    while not self.stop.is_set():
+      s = self.nvml.sample()
+      if s is not None:
+        self.samples.append(s)
+      time.sleep(0.002)
+
   def _read(self):
     for ln in self.proc.stdout:
       self.lines.append(ln.strip())
 
   def __exit__(self, *a):
+    self.stop.set()
+    if self.nvml is not None:
+      self.t.join(timeout=5)
     if self.proc:
       self.proc.terminate()
       try:
@@ -126,22 +181,34 @@ class ClockSampler:
   def summary(self):
     sm, mx, reasons = [], [], set()
     names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-    for ln in self.lines:
-      parts = [p.strip() for p in ln.split(",")]
-      if len(parts) < 7:
-        continue
-      try:
-        sm.append(float(parts[0]))
-        mx.append(float(parts[1]))
-      except ValueError:
-        continue
-      for n, v in zip(names, parts[3:7]):
-        if v.lower() in ("active", "1", "yes"):
-          reasons.add(n)
+    if self.nvml is not None:
+      bits = [_Nvml.HW_SLOWDOWN, _Nvml.HW_THERMAL, _Nvml.SW_THERMAL, _Nvml.SW_POWER_CAP]
+      for mhz, r in self.samples:
+        sm.append(mhz)
+        for n, b in zip(names, bits):
+          if r & b:
+            reasons.add(n)
+      if self.nvml.max_mhz:
+        mx.append(self.nvml.max_mhz)
+      source = "nvml, 2 ms"
+    else:
+      for ln in self.lines:
+        parts = [p.strip() for p in ln.split(",")]
+        if len(parts) < 7:
+          continue
+        try:
+          sm.append(float(parts[0]))
+          mx.append(float(parts[1]))
+        except ValueError:
+          continue
+        for n, v in zip(names, parts[3:7]):
+          if v.lower() in ("active", "1", "yes"):
+            reasons.add(n)
+      source = "nvidia-smi, 200 ms"
     if not sm:
       return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-            "samples": len(sm)}
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx) if mx else None,
+            "reasons": sorted(reasons), "samples": len(sm), "source": source}
 
 
 def cpu_sample(wl, nk_sample, workers, min_seconds=10.0, max_repeats=50):
@@ -196,25 +263,26 @@ def run_reference(args, wl):
          "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
          "steps_sampled": len(per_eval),
          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-         "data": "synthetic", "config": _config(wl, args.gpus),
+         "data": "synthetic", "config": _config(wl, args.gpus, precision=64),
          "cpu_baseline": {"value": val, "unit": UNIT, "cores": workers, "kind": "port",
                           "sample": sample},
          "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
   print(json.dumps(out))
 
 
-def _config(wl, n):
+def _config(wl, n, precision=None):
   return {"workload": wl.name, "cell": "all-electron Si", "grid": list(wl.grid_sizes),
           "num_g": int(wl.mask.sum()), "kpts": wl.num_kpt, "bands": wl.num_band,
-          "occupied": wl.num_occ, "xc": wl.xc, "precision": f"fp{wl.precision}",
+          "occupied": wl.num_occ, "xc": wl.xc,
+          "precision": f"fp{precision or wl.precision}",
           "parallelism": f"replicas{n}" if n > 1 else "single-gpu",
           "l2": "no explicit flush: each step streams >0.7 GB of plane buffers, >5x the 129 MB L2"}
 
 
 # DRAM bytes (read + write) per band of one k_line_apply_v<float, 64> launch,
-# from the ncu --set full capture of the 64^3 Si8 cell at 2x2x2 k-points (135 MB
-# for the 96 bands of one pipeline half, profiles/hot_kernels_si8_cubic_64_k8.md);
-# a full launch is scaled by its band count
+# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# 64^3 Si8 cell at 2x2x2 k-points (135 MB for the 96 bands of one pipeline
+# half); a full launch is scaled by its band count
 LINE_APPLY_V_DRAM_PER_BAND = (98.57996e6 + 36.56985e6) / 96
 
 
@@ -275,6 +343,41 @@ def time_to_tolerance(nsteps=20000, ncells=16, cell_index=1):
   return out
 
 
+def parity_at(plan, wl, params, occ, dev, pseudo=None):
+  """Error of the timed (FP32) path against the FP64 path of the same
+  kernels at the given parameters: energy per atom (each term and the total)
+  and the gradient's 2-norm relative error and max-abs error over the max."""
+  import torch
+  from jrystal_gb300.engine import PlaneWavePlan
+  if plan.precision == 64:
+    return None
+  p64 = PlaneWavePlan(wl.cell, wl.positions, wl.charges, wl.grid_sizes, wl.mask, wl.kpts,
+                      wl.num_band, 1, 64, wl.xc, device=dev)
+  if pseudo is not None:
+    p64.set_pseudopotential(*pseudo)
+  out = []
+  for pl in (plan, p64):
+    p = params.to(pl.rdtype)
+    e, gr, gi = pl.energy_and_grad(p[0].contiguous(), p[1].contiguous(), occ)
+    torch.cuda.synchronize()
+    out.append((e.cpu().numpy().copy(), torch.stack([gr, gi]).double()))
+  (e32, g32), (e64, g64) = out
+  natom = len(wl.charges)
+  names = ["kinetic", "external", "hartree", "xc", "total"]
+  err = {n: float(abs(e32[i] - e64[i]) / natom) for i, n in enumerate(names)}
+  d = g32 - g64
+  res = {"against": "FP64 path of the same kernels at the parameters after the timed steps",
+         "energy_err_ha_per_atom": err, "max_energy_err_ha_per_atom": max(err.values()),
+         "grad_rel_err_2norm": float(torch.linalg.norm(d) / torch.linalg.norm(g64)),
+         "grad_max_abs_err_over_max": float(d.abs().max() / g64.abs().max()),
+         "tolerance": {"energy_ha_per_atom": 1e-6, "grad_rel": 1e-5},
+         "energies_fp64": e64[:5].tolist()}
+  res["within_tolerance"] = bool(res["max_energy_err_ha_per_atom"] <= 1e-6 and
+                                 res["grad_rel_err_2norm"] <= 1e-5)
+  del p64
+  return res
+
+
 def run_ours(args, wl):
   import torch
   import torch.distributed as dist
@@ -289,8 +392,8 @@ def run_ours(args, wl):
   lib = _lib.load()
   plan = PlaneWavePlan(wl.cell, wl.positions, wl.charges, wl.grid_sizes, wl.mask, wl.kpts,
                        wl.num_band, 1, wl.precision, wl.xc, device=dev)
+  from jrystal_gb300.workloads import model_pseudopotential
   if args.pseudo:
-    from jrystal_gb300.workloads import model_pseudopotential
     plan.set_pseudopotential(*model_pseudopotential(wl))
   wr, wi = wl.init_params()
   rdt = plan.rdtype
@@ -441,6 +544,8 @@ def run_ours(args, wl):
                              "achieved_gbs": pb[k] / (phases[k] * 1e-3) / 1e9,
                              "frac": pb[k] / (phases[k] * 1e-3) / 1e9 / peak}
                          for k in ("nl_project", "nl_apply") if phases.get(k, 0) > 0}
+    out["parity"] = parity_at(plan, wl, params, occ, dev,
+                              model_pseudopotential(wl) if args.pseudo else None)
     if not args.no_time_to_tol:
       out["time_to_1e-5_Ha_per_atom"] = time_to_tolerance()
     if not args.no_cpu_baseline and not args.pseudo:
