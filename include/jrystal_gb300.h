@@ -3,8 +3,10 @@
  * energy-and-gradient library.
  *
  * Every entry point takes caller-owned device pointers, plain sizes and a
- * cudaStream_t; none allocates device memory.  Scratch memory is a caller
- * workspace of jrg_workspace_size() bytes (256-byte aligned).  Functions
+ * cudaStream_t.  Plan set-up (jrg_plan_create, jrg_plan_set_pseudopotential)
+ * allocates the plan's device tables; no other entry point allocates device
+ * memory.  Scratch memory is a caller workspace of jrg_workspace_size() bytes
+ * (256-byte aligned).  Functions
  * return a jrg_status; on failure jrg_last_error() gives a thread-local
  * message.  Numerical faults (Cholesky breakdown, non-finite values) are
  * reported through the status word of the call, never by trapping.
@@ -218,7 +220,9 @@ int jrg_fft3d(int precision, const int grid[3], int batch, int direction, const 
  * must fit, else JRG_ERR_INVALID.  All calls share that array, so calls that
  * overlap on the GPU race; nothing in it needs to start at zero.  The first
  * call on a device looks up the array's address (cudaGetSymbolAddress) and
- * should come before any stream capture. */
+ * should come before any stream capture; the address is kept with the
+ * device's context and looked up again after that context is replaced
+ * (cudaDeviceReset).  in and out may alias. */
 int jrg_fft3d_noalloc(int precision, const int grid[3], int batch, int direction,
                       const void* in, void* out, cudaStream_t stream);
 

@@ -23,8 +23,12 @@
 // same device) race on it.  Serialise them on one stream.
 //
 // Set-up: the first call on each device looks up the array's device address
-// with cudaGetSymbolAddress while that device is current and caches it.  Make
-// that first call before any stream capture begins.
+// with cudaGetSymbolAddress while that device is current and caches it with
+// the identity of the device's current context; a call that finds another
+// context (the old one was destroyed, e.g. by cudaDeviceReset, and a new one
+// created) looks the address up again.  Make the first call on a device
+// before any stream capture begins.  in and out may alias.
+#include <cuda.h>   // CUcontext / CUresult types of the two driver entry points below
 #include <mutex>
 #include "plan.h"
 
@@ -42,9 +46,37 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+static unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};   // context id of each cached address
 
-// Device address of the scratch array on the current device (looked up once
-// per device).
+// Unique id of the calling thread's current context (cuCtxGetId: ids are not
+// reused within a process, unlike context handles), 0 when there is none or
+// the driver does not provide the entry points.
+static unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrent)(CUcontext*);
+  typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS || !c) return 0;
+  unsigned long long id = 0;
+  return get_id(c, &id) == CUDA_SUCCESS ? id : 0;
+}
+
+// Device address of the scratch array on the current device: looked up once
+// per device and context, and again when the device's context changed.
 static int noalloc_scratch(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -52,11 +84,13 @@ static int noalloc_scratch(void** out) {
   if (dev < 0 || dev >= kNoAllocMaxDevices)
     return fail(JRG_ERR_UNSUPPORTED, "jrg_fft3d_noalloc: device index beyond 63");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_noalloc_ptr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
     g_noalloc_ptr[dev] = p;
+    g_noalloc_ctx[dev] = current_context_id();   // the lookup made the context current if it was not
   }
   *out = g_noalloc_ptr[dev];
   return JRG_OK;

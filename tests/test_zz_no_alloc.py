@@ -64,6 +64,26 @@ def test_noalloc_matches_workspace_fft(prec, grid, batch):
     assert np.abs(a - npref).max() <= TOL[prec] * np.abs(npref).max(), f"call {call}"
 
 
+@pytest.mark.parametrize("prec", [32, 64])
+def test_noalloc_in_place(prec):
+  """out = in: the result equals the workspace transform of the same input."""
+  import torch
+  from jrystal_gb300 import _lib
+  lib = _lib.load()
+  rng = np.random.default_rng(12)
+  grid, batch = (24, 24, 24), 2
+  cdt = torch.complex128 if prec == 64 else torch.complex64
+  for direction in (-1, +1):
+    xn = rng.normal(size=(batch,) + grid) + 1j * rng.normal(size=(batch,) + grid)
+    x = torch.tensor(xn, dtype=cdt, device="cuda")
+    ref = _call_workspace(lib, prec, grid, batch, direction, x, torch)
+    rc = _call_noalloc(lib, prec, grid, batch, direction, x, x, torch)
+    assert rc == 0, lib.jrg_last_error().decode()
+    torch.cuda.synchronize()
+    a, b = x.cpu().numpy(), ref.cpu().numpy()
+    assert np.abs(a - b).max() <= TOL[prec] * np.abs(b).max()
+
+
 def test_noalloc_rejects_oversize_request():
   import torch
   from jrystal_gb300 import _lib
