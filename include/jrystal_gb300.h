@@ -130,8 +130,16 @@ int jrg_density(const jrg_plan* plan, const void* coeff, const double* occupatio
 
 /* Loss and gradient of the direct-minimisation path.
  * energies (device double[8]): kinetic, external, hartree, xc, total,
- *   then max |C^H C - I| over k, the status word, and the nonlocal
- *   pseudopotential part of the external energy (0 without projectors).
+ *   then the Gram condition estimate max over (s,k) and k of S_kk / d_k (the
+ *   Cholesky pivots d_k of S = W^H W: 1 for orthogonal columns, growing as
+ *   the columns approach linear dependence, +inf at a breakdown), the status
+ *   word (bit 0: a Cholesky pivot at or below the Gram's rounding level,
+ *   1e-7 S_kk in FP32 and 1e-14 S_kk in FP64, or not finite, i.e. a
+ *   rank-deficient or non-finite W; bit 1: a tensor-core Gram wait ran out),
+ *   and the nonlocal pseudopotential part of the external energy (0 without
+ *   projectors).  A non-zero status word is the JRG_ERR_NUMERIC condition of
+ *   the call: it is left on the device (reading it would synchronise) for
+ *   the caller to act on, e.g. with jrg_reorthonormalise.
  * grad_re/grad_im: [S][K][G][B] d total / d w_re, d w_im (may be NULL for
  * energy only). */
 int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
@@ -175,7 +183,9 @@ int jrg_band_trace_grad(const jrg_plan* plan, const void* w_re, const void* w_im
  * update element ([2][S][K][G][B] FP32); with mlp_w32/mlp_wb given it is
  * first overwritten with the learned preconditioner's scales
  * (jrg_precond_scale at step fraction t_frac, cap smax) computed inside the
- * step from this step's band kinetic energies.  num_spin 1, num_band <= 32. */
+ * step from this step's band kinetic energies.  num_spin 1, num_band <= 32.
+ * With a non-zero status word (energies[6]) no update is applied: params, m
+ * and v keep their values. */
 typedef struct {
   int step;                 /* 1-based Adam step */
   double lr, b1, b2, eps;
@@ -188,6 +198,19 @@ typedef struct {
 int jrg_energy_grad_adam(const jrg_plan* plan, void* params, void* m, void* v,
                          const double* occupation, const jrg_adam_step* opt, double* energies,
                          void* grad, void* workspace, cudaStream_t stream);
+
+/* Re-orthonormalisation of raw parameters in place, the recovery for a
+ * non-zero status word or a large condition estimate of jrg_energy_grad
+ * (Cholesky QR, unlike the Householder QR of unitary_module.py:74-80 in the
+ * reference, breaks down on rank-deficient or non-finite W): per (s,k), W
+ * becomes Q diag(n) with Q an orthonormal basis of W's columns (Gram-Schmidt
+ * with a second projection pass, FP64) and n the original column norms.
+ * For a full-rank W the coefficients of the next jrg_energy_grad, and so the
+ * energy, are unchanged; a non-finite or dependent column is replaced by a
+ * fixed pseudo-random direction orthogonal to the previous ones.  Uses the
+ * plan workspace as scratch. */
+int jrg_reorthonormalise(const jrg_plan* plan, void* w_re, void* w_im, void* workspace,
+                         cudaStream_t stream);
 
 /* Effective potential from a density [S][nx][ny][nz] (S must be 1):
  * out [3][nx][ny][nz] real = Hartree, external, xc parts (split form) with

@@ -58,6 +58,7 @@ _SIGS = {
   "jrg_energy_grad_adam": ([_vp, _vp, _vp, _vp, _vp, ct.POINTER(AdamStep), _vp, _vp, _vp, _vp],
                            ct.c_int),
   "jrg_potential": ([_vp, _vp, ct.c_int, _vp, _vp, _vp], ct.c_int),
+  "jrg_reorthonormalise": ([_vp, _vp, _vp, _vp, _vp], ct.c_int),
   "jrg_fft3d_workspace_size": ([ct.c_int, ct.POINTER(ct.c_int), ct.c_int,
                                 ct.POINTER(ct.c_size_t)], ct.c_int),
   "jrg_fft3d": ([ct.c_int, ct.POINTER(ct.c_int), ct.c_int, ct.c_int, _vp, _vp, _vp,
@@ -133,9 +134,15 @@ def load(build_if_missing: bool = True):
     return lib
 
 
+class NumericalError(FloatingPointError):
+  """JRG_ERR_NUMERIC: a Cholesky breakdown or non-finite values (the status
+  word of an energy call, or a status the library returned)."""
+  code = JRG_ERR_NUMERIC
+
+
 def check(status: int, what: str = ""):
   if status != JRG_OK:
     msg = load().jrg_last_error().decode(errors="replace")
-    kind = {JRG_ERR_INVALID: ValueError, JRG_ERR_UNSUPPORTED: NotImplementedError}.get(
-      status, RuntimeError)
+    kind = {JRG_ERR_INVALID: ValueError, JRG_ERR_UNSUPPORTED: NotImplementedError,
+            JRG_ERR_NUMERIC: NumericalError}.get(status, RuntimeError)
     raise kind(f"{what} failed (status {status}): {msg}")

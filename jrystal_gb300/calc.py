@@ -105,10 +105,36 @@ class Minimizer:
     supported = plan.num_spin == 1 and plan.num_band <= 32
     self.fused = fused and supported
     self.keep_grad = keep_grad
+    self.recoveries = 0
 
   def energy_and_grad(self):
     e, _, _ = self.plan.energy_and_grad(self.params[0], self.params[1], self.occ, self.grads[0],
                                         self.grads[1])
+    return e
+
+  def recover(self):
+    """Re-orthonormalise the parameters (same subspace, same column norms)
+    and restart Adam from them: the response to a Cholesky breakdown or a
+    large Gram condition estimate (the step applies no update when it reports
+    a breakdown, so the parameters are those before it)."""
+    self.plan.reorthonormalise(self.params[0], self.params[1])
+    self.m.zero_()
+    self.v.zero_()
+    self.t = 0
+    self.recoveries += 1
+
+  def checked_step(self) -> torch.Tensor:
+    """step(), then the host check of its status (the energies are read back
+    every step, as the reference does): on a breakdown, non-finite energies
+    or a condition estimate above the plan's limit the parameters are
+    re-orthonormalised and the step is taken again; a second failure raises
+    NumericalError."""
+    e = self.step()
+    if not self.plan.needs_reorthonormalisation(e):
+      return e
+    self.recover()
+    e = self.step()
+    self.plan.check_numerics(e, "step after re-orthonormalisation")
     return e
 
   def step(self) -> torch.Tensor:
@@ -123,6 +149,8 @@ class Minimizer:
                                         self.b1, self.b2, self.eps,
                                         grad=self.grads if self.keep_grad else None, **kw)
     e = self.energy_and_grad()
+    if self.plan.status_of(e)["flags"] & 1:
+      return e   # a Cholesky breakdown: no update from this gradient (as the fused step)
     self.t += 1
     scale = self.scale_fn(self) if self.scale_fn is not None else None
     self.last_scale = scale
@@ -306,7 +334,7 @@ def _ground_state(cfg, pseudo: bool) -> GroundStateEnergyOutput:
   i = 0
   for i in range(cfg["epoch"]):
     t0 = time.perf_counter()
-    e = mini.step()
+    e = mini.checked_step()
     etot = float(e[4].item())          # the reference blocks on the energy every step
     train_time += time.perf_counter() - t0
     history.append(etot)

@@ -20,7 +20,7 @@ template <typename R> int launch_fft3d_dense(const FftAxis*, const C_t<R>*, int,
 template <typename R> int launch_pack_params(const void*, const void*, void*, int, int, int, bool, cudaStream_t);
 template <typename R> int launch_unpack(const void*, void*, void*, void*, int, int, int, double, cudaStream_t);
 template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t, int* = nullptr);
-int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t);
+int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t, double);
 int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t,
                          const double* = nullptr, double* = nullptr);
 template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t);
@@ -50,8 +50,9 @@ template <typename R> int launch_potential_gga(const void*, double, void*, const
 constexpr int kXcGga = JRG_XC_GGA_X_PBE | JRG_XC_GGA_C_PBE;
 template <typename R> int launch_geometry_tables(double*, double*, void*, double2*, const double*, const double*, const double*, int, int, int, int, double, cudaStream_t);
 int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
-template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t);
+template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t, const int* = nullptr);
 int launch_twiddles(int n, int prec, void* out, cudaStream_t st);
+template <typename R> int launch_reorthonormalise(void*, void*, double2*, int, int, int, cudaStream_t);
 int launch_dft_axis_inv_f64(const double2*, double2*, int, int, int, int, const double2*, cudaStream_t);
 template <typename R> int launch_rotate_adam(const void*, const double2*, const void*, const double2*, const AdamArgs&, int, int, int, double, cudaStream_t);
 int launch_lda(int prec, long long n, int xc, int ks, const void* rho, void* out, cudaStream_t st);
@@ -515,6 +516,10 @@ namespace jrg {
 
 static inline char* wsp(void* ws, size_t off) { return reinterpret_cast<char*>(ws) + off; }
 
+// Cholesky pivots at or below this fraction of the Gram diagonal are a
+// breakdown: the rounding level of the Gram (FP32 products: ~1e-8 relative)
+static double min_pivot(const jrg_plan* P) { return P->prec == 64 ? 1e-14 : 1e-7; }
+
 // phase timing: events of call `calls` (the call in progress)
 struct PhaseScope {
   const jrg_plan* P;
@@ -556,7 +561,7 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
     PHASE(PH_CHOL);
     if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram), (double2*)wsp(ws, w.rmat),
                                   (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags),
-                                  (double*)wsp(ws, w.dinv), st)))
+                                  (double*)wsp(ws, w.dinv), st, min_pivot(P))))
       return rc;
   }
   PHASE(PH_ROTATE);
@@ -898,7 +903,7 @@ static int phase_forward_range(const jrg_plan* P, const void* w_re, const void* 
     return rc;
   if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram) + k0 * nb2, (double2*)wsp(ws, w.rmat) + k0 * nb2,
                                 (double2*)wsp(ws, w.rinv) + k0 * nb2, n, P->nb, flags,
-                                (double*)wsp(ws, w.dinv) + (size_t)k0 * P->nb, st)))
+                                (double*)wsp(ws, w.dinv) + (size_t)k0 * P->nb, st, min_pivot(P))))
     return rc;
   const int kb = launch_rotate_kinetic<R>(wr, wi, (double2*)wsp(ws, w.rinv) + k0 * nb2,
                                           (C*)wsp(ws, w.c) + co, n, P->ng, P->nb, P->d.tk, P->nk,
@@ -958,7 +963,7 @@ static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re,
     if ((rc = launch_adam<R>(reinterpret_cast<R*>(adam->p[part]) + po, part ? gi : gr,
                              reinterpret_cast<R*>(adam->m[part]) + po,
                              reinterpret_cast<R*>(adam->v[part]) + po, sc, (long long)cnt, adam->lr,
-                             adam->b1, adam->b2, adam->c1, adam->c2, adam->eps, st)))
+                             adam->b1, adam->b2, adam->c1, adam->c2, adam->eps, st, adam->guard)))
       return rc;
   }
   return JRG_OK;
@@ -1153,6 +1158,7 @@ int jrg_energy_grad_adam(const jrg_plan* P, void* params, void* m, void* v, cons
   a.c2 = 1.0 - std::pow(opt->b2, opt->step);
   a.mlp_w32 = opt->mlp_w32; a.mlp_wb = opt->mlp_wb;
   a.t_frac = opt->t_frac; a.smax = opt->smax;
+  a.guard = (const int*)((const char*)ws + P->ws.flags);
   int rc;
   if (pipeline_ok(P) && g_pipeline)   // per-half gradient + Adam in the two-stream pipeline
     rc = P->prec == 64 ? energy_grad_pipelined<double>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a)
@@ -1162,6 +1168,18 @@ int jrg_energy_grad_adam(const jrg_plan* P, void* params, void* m, void* v, cons
                        : energy_grad_impl<float>(P, a.p[0], a.p[1], occ, energies, nullptr, nullptr, ws, st, &a);
   profile_call_done(P);
   return rc;
+}
+
+int jrg_reorthonormalise(const jrg_plan* P, void* w_re, void* w_im, void* ws, cudaStream_t st) {
+  if (!P || !w_re || !w_im || !ws) return fail(JRG_ERR_INVALID, "jrg_reorthonormalise: null argument");
+  const int nsk = P->ns * P->nk;
+  // FP64 scratch for the column being projected: the plane buffer
+  const size_t need = (size_t)nsk * P->ng * sizeof(double2);
+  const size_t have = (size_t)nsk * P->nb * P->nact * P->ny * P->nz * (P->prec == 64 ? 16 : 8);
+  if (need > have) return fail(JRG_ERR_UNSUPPORTED, "jrg_reorthonormalise: workspace too small for the scratch");
+  double2* scratch = (double2*)wsp(ws, P->ws.t);
+  return P->prec == 64 ? launch_reorthonormalise<double>(w_re, w_im, scratch, nsk, P->ng, P->nb, st)
+                       : launch_reorthonormalise<float>(w_re, w_im, scratch, nsk, P->ng, P->nb, st);
 }
 
 int jrg_potential(const jrg_plan* P, const void* rho, int ks, void* out, void* ws, cudaStream_t st) {

@@ -310,6 +310,24 @@ __device__ __forceinline__ double rsqrt_fp64(double d) {
   return r;
 }
 
+// Condition estimate of a Gram matrix from its Cholesky pivots: max over k of
+// S_kk / d_k (d_k the pivot before the square root; 1 for orthogonal
+// columns, ~cond(S) as the columns approach linear dependence; +inf for a
+// non-positive or non-finite pivot).  The largest over all (s,k) blocks of a
+// call is kept in flags[2..3] as the bit pattern of a non-negative double,
+// which orders like the value, so an integer atomicMax of the zeroed word
+// gives the maximum.
+__device__ __forceinline__ void note_condition(int* flags, double est) {
+  if (!(est >= 0.0)) est = __longlong_as_double(0x7ff0000000000000LL);   // NaN -> +inf
+  atomicMax(reinterpret_cast<unsigned long long*>(flags + 2), (unsigned long long)__double_as_longlong(est));
+}
+// A pivot d_k <= min_pivot * S_kk is a breakdown (flags bit 0): below the
+// rounding of the Gram (relative ~1e-8 with FP32 products, ~1e-16 in FP64)
+// it is noise, and R^-1 would amplify that noise into the coefficients.
+__device__ __forceinline__ double pivot_ratio(double s_kk, double d) {
+  return (d > 0.0 && isfinite(d)) ? fabs(s_kk) / d : __longlong_as_double(0x7ff0000000000000LL);
+}
+
 // nb <= 32: one CTA of nb*nb threads per (s,k), thread (i, j) owns element
 // (i, j).  Right-looking Cholesky and a right-looking inverse, so each pivot
 // step is two or three dependent FP64 operations per thread (FP64 latency is
@@ -317,10 +335,12 @@ __device__ __forceinline__ double rsqrt_fp64(double d) {
 __global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __restrict__ S,
                                                             double2* __restrict__ Rm,
                                                             double2* __restrict__ Ri, int nb,
-                                                            int* __restrict__ flags) {
+                                                            int* __restrict__ flags, double min_pivot) {
   __shared__ double2 r[32][33];
   __shared__ double2 x[32][33];
   __shared__ double dinv[32];
+  __shared__ double sdiag[32];
+  __shared__ double cond;
   const int sk = blockIdx.x;
   const int i = threadIdx.x / nb, j = threadIdx.x % nb;
   const bool live = threadIdx.x < nb * nb;
@@ -329,12 +349,15 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __res
     const double2 a = S[off + i * nb + j], b = S[off + j * nb + i];
     r[i][j] = (j >= i) ? make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y)) : make_double2(0.0, 0.0);
     x[i][j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    if (i == j) sdiag[i] = a.x;
   }
+  if (threadIdx.x == 0) cond = 0.0;
   __syncthreads();
   for (int k = 0; k < nb; ++k) {
     if (live && i == k && j == k) {
       double d = r[k][k].x;
-      if (!(d > 0.0) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
+      cond = fmax(cond, pivot_ratio(sdiag[k], d));
+      if (!(d > min_pivot * sdiag[k]) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
       const double rs = rsqrt_fp64(d);
       r[k][k] = make_double2(d * rs, 0.0);
       dinv[k] = rs;
@@ -375,6 +398,7 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __res
     Rm[off + i * nb + j] = r[i][j];
     Ri[off + i * nb + j] = x[i][j];
   }
+  if (threadIdx.x == 0) note_condition(flags, cond);
 }
 
 // nb > 32: the same element-parallel algorithm with the matrices in the
@@ -383,7 +407,8 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __res
 __global__ void __launch_bounds__(1024) k_cholesky_inv_big(const double2* __restrict__ S,
                                                            double2* __restrict__ Rm,
                                                            double2* __restrict__ Ri, double* dinv_g,
-                                                           int nb, int* __restrict__ flags) {
+                                                           int nb, int* __restrict__ flags,
+                                                           double min_pivot) {
   const int sk = blockIdx.x;
   const size_t off = (size_t)sk * nb * nb;
   double2* r = Rm + off;
@@ -397,10 +422,13 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_big(const double2* __rest
     x[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
   }
   __syncthreads();
+  double cond = 0.0;   // thread 0 only
   for (int k = 0; k < nb; ++k) {
     if (threadIdx.x == 0) {
       double d = r[(size_t)k * nb + k].x;
-      if (!(d > 0.0) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
+      const double skk = S[off + (size_t)k * nb + k].x;
+      cond = fmax(cond, pivot_ratio(skk, d));
+      if (!(d > min_pivot * skk) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
       const double rs = rsqrt_fp64(d);
       r[(size_t)k * nb + k] = make_double2(d * rs, 0.0);
       dinv[k] = rs;
@@ -443,6 +471,7 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_big(const double2* __rest
     }
     __syncthreads();
   }
+  if (threadIdx.x == 0) note_condition(flags, cond);
 }
 
 // Adjoint small matrices per (s,k), one CTA each:
@@ -785,6 +814,9 @@ k_rotate_rb(const void* __restrict__ X0a, const void* __restrict__ X0b, const do
       }
     }
     __syncthreads();
+    // a Cholesky breakdown of this call leaves parameters and moments as they
+    // were (the flag is final: every Cholesky of the call ran before)
+    if (adam.guard && *adam.guard) return;
     const R lr = (R)adam.lr, b1 = (R)adam.b1, b2 = (R)adam.b2, c1 = (R)adam.c1, c2 = (R)adam.c2,
             eps = (R)adam.eps;
     constexpr int U = 8;
@@ -941,11 +973,11 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
 }
 
 int launch_cholesky_inv(const double2* S, double2* Rm, double2* Ri, int nsk, int nb, int* flags,
-                        double* dinv_scratch, cudaStream_t st) {
+                        double* dinv_scratch, cudaStream_t st, double min_pivot) {
   if (nb <= 32) {
-    k_cholesky_inv_elem<<<nsk, ((nb * nb + 31) / 32) * 32, 0, st>>>(S, Rm, Ri, nb, flags);
+    k_cholesky_inv_elem<<<nsk, ((nb * nb + 31) / 32) * 32, 0, st>>>(S, Rm, Ri, nb, flags, min_pivot);
   } else {
-    k_cholesky_inv_big<<<nsk, 1024, 0, st>>>(S, Rm, Ri, dinv_scratch, nb, flags);
+    k_cholesky_inv_big<<<nsk, 1024, 0, st>>>(S, Rm, Ri, dinv_scratch, nb, flags, min_pivot);
   }
   JRG_LAUNCH_CHECK("k_cholesky_inv");
   return JRG_OK;
@@ -1088,7 +1120,163 @@ int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const 
   return go(k_rotate_rb<R, LAYOUT_BAND, ROT_ADAM, 32>, 32);
 }
 
+// ------------------------------------------------------------------------
+// Re-orthonormalisation of the raw parameters (the recovery path after a
+// Cholesky breakdown or a growing Gram condition estimate).  Per (s,k) block,
+// in place, W = Q diag(n): Q the orthonormal basis of W's columns by
+// classical Gram-Schmidt with a second projection pass (CGS2) in FP64, n the
+// original column norms.  Cholesky QR of the result returns Q, which for a
+// full-rank W is the Cholesky QR factor of W itself (both are the QR factor
+// with a positive diagonal R), so the energy is unchanged.  A column with a
+// non-finite entry, or whose norm after the projections is below 1e-10 of
+// its own (dependent on the previous columns), is replaced by a fixed
+// pseudo-random vector projected the same way and given the rms norm of the
+// finite columns.  One CTA per (s,k) block; v, the column being projected,
+// sits in FP64 scratch (ng complex per block).
+// ------------------------------------------------------------------------
+constexpr int kReorthThreads = 1024;
+constexpr int kReorthChunk = 8;   // projections reduced together
+
+// block sum of kReorthChunk complex values (all threads get the result)
+__device__ __forceinline__ void reorth_block_sum(double2 (&h)[kReorthChunk], double* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < kReorthChunk; ++q)
+    for (int o = 16; o > 0; o >>= 1) {
+      h[q].x += __shfl_xor_sync(0xffffffffu, h[q].x, o);
+      h[q].y += __shfl_xor_sync(0xffffffffu, h[q].y, o);
+    }
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < kReorthChunk; ++q) {
+      red[(w * kReorthChunk + q) * 2] = h[q].x;
+      red[(w * kReorthChunk + q) * 2 + 1] = h[q].y;
+    }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < kReorthChunk; ++q) {
+    double x = 0.0, y = 0.0;
+    for (int i = 0; i < nw; ++i) { x += red[(i * kReorthChunk + q) * 2]; y += red[(i * kReorthChunk + q) * 2 + 1]; }
+    h[q] = make_double2(x, y);
+  }
+  __syncthreads();
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kReorthThreads) k_reorthonormalise(R* __restrict__ wr, R* __restrict__ wi,
+                                                                     double2* __restrict__ scratch, int ng,
+                                                                     int nb) {
+  __shared__ double red[32 * kReorthChunk * 2];
+  extern __shared__ double colnorm[];   // [nb]: the column's original norm, < 0 for a replaced column
+  const size_t sk = blockIdx.x;
+  R* xr = wr + sk * (size_t)ng * nb;
+  R* xi = wi + sk * (size_t)ng * nb;
+  double2* v = scratch + sk * (size_t)ng;
+  const int t = threadIdx.x, T = blockDim.x;
+  // v -= sum_{j < b} q_j (q_j^H v), twice (the q_j are the finished columns)
+  auto project = [&](int b) {
+    for (int pass = 0; pass < 2; ++pass)
+      for (int j0 = 0; j0 < b; j0 += kReorthChunk) {
+        double2 h[kReorthChunk];
+#pragma unroll
+        for (int q = 0; q < kReorthChunk; ++q) h[q] = make_double2(0.0, 0.0);
+        for (int g = t; g < ng; g += T) {
+          const double2 x = v[g];
+#pragma unroll
+          for (int q = 0; q < kReorthChunk; ++q) {
+            if (j0 + q < b) {
+              const double a = xr[(size_t)g * nb + j0 + q], c = xi[(size_t)g * nb + j0 + q];
+              h[q].x += a * x.x + c * x.y;     // conj(q) x
+              h[q].y += a * x.y - c * x.x;
+            }
+          }
+        }
+        reorth_block_sum(h, red);
+        for (int g = t; g < ng; g += T) {
+          double2 x = v[g];
+#pragma unroll
+          for (int q = 0; q < kReorthChunk; ++q) {
+            if (j0 + q < b) {
+              const double a = xr[(size_t)g * nb + j0 + q], c = xi[(size_t)g * nb + j0 + q];
+              x.x -= a * h[q].x - c * h[q].y;
+              x.y -= a * h[q].y + c * h[q].x;
+            }
+          }
+          v[g] = x;
+        }
+        __syncthreads();
+      }
+  };
+  auto norm2 = [&]() {
+    double2 h[kReorthChunk];
+#pragma unroll
+    for (int q = 0; q < kReorthChunk; ++q) h[q] = make_double2(0.0, 0.0);
+    for (int g = t; g < ng; g += T) h[0].x += v[g].x * v[g].x + v[g].y * v[g].y;
+    reorth_block_sum(h, red);
+    return h[0].x;
+  };
+  for (int b = 0; b < nb; ++b) {
+    // the column; a non-finite entry makes its norm non-finite
+    for (int g = t; g < ng; g += T) v[g] = make_double2((double)xr[(size_t)g * nb + b], (double)xi[(size_t)g * nb + b]);
+    __syncthreads();
+    const double n0 = norm2();
+    bool good = isfinite(n0) && n0 > 0.0;   // the same value in every thread (block sum)
+    double n1 = 0.0;
+    if (good) {
+      project(b);
+      n1 = norm2();
+      good = n1 > 1e-20 * n0;
+    }
+    if (!good) {
+      // fixed pseudo-random replacement (hash of g and b), projected the same way
+      for (int g = t; g < ng; g += T) {
+        const unsigned h1 = (unsigned)g * 2654435761u ^ (unsigned)(b + 1) * 40503u;
+        const unsigned h2 = h1 * 2246822519u + 3266489917u;
+        v[g] = make_double2((double)(h1 >> 8) / 16777216.0 - 0.5, (double)(h2 >> 8) / 16777216.0 - 0.5);
+      }
+      __syncthreads();
+      project(b);
+      n1 = norm2();
+    }
+    const double s = n1 > 0.0 ? 1.0 / sqrt(n1) : 0.0;
+    for (int g = t; g < ng; g += T) {
+      xr[(size_t)g * nb + b] = (R)(v[g].x * s);
+      xi[(size_t)g * nb + b] = (R)(v[g].y * s);
+    }
+    if (t == 0) colnorm[b] = good ? sqrt(n0) : -1.0;
+    __syncthreads();
+  }
+  // the columns back to their norms (replaced ones to the rms of the others)
+  double rms = 0.0;
+  int cnt = 0;
+  for (int b = 0; b < nb; ++b)
+    if (colnorm[b] > 0.0) { rms += colnorm[b] * colnorm[b]; ++cnt; }
+  rms = cnt > 0 ? sqrt(rms / cnt) : 1.0;
+  for (size_t e = t; e < (size_t)ng * nb; e += T) {
+    const int b = (int)(e % nb);
+    const double s = colnorm[b] > 0.0 ? colnorm[b] : rms;
+    xr[e] = (R)((double)xr[e] * s);
+    xi[e] = (R)((double)xi[e] * s);
+  }
+}
+
+template <typename R>
+int launch_reorthonormalise(void* wr, void* wi, double2* scratch, int nsk, int ng, int nb, cudaStream_t st) {
+  const size_t sm = (size_t)nb * sizeof(double);
+  if (sm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_reorthonormalise<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(k_reorthonormalise)");
+  }
+  k_reorthonormalise<R><<<nsk, kReorthThreads, sm, st>>>(reinterpret_cast<R*>(wr), reinterpret_cast<R*>(wi),
+                                                        scratch, ng, nb);
+  JRG_LAUNCH_CHECK("k_reorthonormalise");
+  return JRG_OK;
+}
+
 #define JRG_INST_ORTH(R)                                                                        \
+  template int launch_reorthonormalise<R>(void*, void*, double2*, int, int, int, cudaStream_t);     \
   template int launch_rotate_kinetic<R>(const void*, const void*, const double2*, void*, int, int,  \
                                         int, const double*, int, void*, cudaStream_t, int);     \
   template int launch_rotate_adam<R>(const void*, const double2*, const void*, const double2*,    \

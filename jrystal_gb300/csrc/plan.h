@@ -92,6 +92,7 @@ struct AdamArgs {
   const float* mlp_w32;   // learned preconditioner evaluated inside the step (optional)
   const void* mlp_wb;
   float t_frac, smax;
+  const int* guard;       // status word of the call: no update when non-zero (optional)
 };
 
 // Workspace offsets (bytes) of one plan.

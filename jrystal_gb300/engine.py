@@ -263,6 +263,44 @@ class PlaneWavePlan:
     _lib.check(st, "jrg_energy_grad_adam")
     return self.energies
 
+  # -- numerical status and recovery ------------------------------------
+  # Gram condition estimates above which the parameters are re-orthonormalised
+  # (the coefficients lose orthogonality as the Gram's rounding times this)
+  CONDITION_LIMIT = {32: 1e3, 64: 1e8}
+
+  @staticmethod
+  def status_of(energies) -> dict:
+    """The numerical status of an energy call from its energies vector (host
+    or device): ``flags`` (bit 0: Cholesky breakdown, bit 1: a tensor-core
+    wait ran out), ``condition`` (the Gram condition estimate) and ``finite``
+    (every energy term finite)."""
+    e = energies.detach().cpu().numpy() if isinstance(energies, torch.Tensor) else np.asarray(energies)
+    return {"flags": int(e[6]), "condition": float(e[5]), "finite": bool(np.isfinite(e[:5]).all())}
+
+  def check_numerics(self, energies, what: str = "energy call"):
+    """Raise _lib.NumericalError (JRG_ERR_NUMERIC) when the call's status word
+    is set or an energy is not finite; returns the status otherwise."""
+    st = self.status_of(energies)
+    if st["flags"] or not st["finite"]:
+      raise _lib.NumericalError(
+        f"{what}: status word {st['flags']}, condition estimate {st['condition']:.3g}, "
+        f"finite energies {st['finite']} (JRG_ERR_NUMERIC)")
+    return st
+
+  def needs_reorthonormalisation(self, energies) -> bool:
+    st = self.status_of(energies)
+    return bool(st["flags"] & 1) or not st["finite"] or \
+        not (st["condition"] <= self.CONDITION_LIMIT[self.precision])
+
+  def reorthonormalise(self, w_re: torch.Tensor, w_im: torch.Tensor):
+    """In place: W <- an orthonormal basis of W's columns times the original
+    column norms (jrg_reorthonormalise); the energy of a full-rank W is
+    unchanged, non-finite or dependent columns are replaced."""
+    self._check_param(w_re, "w_re")
+    self._check_param(w_im, "w_im")
+    _lib.check(self.lib.jrg_reorthonormalise(self._h, _ptr(w_re), _ptr(w_im), _ptr(self.workspace),
+                                             _stream()), "jrg_reorthonormalise")
+
   def coeff(self, w_re: torch.Tensor, w_im: torch.Tensor) -> torch.Tensor:
     self._check_param(w_re, "w_re")
     self._check_param(w_im, "w_im")
