@@ -122,6 +122,16 @@ int jrg_plan_set_pseudopotential(jrg_plan* plan, const double* v_local, int num_
 int jrg_coeff(const jrg_plan* plan, const void* w_re, const void* w_im, void* coeff,
               void* workspace, cudaStream_t stream);
 
+/* Vector-Jacobian product of jrg_coeff (the transpose rule of the QR in
+ * unitary_module.py:74-80 as jax.grad applies it through pw.coeff,
+ * jrystal/_src/pw.py:94-137): given W and the cotangent grad_coeff of the
+ * coefficients ([S][K][G][B] complex, dL/dRe C + i dL/dIm C for a real loss
+ * L), writes dL/dw_re and dL/dw_im ([S][K][G][B] real).  Recomputes the
+ * orthonormalisation from W. */
+int jrg_coeff_adjoint(const jrg_plan* plan, const void* w_re, const void* w_im,
+                      const void* grad_coeff, void* grad_re, void* grad_im, void* workspace,
+                      cudaStream_t stream);
+
 /* Occupation-weighted density on the grid from sphere coefficients.
  * coeff: [S][K][G][B] complex; occupation: device double [S][K][B];
  * density: [S][nx][ny][nz] real. */

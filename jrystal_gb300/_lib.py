@@ -51,6 +51,7 @@ _SIGS = {
   "jrg_plan_set_pseudopotential": ([_vp, _vp, ct.c_int, _vp], ct.c_int),
   "jrg_coeff": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
   "jrg_density": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
+  "jrg_coeff_adjoint": ([_vp] * 8, ct.c_int),
   "jrg_energy_grad": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
   "jrg_band_trace_grad": ([_vp] * 11, ct.c_int),
   "jrg_pipeline": ([ct.c_int], ct.c_int),

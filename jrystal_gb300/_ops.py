@@ -1,5 +1,12 @@
 """Device helpers shared by the jrystal-compatible modules: tensor
-conversion, the library's 3-D FFT and elementwise LDA, and plan caches."""
+conversion, the library's 3-D FFT and elementwise LDA with their
+vector-Jacobian products (torch.autograd), and plan caches.
+
+Gradients follow torch's convention for complex tensors (the cotangent of z
+is dL/dRe z + i dL/dIm z).  The FFTs carry the transpose rules of
+jrystal/_src/spmd/fft.py:88-101 in that convention: the adjoint of the
+unnormalised forward transform is N times the normalised inverse, and the
+reverse."""
 from __future__ import annotations
 
 import ctypes as ct
@@ -67,17 +74,72 @@ def precision_of(t: torch.Tensor) -> int:
   return 64 if t.dtype in (torch.float64, torch.complex128) else 32
 
 
+class _Fft3(torch.autograd.Function):
+  """The library's batched 3-D FFT with its adjoint as the backward."""
+
+  @staticmethod
+  def forward(ctx, x, inverse):
+    ctx.inverse = bool(inverse)
+    ctx.n = float(np.prod(x.shape[-3:]))
+    return _fft3d(x.contiguous(), inverse=ctx.inverse)
+
+  @staticmethod
+  def backward(ctx, g):
+    g = g.contiguous()
+    if ctx.inverse:   # y = conj(F) x / N  ->  x_bar = F y_bar / N
+      return _fft3d(g, inverse=False) / ctx.n, None
+    return _fft3d(g, inverse=True) * ctx.n, None   # y = F x  ->  x_bar = conj(F) y_bar
+
+
+def _complex(x: torch.Tensor) -> torch.Tensor:
+  if torch.is_complex(x):
+    return x
+  return x.to(torch.complex128 if x.dtype == torch.float64 else torch.complex64)
+
+
 def fftn(x: torch.Tensor) -> torch.Tensor:
   """Unnormalised forward FFT over the last three axes (jnp.fft.fftn)."""
-  return _fft3d(x, inverse=False)
+  return _Fft3.apply(_complex(x), False)
 
 
 def ifftn(x: torch.Tensor) -> torch.Tensor:
   """Inverse FFT over the last three axes with 1/N (jnp.fft.ifftn)."""
-  return _fft3d(x, inverse=True)
+  return _Fft3.apply(_complex(x), True)
+
+
+class _LdaEps(torch.autograd.Function):
+  """LDA energy per particle eps(rho), elementwise; its derivative
+  d eps / d rho = (v_xc - eps) / rho from the library's v_xc."""
+
+  @staticmethod
+  def forward(ctx, rho, xc):
+    eps = _lda_raw(rho, xc, False)
+    ctx.save_for_backward(rho, eps)
+    ctx.xc = xc
+    return eps
+
+  @staticmethod
+  def backward(ctx, g):
+    rho, eps = ctx.saved_tensors
+    v = _lda_raw(rho, ctx.xc, True)
+    d = torch.where(rho > 1e-15, (v - eps) / torch.where(rho > 1e-15, rho, torch.ones_like(rho)),
+                    torch.zeros_like(rho))
+    return g * d, None
+
+
+def lda_eps(rho: torch.Tensor, xc: str) -> torch.Tensor:
+  """Differentiable LDA energy per particle (the non-Kohn-Sham xc_density)."""
+  return _LdaEps.apply(rho, xc)
 
 
 def lda(rho: torch.Tensor, xc: str, kohn_sham: bool) -> torch.Tensor:
+  """Elementwise LDA energy per particle (or potential) on the device, no
+  gradient (the Kohn-Sham potential is taken at a stopped density, as
+  jrystal/_src/xc.py:246-250 does)."""
+  return _lda_raw(rho.detach(), xc, kohn_sham)
+
+
+def _lda_raw(rho: torch.Tensor, xc: str, kohn_sham: bool) -> torch.Tensor:
   """Elementwise LDA energy per particle (or potential) on the device."""
   lib = _lib.load()
   rho = rho.contiguous()

@@ -1052,6 +1052,32 @@ static int coeff_entry(const jrg_plan* P, const void* w_re, const void* w_im, vo
   return orthonormalise<R>(P, w_re, w_im, ws, st, kRotGC, coeff);
 }
 
+// Vector-Jacobian product of the coefficient map: g_W = (g_C - C K) R^-H with
+// K the Hermitian completion of the upper triangle of C^H g_C (real diagonal);
+// grad_coeff is the cotangent of C as torch reports it for a real loss,
+// dL/dRe C + i dL/dIm C, and grad_re + i grad_im = g_W the same way.
+template <typename R>
+static int coeff_adjoint_entry(const jrg_plan* P, const void* w_re, const void* w_im, const void* gcoeff,
+                               void* g_re, void* g_im, void* ws, cudaStream_t st) {
+  const Workspace& w = P->ws;
+  const int nsk = P->ns * P->nk;
+  int rc;
+  JRG_CUDA(cudaMemsetAsync(wsp(ws, w.flags), 0, 64, st));
+  if ((rc = orthonormalise<R>(P, w_re, w_im, ws, st))) return rc;   // C band-major, R^-1
+  if ((rc = launch_pack_params<R>(gcoeff, nullptr, wsp(ws, w.gc), nsk, P->ng, P->nb, true, st))) return rc;
+  if ((rc = launch_gram<R>(kBand, wsp(ws, w.c), nullptr, kBand, wsp(ws, w.gc), nullptr,
+                           (double2*)wsp(ws, w.adj_part), (double2*)wsp(ws, w.adj), nsk, P->ng, P->nb,
+                           P->ws.gram_splits, st, (int*)wsp(ws, w.flags))))
+    return rc;
+  double2* rh = (double2*)wsp(ws, w.kmat);
+  double2* negm2 = rh + (size_t)nsk * P->nb * P->nb;
+  if ((rc = launch_adjoint_small((double2*)wsp(ws, w.adj), (double2*)wsp(ws, w.rinv), rh, negm2, nsk, P->nb,
+                                 st)))
+    return rc;
+  return launch_rotate<R>(kRotGSplit, kBand, wsp(ws, w.gc), nullptr, rh, wsp(ws, w.c), negm2, g_re, g_im, nsk,
+                          P->ng, P->nb, 1.0, wsp(ws, w.rot_scratch), st);
+}
+
 template <typename R>
 static int potential_entry(const jrg_plan* P, const void* rho, int ks, void* out, void* ws,
                            cudaStream_t st) {
@@ -1086,6 +1112,14 @@ int jrg_coeff(const jrg_plan* P, const void* w_re, const void* w_im, void* coeff
   if (!P || !w_re || !w_im || !coeff || !ws) return fail(JRG_ERR_INVALID, "jrg_coeff: null argument");
   return P->prec == 64 ? coeff_entry<double>(P, w_re, w_im, coeff, ws, st)
                        : coeff_entry<float>(P, w_re, w_im, coeff, ws, st);
+}
+
+int jrg_coeff_adjoint(const jrg_plan* P, const void* w_re, const void* w_im, const void* grad_coeff,
+                      void* grad_re, void* grad_im, void* ws, cudaStream_t st) {
+  if (!P || !w_re || !w_im || !grad_coeff || !grad_re || !grad_im || !ws)
+    return fail(JRG_ERR_INVALID, "jrg_coeff_adjoint: null argument");
+  return P->prec == 64 ? coeff_adjoint_entry<double>(P, w_re, w_im, grad_coeff, grad_re, grad_im, ws, st)
+                       : coeff_adjoint_entry<float>(P, w_re, w_im, grad_coeff, grad_re, grad_im, ws, st);
 }
 
 int jrg_density(const jrg_plan* P, const void* coeff, const double* occ, void* rho, void* ws,

@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __res
   __shared__ double2 x[32][33];
   __shared__ double dinv[32];
   __shared__ double sdiag[32];
-  __shared__ double cond;
+  __shared__ double dpiv[32];   // the pivots before the square root
   const int sk = blockIdx.x;
   const int i = threadIdx.x / nb, j = threadIdx.x % nb;
   const bool live = threadIdx.x < nb * nb;
@@ -351,12 +351,11 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __res
     x[i][j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
     if (i == j) sdiag[i] = a.x;
   }
-  if (threadIdx.x == 0) cond = 0.0;
   __syncthreads();
   for (int k = 0; k < nb; ++k) {
     if (live && i == k && j == k) {
       double d = r[k][k].x;
-      cond = fmax(cond, pivot_ratio(sdiag[k], d));
+      dpiv[k] = d;
       if (!(d > min_pivot * sdiag[k]) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
       const double rs = rsqrt_fp64(d);
       r[k][k] = make_double2(d * rs, 0.0);
@@ -398,7 +397,12 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_elem(const double2* __res
     Rm[off + i * nb + j] = r[i][j];
     Ri[off + i * nb + j] = x[i][j];
   }
-  if (threadIdx.x == 0) note_condition(flags, cond);
+  // condition estimate off the pivot chain: one ratio per lane of warp 0
+  if (threadIdx.x < 32) {
+    double c = threadIdx.x < nb ? pivot_ratio(sdiag[threadIdx.x], dpiv[threadIdx.x]) : 0.0;
+    for (int o = 16; o > 0; o >>= 1) c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
+    if (threadIdx.x == 0) note_condition(flags, c);
+  }
 }
 
 // nb > 32: the same element-parallel algorithm with the matrices in the

@@ -51,6 +51,10 @@ def xc_energy(density_grid, g_vector_grid, vol, xc_type, kohn_sham=False):
   if rho.dim() != 4:
     raise AssertionError("density_grid must contains spin axis")
   num = float(np.prod(rho.shape[-3:]))
+  if not kohn_sham:
+    # gradient v_xc (LDA and PBE) through the library's potential
+    from .xc import xc_energy_grad
+    return xc_energy_grad(rho, g_vector_grid, vol, xc_type)
   e = xc_density(rho, g_vector_grid, kohn_sham, xc_type)
   return torch.sum(e * rho) * vol / num
 

@@ -310,6 +310,19 @@ class PlaneWavePlan:
     _lib.check(st, "jrg_coeff")
     return out
 
+  def coeff_adjoint(self, w_re: torch.Tensor, w_im: torch.Tensor, grad_coeff: torch.Tensor):
+    """dL/dw_re, dL/dw_im from the cotangent of coeff(w_re, w_im) (torch's
+    convention for complex tensors: dL/dRe + i dL/dIm)."""
+    self._check_param(w_re, "w_re")
+    self._check_param(w_im, "w_im")
+    g = grad_coeff.to(self.cdtype).contiguous()
+    self._check_param(g, "grad_coeff", self.cdtype)
+    gr, gi = torch.empty_like(w_re), torch.empty_like(w_im)
+    st = self.lib.jrg_coeff_adjoint(self._h, _ptr(w_re), _ptr(w_im), _ptr(g), _ptr(gr), _ptr(gi),
+                                    _ptr(self.workspace), _stream())
+    _lib.check(st, "jrg_coeff_adjoint")
+    return gr, gi
+
   def density(self, coeff_sphere: torch.Tensor, occupation) -> torch.Tensor:
     self._check_param(coeff_sphere, "coeff", self.cdtype)
     occ = self._occ(occupation)

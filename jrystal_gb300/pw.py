@@ -48,16 +48,35 @@ def _params(pw_param):
   return w, torch.zeros_like(w)
 
 
+class _Coeff(torch.autograd.Function):
+  """Cholesky QR of the parameters on the device; backward: the library's
+  vector-Jacobian product of the map (jrg_coeff_adjoint)."""
+
+  @staticmethod
+  def forward(ctx, w_re, w_im, plan):
+    w_re, w_im = w_re.detach().contiguous(), w_im.detach().contiguous()
+    ctx.save_for_backward(w_re, w_im)
+    ctx.plan = plan
+    return plan.coeff(w_re, w_im)
+
+  @staticmethod
+  def backward(ctx, g):
+    w_re, w_im = ctx.saved_tensors
+    gr, gi = ctx.plan.coeff_adjoint(w_re, w_im, g)
+    return gr, gi, None
+
+
 def coeff_sphere(pw_param, freq_mask) -> torch.Tensor:
   """Orthonormal sphere coefficients (spin, kpt, num_g, band), Cholesky QR on
-  the device (equal to the QR of unitary_module.py:74-80 up to a phase per band)."""
+  the device (equal to the QR of unitary_module.py:74-80 up to a phase per
+  band), differentiable with respect to the parameters."""
   w_re, w_im = _params(pw_param)
   prec = precision_of(w_re)
   w_im = w_im.to(w_re.dtype)
   s, k, g, b = w_re.shape
   plan = plans.mask_plan(to_numpy(freq_mask),
                          k, b, s, prec)
-  return plan.coeff(w_re.contiguous(), w_im.contiguous())
+  return _Coeff.apply(w_re, w_im, plan)
 
 
 def coeff(pw_param, freq_mask, sharding=None) -> torch.Tensor:
