@@ -321,25 +321,34 @@ def phase_bytes(plan, fused=False):
 
 def time_to_tolerance(nsteps=20000, ncells=16, cell_index=1):
   """Learned vs plain optimiser on the held-out strained cells of the
-  preconditioner's evaluation sequence (seed 99): wall time until
-  |E - E_ref| < 1e-5 Ha/atom, E_ref the lower of the two final energies; the
-  median speed-up over the cells (a plain run that never reaches the
-  tolerance counts as its full length) and the detail of one cell."""
+  preconditioner's evaluation sequence (seed 99), judged against the
+  converged plain energy E_ref (the plain run's energy after nsteps): wall
+  time until E stays within 1e-5 Ha/atom of E_ref (two-sided: |E - E_ref|)
+  and until E stays below E_ref + 1e-5 Ha/atom (one-sided, the "_below"
+  keys: at least as converged as the plain run; the learned runs end below
+  E_ref, so the two-sided form charges them for going lower).  Medians over
+  the cells, with cells where the learned run never settles counted as 0,
+  and the detail of one cell."""
   from jrystal_gb300 import precond, precond_train
   mlp = precond.MLP.load(precond.DEFAULT_WEIGHTS)
   res = precond_train.evaluate(mlp, ncells=ncells, nsteps=nsteps, seed=99, grids=(24, 27, 32))
   row = res["cells"][cell_index]
-  out = {"cell": row["cell"], "tol_ha_per_atom": 1e-5, "max_steps": nsteps}
+  out = {"cell": row["cell"], "tol_ha_per_atom": 1e-5, "max_steps": nsteps,
+         "judge": "converged plain energy (the plain run's energy after max_steps)",
+         "E_ref": row["E_ref"], "plain_drift_last10pct_ha_per_atom": row["plain_drift_last10pct_ha_per_atom"]}
   for mode in ("plain", "learned"):
     r = row[mode]
-    out[mode] = {"steps": r["steps"], "ms_per_step": round(r["ms_per_step"], 4),
-                 "seconds": None if r["seconds"] is None else round(r["seconds"], 4)}
-  p, l = out["plain"]["seconds"], out["learned"]["seconds"]
-  out["speedup_wall"] = None if (p is None or l is None) else round(p / l, 3)
-  out["heldout"] = {"cells": ncells, "median_speedup_wall": res["median_speedup_wall"],
-                    "learned_reached": res["learned_reached"], "plain_reached": res["plain_reached"],
-                    "speedups": [None if r["speedup_wall"] is None else round(r["speedup_wall"], 3)
-                                 for r in res["cells"]]}
+    out[mode] = {k: (round(r[k], 4) if isinstance(r[k], float) else r[k])
+                 for k in ("steps", "steps_below", "ms_per_step", "seconds", "seconds_below",
+                           "end_minus_ref_ha_per_atom")}
+  out["speedup_wall"] = row["speedup_wall"]
+  out["speedup_wall_below"] = row["speedup_wall_below"]
+  out["heldout"] = {k: res[k] for k in res if k not in ("cells",)}
+  out["heldout"]["cells"] = ncells
+  out["heldout"]["speedups_below"] = [None if r["speedup_wall_below"] is None else round(r["speedup_wall_below"], 3)
+                                      for r in res["cells"]]
+  out["heldout"]["speedups"] = [None if r["speedup_wall"] is None else round(r["speedup_wall"], 3)
+                                for r in res["cells"]]
   return out
 
 

@@ -260,6 +260,16 @@ def collect_records(plan: PlaneWavePlan, occupation, params: torch.Tensor, steps
   return {"x": torch.cat(xs), "a": torch.cat(As), "c": torch.cat(Cs), "w": torch.cat(Ws)}
 
 
+def time_below(history: np.ndarray, e_max: float) -> Optional[int]:
+  """First step after which E < e_max for the rest of the run (None if never)."""
+  bad = np.nonzero(np.asarray(history) >= e_max)[0]
+  if len(bad) == 0:
+    return 0
+  if bad[-1] == len(history) - 1:
+    return None
+  return int(bad[-1] + 1)
+
+
 def time_to_tolerance(history: np.ndarray, e_ref: float, tol: float) -> Optional[int]:
   """First step after which |E - e_ref| stays below tol (None if never)."""
   bad = np.nonzero(np.abs(np.asarray(history) - e_ref) >= tol)[0]
