@@ -360,8 +360,11 @@ def parity_at(plan, wl, params, occ, dev, pseudo=None):
   from jrystal_gb300.engine import PlaneWavePlan
   if plan.precision == 64:
     return None
-  p64 = PlaneWavePlan(wl.cell, wl.positions, wl.charges, wl.grid_sizes, wl.mask, wl.kpts,
-                      wl.num_band, 1, 64, wl.xc, device=dev)
+  try:
+    p64 = PlaneWavePlan(wl.cell, wl.positions, wl.charges, wl.grid_sizes, wl.mask, wl.kpts,
+                        wl.num_band, 1, 64, wl.xc, device=dev)
+  except NotImplementedError as err:
+    return {"against": "FP64 path of the same kernels", "unavailable": str(err)}
   if pseudo is not None:
     p64.set_pseudopotential(*pseudo)
   out = []

@@ -97,6 +97,18 @@ int jrg_plan_destroy(jrg_plan* plan);
 /* Caller workspace needed by the entry points below (bytes). */
 int jrg_workspace_size(const jrg_plan* plan, size_t* bytes);
 
+/* Bound on the workspace (bytes; 0 removes it).  The largest buffer holds
+ * the plane transforms of every band (the reference keeps the whole wave
+ * grid instead, jrystal/_src/pw.py:140-211); under a bound it holds as many
+ * (s,k) blocks as fit, at least one, and the energy entry points run the
+ * blocks in chunks, transforming each chunk's coefficients again for the
+ * adjoint instead of keeping the planes of the density pass (about one more
+ * inverse plane pass per band, no two-stream pipeline).  Query
+ * jrg_workspace_size again afterwards; jrg_plan_memory_chunk gives the
+ * blocks per chunk (the number of (s,k) blocks when nothing is recomputed). */
+int jrg_plan_set_memory_limit(jrg_plan* plan, size_t bytes);
+int jrg_plan_memory_chunk(const jrg_plan* plan, int* kchunk);
+
 /* Norm-conserving pseudopotential of the plan's atoms (replaces the
  * all-electron Coulomb external potential; plan setup, allocates and
  * synchronises like jrg_plan_create):

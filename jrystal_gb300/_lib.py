@@ -48,6 +48,8 @@ _SIGS = {
   "jrg_plan_create": ([_vp, ct.POINTER(_vp)], ct.c_int),
   "jrg_plan_destroy": ([_vp], ct.c_int),
   "jrg_workspace_size": ([_vp, ct.POINTER(ct.c_size_t)], ct.c_int),
+  "jrg_plan_set_memory_limit": ([_vp, ct.c_size_t], ct.c_int),
+  "jrg_plan_memory_chunk": ([_vp, ct.POINTER(ct.c_int)], ct.c_int),
   "jrg_plan_set_pseudopotential": ([_vp, _vp, ct.c_int, _vp], ct.c_int),
   "jrg_coeff": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),
   "jrg_density": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),

@@ -92,7 +92,25 @@ constexpr int kEwaldBlocks = 512;
 static int csize(int prec) { return prec == 64 ? 16 : 8; }
 static int rsize(int prec) { return prec == 64 ? 8 : 4; }
 
+static void layout_workspace_k(jrg_plan* P, int kc);
+
+// Workspace layout; with a memory limit the plane buffer holds only as many
+// (s,k) blocks as fit (at least one), and the energy entry points process the
+// blocks in chunks, transforming each chunk's coefficients again for the
+// adjoint instead of keeping all planes from the density pass.
 static void layout_workspace(jrg_plan* P) {
+  const int nsk = P->ns * P->nk;
+  layout_workspace_k(P, nsk);
+  if (P->mem_limit == 0 || P->ws.total <= P->mem_limit) return;
+  const size_t per_k = (size_t)P->nb * P->nact * P->ny * P->nz * csize(P->prec);
+  const size_t fixed = P->ws.total - P->ws.t_bytes;
+  int kc = P->mem_limit > fixed ? (int)((P->mem_limit - fixed) / per_k) : 1;
+  kc = std::max(1, std::min(kc, nsk));
+  layout_workspace_k(P, kc);
+}
+
+static void layout_workspace_k(jrg_plan* P, int kc) {
+  P->kchunk = kc;
   Workspace& w = P->ws;
   const size_t C = csize(P->prec), Rz = rsize(P->prec);
   const size_t nsk = (size_t)P->ns * P->nk, nbt = nsk * P->nb;
@@ -119,7 +137,8 @@ static void layout_workspace(jrg_plan* P) {
   w.rinv = take(nsk * b2);
   w.adj = take(nsk * b2);
   w.kmat = take(2 * nsk * b2);          // R^{-H} and -K R^{-H}
-  w.t = take(nbt * P->nact * (size_t)P->ny * P->nz * C);
+  w.t_bytes = (size_t)kc * P->nb * P->nact * (size_t)P->ny * P->nz * C;
+  w.t = take(w.t_bytes);
   w.u = w.t;                            // adjoint line pass works in place
   w.rho_part = take((size_t)w.ngroups * P->ngrid * Rz);
   w.rho_scale = take((size_t)w.ngroups * sizeof(double));
@@ -460,6 +479,19 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
   return JRG_OK;
 }
 
+int jrg_plan_set_memory_limit(jrg_plan* P, size_t bytes) {
+  if (!P) return fail(JRG_ERR_INVALID, "jrg_plan_set_memory_limit: null plan");
+  P->mem_limit = bytes;
+  layout_workspace(P);
+  return upload_slot_layout(P);
+}
+
+int jrg_plan_memory_chunk(const jrg_plan* P, int* kchunk) {
+  if (!P || !kchunk) return fail(JRG_ERR_INVALID, "jrg_plan_memory_chunk: null argument");
+  *kchunk = P->kchunk;
+  return JRG_OK;
+}
+
 int jrg_workspace_size(const jrg_plan* P, size_t* bytes) {
   if (!P || !bytes) return fail(JRG_ERR_INVALID, "null argument");
   *bytes = P->ws.total;
@@ -671,18 +703,26 @@ static int sum_energy_slots(const jrg_plan* P, double* slots, double* energies, 
 template <typename R>
 static int density_from_c(const jrg_plan* P, const double* occ, void* ws, void* rho_out,
                           cudaStream_t st, double* qpart = nullptr) {
+  using C = C_t<R>;
   const Workspace& w = P->ws;
-  const int nbt = P->ns * P->nk * P->nb;
+  const int nsk = P->ns * P->nk;
   int rc;
-  {
-    PHASE(PH_PLANE_INV);
-    if ((rc = launch_plane_inv_sphere<R>(P, wsp(ws, w.c), wsp(ws, w.t), nbt, st))) return rc;
-  }
-  {
-    PHASE(PH_LINE_DENSITY);
-    if ((rc = launch_line_density<R>(P, wsp(ws, w.t), wsp(ws, w.rho_part), occ, 1.0 / P->vol, 0,
-                                     nbt, P->nb, (double*)wsp(ws, w.rho_scale), st)))
-      return rc;
+  // (s,k) blocks in chunks of P->kchunk through the plane buffer
+  for (int k0 = 0; k0 < nsk; k0 += P->kchunk) {
+    const int n = std::min(P->kchunk, nsk - k0);
+    {
+      PHASE(PH_PLANE_INV);
+      if ((rc = launch_plane_inv_sphere<R>(P, (C*)wsp(ws, w.c) + (size_t)k0 * P->nb * P->ng, wsp(ws, w.t),
+                                           n * P->nb, st)))
+        return rc;
+    }
+    {
+      PHASE(PH_LINE_DENSITY);
+      if ((rc = launch_line_density<R>(P, wsp(ws, w.t), (R*)wsp(ws, w.rho_part) + (size_t)k0 * P->ngrid, occ,
+                                       1.0 / P->vol, k0 * P->nb, n * P->nb, P->nb,
+                                       (double*)wsp(ws, w.rho_scale) + k0, st)))
+        return rc;
+    }
   }
   PHASE(PH_REDUCE_DENSITY);
   return launch_reduce_density<R>(wsp(ws, w.rho_part), rho_out, P->nk, P->ns, P->ngrid,
@@ -772,19 +812,29 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
   }
   if (!adam && !g_re && !g_im) return JRG_OK;
   if (!adam && (!g_re || !g_im)) return fail(JRG_ERR_INVALID, "grad_re and grad_im must both be given");
-  // adjoint: planes -> x lines (x V) -> planes -> sphere gradient
-  {
-    PHASE(PH_LINE_APPLY_V);
-    if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), wsp(ws, w.vr), nbt, P->nb, st)))
-      return rc;
-  }
-  {
-    // with band energies requested, g_C = H c unweighted; the occupations
-    // are folded into the small adjoint matrices below
-    PHASE(PH_PLANE_FWD);
-    if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), wsp(ws, w.c), wsp(ws, w.gc),
-                                         band_e ? P->d_ones : occ, 0, nbt, 1.0 / N, st)))
-      return rc;
+  // adjoint: planes -> x lines (x V) -> planes -> sphere gradient, per chunk
+  // of (s,k) blocks; with more than one chunk the planes of each are
+  // transformed again from the coefficients (the density pass overwrote them)
+  for (int k0 = 0; k0 < nsk; k0 += P->kchunk) {
+    const int n = std::min(P->kchunk, nsk - k0);
+    const size_t co = (size_t)k0 * P->nb * P->ng;
+    if (P->kchunk < nsk) {
+      PHASE(PH_PLANE_INV);
+      if ((rc = launch_plane_inv_sphere<R>(P, (C*)wsp(ws, w.c) + co, wsp(ws, w.t), n * P->nb, st))) return rc;
+    }
+    {
+      PHASE(PH_LINE_APPLY_V);
+      if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), wsp(ws, w.vr), n * P->nb, P->nb, st)))
+        return rc;
+    }
+    {
+      // with band energies requested, g_C = H c unweighted; the occupations
+      // are folded into the small adjoint matrices below
+      PHASE(PH_PLANE_FWD);
+      if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), (C*)wsp(ws, w.c) + co, (C*)wsp(ws, w.gc) + co,
+                                           band_e ? P->d_ones : occ, k0 * P->nb, n * P->nb, 1.0 / N, st)))
+        return rc;
+    }
   }
   if ((rc = nl_adjoint<R>(P, ws, 0, nsk, st))) return rc;
   // orthonormalisation adjoint
@@ -834,19 +884,24 @@ static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im
       return rc;
   }
   if ((rc = nl_forward<R>(P, ws, 0, nsk, wts, wts, st))) return rc;
-  {
-    PHASE(PH_PLANE_INV);
-    if ((rc = launch_plane_inv_sphere<R>(P, wsp(ws, w.c), wsp(ws, w.t), nbt, st))) return rc;
-  }
-  {
-    PHASE(PH_LINE_APPLY_V);
-    if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), v_eff, nbt, P->nb, st))) return rc;
-  }
-  {
-    PHASE(PH_PLANE_FWD);
-    if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), wsp(ws, w.c), wsp(ws, w.gc), wts, 0, nbt,
-                                         1.0 / N, st)))
-      return rc;
+  for (int k0 = 0; k0 < nsk; k0 += P->kchunk) {
+    const int n = std::min(P->kchunk, nsk - k0);
+    const size_t co = (size_t)k0 * P->nb * P->ng;
+    {
+      PHASE(PH_PLANE_INV);
+      if ((rc = launch_plane_inv_sphere<R>(P, (C_t<R>*)wsp(ws, w.c) + co, wsp(ws, w.t), n * P->nb, st)))
+        return rc;
+    }
+    {
+      PHASE(PH_LINE_APPLY_V);
+      if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), v_eff, n * P->nb, P->nb, st))) return rc;
+    }
+    {
+      PHASE(PH_PLANE_FWD);
+      if ((rc = launch_plane_fwd_sphere<R>(P, wsp(ws, w.u), (C_t<R>*)wsp(ws, w.c) + co,
+                                           (C_t<R>*)wsp(ws, w.gc) + co, wts, k0 * P->nb, n * P->nb, 1.0 / N, st)))
+        return rc;
+    }
   }
   if ((rc = nl_adjoint<R>(P, ws, 0, nsk, st))) return rc;
   {
@@ -972,7 +1027,7 @@ static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re,
 static bool g_pipeline = true;   // two-way k-point pipeline of jrg_energy_grad
 
 static bool pipeline_ok(const jrg_plan* P) {
-  return P->ns * P->nk >= 2 && P->nb <= 32 && jrg_tensor_core_paths(-1) == 0 &&
+  return P->ns * P->nk >= 2 && P->nb <= 32 && P->kchunk >= P->ns * P->nk && jrg_tensor_core_paths(-1) == 0 &&
          jrg_fast_paths(-1) == 1 && !(P->prof && P->prof->max_calls > 0);
 }
 
@@ -1209,7 +1264,7 @@ int jrg_reorthonormalise(const jrg_plan* P, void* w_re, void* w_im, void* ws, cu
   const int nsk = P->ns * P->nk;
   // FP64 scratch for the column being projected: the plane buffer
   const size_t need = (size_t)nsk * P->ng * sizeof(double2);
-  const size_t have = (size_t)nsk * P->nb * P->nact * P->ny * P->nz * (P->prec == 64 ? 16 : 8);
+  const size_t have = P->ws.t_bytes;
   if (need > have) return fail(JRG_ERR_UNSUPPORTED, "jrg_reorthonormalise: workspace too small for the scratch");
   double2* scratch = (double2*)wsp(ws, P->ws.t);
   return P->prec == 64 ? launch_reorthonormalise<double>(w_re, w_im, scratch, nsk, P->ng, P->nb, st)

@@ -426,13 +426,12 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_big(const double2* __rest
     x[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
   }
   __syncthreads();
-  double cond = 0.0;   // thread 0 only
+  bool broke = false;   // thread 0 only
   for (int k = 0; k < nb; ++k) {
     if (threadIdx.x == 0) {
       double d = r[(size_t)k * nb + k].x;
       const double skk = S[off + (size_t)k * nb + k].x;
-      cond = fmax(cond, pivot_ratio(skk, d));
-      if (!(d > min_pivot * skk) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; }
+      if (!(d > min_pivot * skk) || !isfinite(d)) { atomicOr(flags, 1); d = 1.0; broke = true; }
       const double rs = rsqrt_fp64(d);
       r[(size_t)k * nb + k] = make_double2(d * rs, 0.0);
       dinv[k] = rs;
@@ -475,7 +474,14 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_big(const double2* __rest
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) note_condition(flags, cond);
+  // condition estimate off the pivot chain: S_kk / d_k = S_kk dinv_k^2 (warp 0)
+  if (threadIdx.x < 32) {
+    double c = 0.0;
+    for (int k = threadIdx.x; k < nb; k += 32)
+      c = fmax(c, fabs(S[off + (size_t)k * nb + k].x) * dinv[k] * dinv[k]);
+    for (int o = 16; o > 0; o >>= 1) c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
+    if (threadIdx.x == 0) note_condition(flags, broke ? __longlong_as_double(0x7ff0000000000000LL) : c);
+  }
 }
 
 // Adjoint small matrices per (s,k), one CTA each:
@@ -488,7 +494,7 @@ __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict
                                                        double2* __restrict__ Rh,
                                                        double2* __restrict__ negM2, int nb,
                                                        const double* __restrict__ f,
-                                                       double* __restrict__ eps) {
+                                                       double* __restrict__ eps, bool with_m2) {
   const int sk = blockIdx.x;
   const size_t off = (size_t)sk * nb * nb;
   const double2* a = A + off;
@@ -503,6 +509,7 @@ __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict
     const double s = fw(i);
     Rh[off + e] = make_double2(s * v.x, -s * v.y);
   }
+  if (!with_m2) return;   // formed by k_adjoint_m2_tiled
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int i = e / nb, j = e % nb;
     // (K R^{-H})[i][j] = sum_l K[i][l] conj(Ri[j][l]),  Ri upper => l >= j
@@ -517,6 +524,67 @@ __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict
       sy += kil.y * r.x - kil.x * r.y;
     }
     negM2[off + e] = make_double2(-sx, -sy);
+  }
+}
+
+// -M2 = -K R^{-H} for larger band counts: a 32 x 32 output tile per CTA
+// (256 threads, four elements each), the contraction over l in 32-wide
+// tiles of K (the Hermitian completion of A's upper triangle with real
+// diagonal, columns weighted by f) and of conj(Ri)^T staged in shared
+// memory.  Ri is upper triangular (zero below the diagonal).
+__global__ void __launch_bounds__(256) k_adjoint_m2_tiled(const double2* __restrict__ A,
+                                                          const double2* __restrict__ Ri,
+                                                          double2* __restrict__ negM2, int nb,
+                                                          const double* __restrict__ f) {
+  __shared__ double2 ks[32][33];   // K[i0 + r][l0 + c]
+  __shared__ double2 rs[32][33];   // conj(Ri[j0 + c][l0 + r]) = R^{-H}[l0 + r][j0 + c]
+  const size_t off = (size_t)blockIdx.z * nb * nb;
+  const double2* a = A + off;
+  const double2* ri = Ri + off;
+  const double* fb = f ? f + (size_t)blockIdx.z * nb : nullptr;
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // ty 0..7
+  double2 acc[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) acc[q] = make_double2(0.0, 0.0);
+  const int lstart = (j0 / 32) * 32;   // R^{-H}[l][j] = 0 for l < j: tiles below j0 vanish
+  for (int l0 = lstart; l0 < nb; l0 += 32) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = ty + 8 * q;
+      // K[i][l], i = i0 + r, l = l0 + tx
+      const int i = i0 + r, l = l0 + tx;
+      double2 kv = make_double2(0.0, 0.0);
+      if (i < nb && l < nb) {
+        const double wl = fb ? fb[l] : 1.0, wi = fb ? fb[i] : 1.0;
+        if (l > i) { const double2 t = a[(size_t)i * nb + l]; kv = make_double2(wl * t.x, wl * t.y); }
+        else if (l < i) { const double2 t = a[(size_t)l * nb + i]; kv = make_double2(wi * t.x, -wi * t.y); }
+        else kv = make_double2(wi * a[(size_t)i * nb + i].x, 0.0);
+      }
+      ks[r][tx] = kv;
+      // R^{-H}[l][j] with l = l0 + r, j = j0 + tx
+      const int lr = l0 + r, j = j0 + tx;
+      double2 rv = make_double2(0.0, 0.0);
+      if (lr < nb && j < nb) { const double2 t = ri[(size_t)j * nb + lr]; rv = make_double2(t.x, -t.y); }
+      rs[r][tx] = rv;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int c = 0; c < 32; ++c) {
+      const double2 r = rs[c][tx];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double2 k = ks[ty + 8 * q][c];
+        acc[q].x = fma(k.x, r.x, fma(-k.y, r.y, acc[q].x));
+        acc[q].y = fma(k.x, r.y, fma(k.y, r.x, acc[q].y));
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = i0 + ty + 8 * q, j = j0 + tx;
+    if (i < nb && j < nb) negM2[off + (size_t)i * nb + j] = make_double2(-acc[q].x, -acc[q].y);
   }
 }
 
@@ -989,8 +1057,14 @@ int launch_cholesky_inv(const double2* S, double2* Rm, double2* Ri, int nsk, int
 
 int launch_adjoint_small(const double2* A, const double2* Ri, double2* Rh, double2* negM2, int nsk,
                          int nb, cudaStream_t st, const double* f, double* eps) {
-  k_adjoint_small<<<nsk, 256, 0, st>>>(A, Ri, Rh, negM2, nb, f, eps);
+  const bool tiled = nb > 32;
+  k_adjoint_small<<<nsk, 256, 0, st>>>(A, Ri, Rh, negM2, nb, f, eps, !tiled);
   JRG_LAUNCH_CHECK("k_adjoint_small");
+  if (tiled) {
+    const unsigned nt = (unsigned)((nb + 31) / 32);
+    k_adjoint_m2_tiled<<<dim3(nt, nt, nsk), 256, 0, st>>>(A, Ri, negM2, nb, f);
+    JRG_LAUNCH_CHECK("k_adjoint_m2_tiled");
+  }
   return JRG_OK;
 }
 

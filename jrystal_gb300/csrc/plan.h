@@ -100,6 +100,7 @@ struct Workspace {
   size_t wc, c, gram_part, gram, rmat, rinv, t, u, rho_part, rho_scale, rho_q, rho, rhog, fft_scratch, vr,
       gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, kin_part, nl_part, nl_fw,
       total;
+  size_t t_bytes; // plane buffer
   int gram_splits;
   int nl_splits;  // G splits of the projector contraction
   int ngroups;    // density partial groups
@@ -124,6 +125,8 @@ struct jrg_plan {
   std::vector<double> pos, charge, kpts;
   int xc;
   int nproj = 0;            // beta-projector rows of the pseudopotential (0: all-electron)
+  size_t mem_limit = 0;     // workspace bound set by jrg_plan_set_memory_limit (0: none)
+  int kchunk = 0;           // (s,k) blocks whose plane buffers are resident at once
   jrg::FftAxis ax[3];
   jrg::PlanTables d;
   jrg::Workspace ws;

@@ -137,6 +137,21 @@ class PlaneWavePlan:
       self.workspace_bytes = int(nbytes.value)
       self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=self.device)
 
+  def set_memory_limit(self, nbytes: int) -> int:
+    """Bound the workspace (jrg_plan_set_memory_limit; 0 removes the bound):
+    the plane transforms are recomputed per chunk of (s,k) blocks when all
+    of them do not fit.  Reallocates the workspace; returns the (s,k) blocks
+    per chunk."""
+    torch.cuda.synchronize(self.device)
+    _lib.check(self.lib.jrg_plan_set_memory_limit(self._h, int(nbytes)), "jrg_plan_set_memory_limit")
+    nb = ct.c_size_t()
+    _lib.check(self.lib.jrg_workspace_size(self._h, ct.byref(nb)), "jrg_workspace_size")
+    self.workspace_bytes = int(nb.value)
+    self.workspace = torch.empty(self.workspace_bytes, dtype=torch.uint8, device=self.device)
+    kc = ct.c_int()
+    _lib.check(self.lib.jrg_plan_memory_chunk(self._h, ct.byref(kc)), "jrg_plan_memory_chunk")
+    return int(kc.value)
+
   # -- shapes -------------------------------------------------------------
   @property
   def param_shape(self):

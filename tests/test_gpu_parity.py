@@ -44,6 +44,8 @@ CASES = [
   dict(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 2), nb=40, nocc=20),
   # 32^3 sphere: the pruned eight-values-per-thread transforms
   dict(kind="si8", grid=(32, 32, 32), kgrid=(2, 1, 1), nb=4, nocc=2),
+  # the band count of the Si64 supercell workload (160 bands, 128 occupied)
+  dict(kind="si8", grid=(32, 32, 32), kgrid=(1, 1, 1), nb=160, nocc=128),
 ]
 
 
