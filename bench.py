@@ -574,9 +574,194 @@ def run_ours(args, wl):
     dist.destroy_process_group()
 
 
+BATCH_METRIC = "cell-steps/s (batched plain-Adam trajectory generation incl. records)"
+BATCH_UNIT = "cell-steps/s"
+
+
+def batch_cells(ncells=64, seed=2, grids=(24, 27, 32, 36, 48)):
+  """The 64 strained Si / C / Al cells of the trajectory-generation workload
+  (uniform +-3 % strain per lattice vector, grids 24^3-48^3, 2x2x2 k-points,
+  8-16 bands, the lower half doubly occupied, FP32)."""
+  from jrystal_gb300 import cells
+  rng = np.random.default_rng(seed)
+  return [cells.strained_cell(rng, grids=grids) for _ in range(ncells)]
+
+
+def _batch_config(wls, n):
+  return {"workload": "batch64_trajectories", "cells": len(wls),
+          "kinds": {k: sum(w.name.startswith(k + "_") for w in wls) for k in ("si", "c", "al")},
+          "grids": sorted({w.grid_sizes[0] for w in wls}), "kpts": 8,
+          "bands": [min(w.num_band for w in wls), max(w.num_band for w in wls)],
+          "records_per_step_per_cell": 6, "precision": "fp32", "xc": "lda_x+lda_c_vwn",
+          "parallelism": f"replicas{n}" if n > 1 else "single-gpu",
+          "l2": "no explicit flush: the 64 cells' plane buffers total > 1 GB, > 8x the 129 MB L2"}
+
+
+def run_batch_reference(args, wls):
+  """The FP64 CPU restatement stepping the cells one at a time (energy,
+  gradient, Adam per cell-step), over a bounded sample of cells."""
+  ws, rank, _ = _dist()
+  if rank != 0:
+    return
+  workers = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+  cpu_sample(wls[0], wls[0].num_kpt, workers, min_seconds=0.0)
+  per, t_start, i = [], time.time(), 0
+  while i < args.steps and time.time() - t_start < 60.0:
+    wl = wls[i % len(wls)]
+    per.append(cpu_sample(wl, wl.num_kpt, workers, min_seconds=0.0)[0])
+    i += 1
+  val = len(per) / sum(per)
+  out = {"impl": "reference", "metric": BATCH_METRIC, "value": val, "unit": BATCH_UNIT,
+         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+         "ms_per_step": 1e3 / val, "steps_sampled": len(per), "higher_is_better": True,
+         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+         "config": _batch_config(wls, args.gpus),
+         "cpu_baseline": {"value": val, "unit": BATCH_UNIT, "cores": workers, "kind": "port",
+                          "sample": f"FP64 NumPy restatement, {len(per)} cell-steps of the first "
+                                    f"{min(len(per), len(wls))} cells, one cell at a time"},
+         "e2e": {"value": val, "unit": BATCH_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+  print(json.dumps(out))
+
+
+def run_batch(args, wls):
+  """Batched trajectory generation: args.warmup + args.steps plain Adam
+  steps of every cell (one CUDA graph launch per step of all cells, records
+  drawn on the device), timed over the last args.steps; beside it the same
+  cells stepped one at a time (the single-cell two-call loop, a bounded
+  sample), and the whole job end to end (parameters copied in from pinned
+  host memory, records and energies copied out)."""
+  import torch
+  import torch.distributed as dist
+  from jrystal_gb300 import _lib
+  from jrystal_gb300.batch import TrajectoryBatch, _plan
+  from jrystal_gb300.engine import adam_update
+
+  ws, rank, local = _dist()
+  if ws > 1:
+    dist.init_process_group("nccl")
+  torch.cuda.set_device(local)
+  dev = torch.device("cuda", local)
+  lib = _lib.load()
+  total = args.warmup + args.steps
+  batch = TrajectoryBatch(wls, total, per_step=6, seed=2, device=dev)
+  stream = torch.cuda.current_stream()
+
+  def barrier():
+    if ws > 1:
+      dist.barrier()
+    torch.cuda.synchronize()
+
+  batch.run(args.warmup)
+  barrier()
+  launches0 = lib.jrg_launch_count()
+  t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  with ClockSampler(local) as clk:
+    barrier()
+    t0.record(stream)
+    batch.run(args.steps)
+    t1.record(stream)
+    barrier()
+  kernels_per_step = (lib.jrg_launch_count() - launches0)
+  ms = _max_over_ranks(t0.elapsed_time(t1) / args.steps, dev)
+  last_e = batch.energies[-1].cpu().numpy()
+  nrec = int(batch.rec_a.numel())
+  # the graph's kernel launches are not counted by the library's host-side
+  # launch counter; count one eager step instead
+  probe = TrajectoryBatch(wls[:len(wls)], 1, per_step=6, seed=2, device=dev)
+  c0 = lib.jrg_launch_count()
+  probe.step(graph=False)
+  barrier()
+  launches_per_step = lib.jrg_launch_count() - c0
+  probe.close()
+
+  # the same cells one at a time (single-cell two-call loop), bounded sample
+  seq_steps, seq_cells = 20, min(16, len(wls))
+  seq_ms = 0.0
+  for wl in wls[:seq_cells]:
+    plan = _plan(wl, dev)
+    wr, wi = wl.init_params()
+    p = torch.tensor(np.stack([wr, wi]), dtype=plan.rdtype, device=dev)
+    g, m, v = torch.zeros_like(p), torch.zeros_like(p), torch.zeros_like(p)
+    occ = torch.as_tensor(np.asarray(wl.occupation), dtype=torch.float64, device=dev)
+    for t in range(3):
+      plan.energy_and_grad(p[0], p[1], occ, g[0], g[1])
+      adam_update(p, g, m, v, t + 1, 1e-2)
+    barrier()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for t in range(seq_steps):
+      plan.energy_and_grad(p[0], p[1], occ, g[0], g[1])
+      adam_update(p, g, m, v, t + 4, 1e-2)
+    a1.record(stream)
+    barrier()
+    seq_ms += a0.elapsed_time(a1)
+    plan.close()
+  seq_val = seq_cells * seq_steps / (seq_ms * 1e-3)
+
+  # end to end: parameters from pinned host memory, all steps, records and
+  # energies back to pinned host memory
+  host_p = [torch.tensor(np.stack(wl.init_params())).pin_memory() for wl in wls]
+  e2e = TrajectoryBatch(wls, args.steps, per_step=6, seed=3, device=dev)
+  host_rec = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in e2e.records().items()}
+  host_hist = torch.empty(e2e.energies.shape, dtype=torch.float64).pin_memory()
+  barrier()
+  b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  b0.record(stream)
+  for dst, src in zip(e2e.params, host_p):
+    dst.copy_(src, non_blocking=True)
+  e2e.run()
+  for k, v in e2e.records().items():
+    host_rec[k].copy_(v, non_blocking=True)
+  host_hist.copy_(e2e.energies, non_blocking=True)
+  b1.record(stream)
+  barrier()
+  e2e_ms = _max_over_ranks(b0.elapsed_time(b1) / args.steps, dev)
+  h2d = sum(p.numel() * p.element_size() for p in e2e.params)
+  d2h = sum(v.numel() * v.element_size() for v in e2e.records().values()) + host_hist.numel() * 8
+  e2e.close()
+
+  if rank == 0:
+    peak, peak_kind = _peaks()
+    step_bytes = sum(sum(phase_bytes(p).values()) - phase_bytes(p)["pack_params"] for p in batch.plans)
+    adam_bytes = sum(7 * p.numel() * p.element_size() for p in batch.params)
+    achieved = (step_bytes + adam_bytes) / (ms * 1e-3) / 1e9
+    ncell = len(wls)
+    out = {"metric": BATCH_METRIC, "value": ncell * 1000.0 / ms * ws, "unit": BATCH_UNIT, "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic", "config": _batch_config(wls, ws), "clocks": clk.summary(),
+           "e2e": {"value": ncell * 1000.0 / e2e_ms * ws, "unit": BATCH_UNIT,
+                   "h2d_bytes_per_step": int(h2d / args.steps), "d2h_bytes_per_step": int(d2h / args.steps)},
+           "gpu_launches": int(launches_per_step * args.steps),
+           "graph_launches": args.steps,
+           "roofline": {"bound": "hbm", "kernel": "whole batched step (every kernel of the 64 cells)",
+                        "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "peak_source": peak_kind, "traffic": None,
+                        "algorithmic_bytes": int(step_bytes + adam_bytes)},
+           "sequential": {"value": seq_val, "unit": BATCH_UNIT,
+                          "sample": f"{seq_cells} cells x {seq_steps} steps, one cell at a time "
+                                    "(jrg_energy_grad + jrg_adam_update per step)",
+                          "batched_over_sequential": ncell * 1000.0 / ms / seq_val},
+           "records": {"rows": nrec, "records_per_s": nrec / ((args.warmup + args.steps) * ms * 1e-3)},
+           "energies_last_step_cell0": last_e[0, :5].tolist()}
+    if kernels_per_step:
+      out["host_counted_launches_in_timed_region"] = int(kernels_per_step)
+    print(json.dumps(out))
+  batch.close()
+  if ws > 1:
+    dist.destroy_process_group()
+
+
 def main():
   args = _args()
   from jrystal_gb300 import workloads
+  if args.workload == "batch64_trajectories":
+    wls = batch_cells()
+    if args.impl == "reference":
+      run_batch_reference(args, wls)
+    else:
+      run_batch(args, wls)
+    return
   wl = workloads.WORKLOADS[args.workload]()
   if args.kgrid:
     wl.kgrid = tuple(args.kgrid)

@@ -347,6 +347,55 @@ int jrg_profile_read(jrg_plan* plan, double* ms, int* calls, int num_phases);
 const char* jrg_profile_phase_name(int phase);
 int jrg_profile_num_phases(void);
 
+/* Batched trajectory generation (no counterpart as one call: jrystal runs one
+ * cell per driver loop, calc/calc_ground_state_energy_all_electrons.py:205-220,
+ * each step being value_and_grad + optax.adam, :175-190).  A batch runs plain
+ * Adam (jrg_energy_grad, then the jrg_adam_update rule) on many independent
+ * cells at once -- any grids, k-sets and band counts, one plan each -- every
+ * cell on its own stream branch forked from and joined back to the caller's
+ * stream; with use_graph the fan-out of one step is captured into a CUDA
+ * graph on the first such call and replayed after that, one graph launch per
+ * step of every cell.  Each cell's trajectory equals the same steps taken one
+ * cell at a time (energy and gradient, then Adam with no update on a non-zero
+ * status word).  The step count lives on the device; a batch takes exactly
+ * `steps` jrg_batch_step calls.  Records (per_step > 0): at every step t <
+ * steps - 1, per_step occupied coefficients are drawn per cell (counter-based
+ * hash of seed, cell, t, draw) and row t holds x = (|G+k|^2/2 / E_kin(band),
+ * band/B, t/steps), a = g_t . u_t, c = max((g_{t+1} - g_t) . u_t, c_floor |a|)
+ * (u_t the applied update of those elements, real and imaginary parts) and
+ * w = (number of non-zero a) / sum |a| over the row -- the one-step secant
+ * records of the learned preconditioner's training set.  Creation allocates
+ * the batch's device state and streams and synchronises; steps only enqueue
+ * (the first graph step also captures and instantiates).  The plans,
+ * workspaces and buffers belong to the batch until it is destroyed. */
+typedef struct jrg_batch jrg_batch;
+typedef struct {
+  int num_cells;
+  jrg_plan* const* plans;            /* host array [num_cells]; num_spin 1 */
+  void* const* workspaces;           /* device pointers, jrg_workspace_size bytes each */
+  void* const* params;               /* [2][S][K][G][B] each, updated in place */
+  void* const* m;                    /* Adam moments, zero before the first step */
+  void* const* v;
+  void* const* grads;                /* [2][S][K][G][B]: the last step's gradient */
+  const double* const* occupations;  /* device [S*K*B] each */
+  int steps;                         /* horizon */
+  double lr, b1, b2, eps;
+  double* energies;                  /* optional device [steps][num_cells][8] (as jrg_energy_grad) */
+  int per_step;                      /* records per step and cell (0: none) */
+  unsigned long long seed;
+  double c_floor;
+  float* rec_x;                      /* device [num_cells][steps-1][per_step][3] */
+  float* rec_a;                      /* device [num_cells][steps-1][per_step] */
+  float* rec_c;
+  float* rec_w;
+  int64_t* rec_idx;                  /* optional: flat element index of each draw in [S][K][G][B] */
+} jrg_batch_desc;
+
+int jrg_batch_create(const jrg_batch_desc* desc, jrg_batch** out);
+int jrg_batch_step(jrg_batch* batch, int use_graph, cudaStream_t stream);
+int jrg_batch_steps_done(const jrg_batch* batch, int* steps);
+int jrg_batch_destroy(jrg_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,34 @@ class AdamStep(ct.Structure):
   ]
 
 
+class BatchDesc(ct.Structure):
+  """jrg_batch_desc."""
+  _fields_ = [
+    ("num_cells", ct.c_int),
+    ("plans", ct.POINTER(ct.c_void_p)),
+    ("workspaces", ct.POINTER(ct.c_void_p)),
+    ("params", ct.POINTER(ct.c_void_p)),
+    ("m", ct.POINTER(ct.c_void_p)),
+    ("v", ct.POINTER(ct.c_void_p)),
+    ("grads", ct.POINTER(ct.c_void_p)),
+    ("occupations", ct.POINTER(ct.c_void_p)),
+    ("steps", ct.c_int),
+    ("lr", ct.c_double),
+    ("b1", ct.c_double),
+    ("b2", ct.c_double),
+    ("eps", ct.c_double),
+    ("energies", ct.c_void_p),
+    ("per_step", ct.c_int),
+    ("seed", ct.c_ulonglong),
+    ("c_floor", ct.c_double),
+    ("rec_x", ct.c_void_p),
+    ("rec_a", ct.c_void_p),
+    ("rec_c", ct.c_void_p),
+    ("rec_w", ct.c_void_p),
+    ("rec_idx", ct.c_void_p),
+  ]
+
+
 _SIGS = {
   "jrg_version": ([], ct.c_int),
   "jrg_last_error": ([], ct.c_char_p),
@@ -49,6 +77,10 @@ _SIGS = {
   "jrg_plan_destroy": ([_vp], ct.c_int),
   "jrg_workspace_size": ([_vp, ct.POINTER(ct.c_size_t)], ct.c_int),
   "jrg_plan_set_memory_limit": ([_vp, ct.c_size_t], ct.c_int),
+  "jrg_batch_create": ([ct.POINTER(BatchDesc), ct.POINTER(_vp)], ct.c_int),
+  "jrg_batch_step": ([_vp, ct.c_int, _vp], ct.c_int),
+  "jrg_batch_steps_done": ([_vp, ct.POINTER(ct.c_int)], ct.c_int),
+  "jrg_batch_destroy": ([_vp], ct.c_int),
   "jrg_plan_memory_chunk": ([_vp, ct.POINTER(ct.c_int)], ct.c_int),
   "jrg_plan_set_pseudopotential": ([_vp, _vp, ct.c_int, _vp], ct.c_int),
   "jrg_coeff": ([_vp, _vp, _vp, _vp, _vp, _vp], ct.c_int),

@@ -50,7 +50,7 @@ template <typename R> int launch_potential_gga(const void*, double, void*, const
 constexpr int kXcGga = JRG_XC_GGA_X_PBE | JRG_XC_GGA_C_PBE;
 template <typename R> int launch_geometry_tables(double*, double*, void*, double2*, const double*, const double*, const double*, int, int, int, int, double, cudaStream_t);
 int launch_ewald(const double*, const double*, const double*, const double*, int, int, long long, double, double, double*, int, double*, cudaStream_t);
-template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t, const int* = nullptr);
+template <typename R> int launch_adam(void*, const void*, void*, void*, const float*, long long, double, double, double, double, double, double, cudaStream_t, const int* = nullptr, const double* = nullptr);
 int launch_twiddles(int n, int prec, void* out, cudaStream_t st);
 template <typename R> int launch_reorthonormalise(void*, void*, double2*, int, int, int, cudaStream_t);
 int launch_dft_axis_inv_f64(const double2*, double2*, int, int, int, int, const double2*, cudaStream_t);

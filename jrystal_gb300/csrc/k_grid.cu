@@ -637,10 +637,14 @@ __global__ void k_ewald_finish(const double* __restrict__ slots, int nslots, con
 template <typename R>
 __global__ void k_adam(R* __restrict__ p, const R* __restrict__ g, R* __restrict__ m,
                        R* __restrict__ v, const float* __restrict__ scale, long long n, R lr, R b1,
-                       R b2, R c1, R c2, R eps, const int* __restrict__ guard) {
+                       R b2, R c1, R c2, R eps, const int* __restrict__ guard,
+                       const double* __restrict__ coefs) {
   // guard: the status word of the energy call that made g; non-zero (a
   // Cholesky breakdown) leaves the parameters and moments unchanged
   if (guard && *guard) return;
+  // coefs: bias corrections (c1, c2) read from device memory instead of the
+  // arguments (a step replayed from a CUDA graph, the step count on device)
+  if (coefs) { c1 = (R)coefs[0]; c2 = (R)coefs[1]; }
   const long long stride = (long long)gridDim.x * blockDim.x;
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if constexpr (sizeof(R) == 4) {
@@ -893,10 +897,10 @@ int launch_ewald(const double* cell, const double* gvec, const double* pos, cons
 template <typename R>
 int launch_adam(void* p, const void* g, void* m, void* v, const float* scale, long long n, double lr,
                 double b1, double b2, double c1, double c2, double eps, cudaStream_t st,
-                const int* guard) {
+                const int* guard, const double* coefs) {
   k_adam<R><<<grid_for((n + 3) / 4, 256, 152 * 16), 256, 0, st>>>(
       reinterpret_cast<R*>(p), reinterpret_cast<const R*>(g), reinterpret_cast<R*>(m),
-      reinterpret_cast<R*>(v), scale, n, (R)lr, (R)b1, (R)b2, (R)c1, (R)c2, (R)eps, guard);
+      reinterpret_cast<R*>(v), scale, n, (R)lr, (R)b1, (R)b2, (R)c1, (R)c2, (R)eps, guard, coefs);
   JRG_LAUNCH_CHECK("k_adam");
   return JRG_OK;
 }
@@ -939,7 +943,8 @@ int launch_twiddles(int n, int prec, void* out, cudaStream_t st) {
   template int launch_potential_gga<R>(const void*, double, void*, const void*, long long,        \
                                        const double*, cudaStream_t);                            \
   template int launch_adam<R>(void*, const void*, void*, void*, const float*, long long, double,  \
-                              double, double, double, double, double, cudaStream_t, const int*);
+                              double, double, double, double, double, cudaStream_t, const int*,  \
+                              const double*);
 JRG_INST_GRID(float)
 JRG_INST_GRID(double)
 

@@ -46,8 +46,21 @@ def _params(wl, plan):
 
 
 def generate(ncells=64, steps=300, per_step=6, seed=2, grids=(24, 27, 32, 36, 48), mlp=None,
-             smax=4.0, lr=1e-2):
+             smax=4.0, lr=1e-2, batched=True):
+  """Training records from ``steps``-step trajectories of ``ncells`` strained
+  cells: plain trajectories run as one batch (batch.TrajectoryBatch: one
+  graph launch per step of every cell, records drawn on the device);
+  trajectories under the network (``mlp``), or with ``batched=False``, one
+  cell at a time (precond.collect_records)."""
   rng = np.random.default_rng(seed)
+  if mlp is None and batched:
+    from .batch import TrajectoryBatch
+    wls = [cells.strained_cell(rng, grids=grids) for _ in range(ncells)]
+    b = TrajectoryBatch(wls, steps, lr=lr, per_step=per_step, seed=seed)
+    b.run()
+    out = {k: v.clone() for k, v in b.records().items()}
+    b.close()
+    return out
   recs = []
   for i in range(ncells):
     wl = cells.strained_cell(rng, grids=grids)

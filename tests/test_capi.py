@@ -81,3 +81,25 @@ def test_pseudopotential_types():
     calc.create_pseudopotential({"pseudopotential_type": "paw", "pseudopotential_file_dir": "."}, cr)
   with pytest.raises(ValueError):
     calc.create_pseudopotential({"pseudopotential_type": "nc", "pseudopotential_file_dir": None}, cr)
+
+
+def test_batch_create_rejects_bad_descriptions_without_gpu():
+  """jrg_batch_create checks its description before touching the device."""
+  lib = _lib.load()
+  h = ct.c_void_p()
+  assert lib.jrg_batch_create(None, ct.byref(h)) == _lib.JRG_ERR_INVALID
+  d = _lib.BatchDesc()
+  d.num_cells = 0
+  assert lib.jrg_batch_create(ct.byref(d), ct.byref(h)) == _lib.JRG_ERR_INVALID
+  assert b"num_cells" in lib.jrg_last_error()
+  one = (ct.c_void_p * 1)(ct.c_void_p(8))
+  p = ct.cast(one, ct.POINTER(ct.c_void_p))
+  d.num_cells = 1
+  d.plans = d.workspaces = d.params = d.m = d.v = d.grads = d.occupations = p
+  d.steps, d.lr, d.b1, d.b2, d.eps = 0, 1e-2, 0.9, 0.99, 1e-8
+  assert lib.jrg_batch_create(ct.byref(d), ct.byref(h)) == _lib.JRG_ERR_INVALID
+  d.steps, d.per_step = 10, 4      # records without record buffers
+  assert lib.jrg_batch_create(ct.byref(d), ct.byref(h)) == _lib.JRG_ERR_INVALID
+  assert b"record" in lib.jrg_last_error()
+  assert lib.jrg_batch_step(None, 1, None) == _lib.JRG_ERR_INVALID
+  assert lib.jrg_batch_destroy(None) == _lib.JRG_OK
