@@ -318,12 +318,15 @@ int jrg_kinetic_table(const jrg_plan* plan, double* out, cudaStream_t stream);
  * previous setting.  Process-wide; no reference counterpart. */
 int jrg_fast_paths(int enable);
 
-/* Selects the contraction kernels of the FP32 path (num_band <= 32):
- * 0 = CUDA cores (the default: fastest at these band counts), 1 = mma.sync
- * TF32 Gram and rotation with a three-product hi/lo split, 2 = tcgen05
- * (5th-generation tensor cores, tensor-memory accumulators) TF32 x 3 Gram
- * with CUDA-core rotation; enable < 0 only queries.  Returns the previous
- * setting.  Process-wide; no reference counterpart. */
+/* Selects the contraction kernels (Gram and rotations):
+ * 0 = CUDA cores (the default: the only mode whose FP32 energies stay within
+ * 1e-6 Ha/atom of the FP64 path at the 24-band Si8 cell; thread-per-G
+ * rotations), 1 = mma.sync TF32 Gram and rotation with a three-product hi/lo
+ * split (FP32 path, num_band <= 32), 2 = tcgen05 (5th-generation tensor
+ * cores, tensor-memory accumulators) TF32 x 3 Gram with CUDA-core rotation
+ * (FP32 path, num_band <= 32), 3 = CUDA cores with the register-blocked
+ * shared-memory rotations of earlier versions; enable < 0 only queries.
+ * Returns the previous setting.  Process-wide; no reference counterpart. */
 int jrg_tensor_core_paths(int enable);
 
 /* Two-way k-point pipeline of jrg_energy_grad (enable = 1, the default):

@@ -23,7 +23,8 @@ template <typename R> int launch_gram(int, const void*, const void*, int, const 
 int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t, double);
 int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t,
                          const double* = nullptr, double* = nullptr);
-template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t);
+template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t, int = 0);
+constexpr int kTriUpper = 1, kTriLower = 2;   // zero pattern of a rotation's first matrix: R^-1, R^-H
 constexpr int kSplit = 0, kBand = 1;           // tall-operand layouts (k_orth.cu)
 constexpr int kRotBand = 0, kRotGC = 1, kRotGSplit = 2;
 template <typename R> int launch_reduce_density(const void*, void*, int, int, long long, const double*, double*, cudaStream_t);
@@ -606,7 +607,7 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
   }
   return launch_rotate<R>(out_kind, kSplit, w_re, w_im, (double2*)wsp(ws, w.rinv), nullptr, nullptr,
                           out ? out : wsp(ws, w.c), nullptr, nsk, P->ng, P->nb, 1.0,
-                          wsp(ws, w.rot_scratch), st);
+                          wsp(ws, w.rot_scratch), st, kTriUpper);
 }
 
 // PBE terms of the grid phase.  Step 1 (from rho(G) in rhog, before it is
@@ -858,7 +859,7 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
     return launch_rotate_adam<R>(wsp(ws, w.gc), rh, wsp(ws, w.c), negm2, *adam, nsk, P->ng, P->nb,
                                  2.0, st);
   return launch_rotate<R>(kRotGSplit, kBand, wsp(ws, w.gc), nullptr, rh, wsp(ws, w.c), negm2, g_re,
-                          g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st);
+                          g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st, kTriLower);
 }
 
 // Band trace of a fixed effective potential (band-structure objective):
@@ -928,7 +929,7 @@ static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im
   }
   PHASE(PH_ADJ_ROTATE);
   return launch_rotate<R>(kRotGSplit, kBand, wsp(ws, w.gc), nullptr, rh, wsp(ws, w.c), negm2, g_re,
-                          g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st);
+                          g_im, nsk, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st, kTriLower);
 }
 
 // Two-way k-point pipeline of the energy/gradient evaluation: the (s,k)
@@ -1010,7 +1011,7 @@ static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re,
   R* gi = adam ? (adam->grad[1] ? reinterpret_cast<R*>(adam->grad[1]) + po : reinterpret_cast<R*>(t) + cnt)
                : reinterpret_cast<R*>(g_im) + po;
   if ((rc = launch_rotate<R>(kRotGSplit, kBand, gc, nullptr, rh + k0 * nb2, c, negm2 + k0 * nb2, gr, gi,
-                             n, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st)))
+                             n, P->ng, P->nb, 2.0, wsp(ws, w.rot_scratch), st, kTriLower)))
     return rc;
   if (!adam) return JRG_OK;
   for (int part = 0; part < 2; ++part) {
@@ -1027,7 +1028,8 @@ static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re,
 static bool g_pipeline = true;   // two-way k-point pipeline of jrg_energy_grad
 
 static bool pipeline_ok(const jrg_plan* P) {
-  return P->ns * P->nk >= 2 && P->nb <= 32 && P->kchunk >= P->ns * P->nk && jrg_tensor_core_paths(-1) == 0 &&
+  return P->ns * P->nk >= 2 && P->nb <= 32 && P->kchunk >= P->ns * P->nk &&
+         (jrg_tensor_core_paths(-1) == 0 || jrg_tensor_core_paths(-1) == 3) &&
          jrg_fast_paths(-1) == 1 && !(P->prof && P->prof->max_calls > 0);
 }
 
@@ -1130,7 +1132,7 @@ static int coeff_adjoint_entry(const jrg_plan* P, const void* w_re, const void* 
                                  st)))
     return rc;
   return launch_rotate<R>(kRotGSplit, kBand, wsp(ws, w.gc), nullptr, rh, wsp(ws, w.c), negm2, g_re, g_im, nsk,
-                          P->ng, P->nb, 1.0, wsp(ws, w.rot_scratch), st);
+                          P->ng, P->nb, 1.0, wsp(ws, w.rot_scratch), st, kTriLower);
 }
 
 template <typename R>

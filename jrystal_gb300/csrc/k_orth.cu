@@ -174,13 +174,14 @@ __global__ void __launch_bounds__(256) k_gram_partial(const void* __restrict__ X
 constexpr int kGwCG = 64;   // G vectors per chunk
 
 template <typename R>
-size_t gram_w_smem(int NBP) {
-  const size_t stage = 2 * 2 * (size_t)kGwCG * (NBP + 1) * sizeof(C_t<R>);
-  const size_t red = 8 * (size_t)NBP * NBP * sizeof(double2);
+size_t gram_w_smem(int NBP, bool same = false) {
+  const size_t stage = (same ? 1 : 2) * 2 * (size_t)kGwCG * (NBP + 1) * sizeof(C_t<R>);
+  const size_t red = 8 * (size_t)NBP * NBP * sizeof(C_t<R>);
   return stage > red ? stage : red;
 }
 
-template <typename R, int LX, int LY, int NBP>
+// SAME: Y is X (W^H W): the chunk is staged once.
+template <typename R, int LX, int LY, int NBP, bool SAME = false>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
 k_gram_w(const void* __restrict__ X0, const void* __restrict__ X1, const void* __restrict__ Y0,
          const void* __restrict__ Y1, double2* __restrict__ part, int ng, int nb, int split_len) {
@@ -188,7 +189,7 @@ k_gram_w(const void* __restrict__ X0, const void* __restrict__ X1, const void* _
   constexpr int CG = kGwCG, LD = NBP + 1, TI = NBP / 4, TJ = NBP / 8;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* xs = reinterpret_cast<C*>(smem_raw);   // [2][CG][LD]
-  C* ys = xs + 2 * CG * LD;                 // [2][CG][LD]
+  C* ys = SAME ? xs : xs + 2 * CG * LD;     // [2][CG][LD]
   const int split = blockIdx.x;
   const size_t sk = blockIdx.z;
   const int nsplit = gridDim.x;
@@ -212,17 +213,19 @@ k_gram_w(const void* __restrict__ X0, const void* __restrict__ X1, const void* _
       C* dy = yd + c * LD + r;
       if (g >= g_end) {
         *dx = czero<C>();
-        *dy = czero<C>();
+        if (!SAME) *dy = czero<C>();
       } else if (LX == LAYOUT_SPLIT) {
         const size_t o = (sk * ng + g) * nb + r;
         cp_async<sizeof(R)>(&dx->x, reinterpret_cast<const R*>(X0) + o);
         cp_async<sizeof(R)>(&dx->y, reinterpret_cast<const R*>(X1) + o);
-        cp_async<sizeof(R)>(&dy->x, reinterpret_cast<const R*>(Y0) + o);
-        cp_async<sizeof(R)>(&dy->y, reinterpret_cast<const R*>(Y1) + o);
+        if (!SAME) {
+          cp_async<sizeof(R)>(&dy->x, reinterpret_cast<const R*>(Y0) + o);
+          cp_async<sizeof(R)>(&dy->y, reinterpret_cast<const R*>(Y1) + o);
+        }
       } else {
         const size_t o = (sk * nb + r) * ng + g;
         cp_async<sizeof(C)>(dx, reinterpret_cast<const C*>(X0) + o);
-        cp_async<sizeof(C)>(dy, reinterpret_cast<const C*>(Y0) + o);
+        if (!SAME) cp_async<sizeof(C)>(dy, reinterpret_cast<const C*>(Y0) + o);
       }
     }
     cp_async_commit();
@@ -263,25 +266,26 @@ k_gram_w(const void* __restrict__ X0, const void* __restrict__ X1, const void* _
     }
     __syncthreads();
   }
-  double2* red = reinterpret_cast<double2*>(smem_raw);   // [8][NBP][NBP]
+  // the eight warps' FP32 sums are added in FP32 (pairwise, a few roundings
+  // against the hundreds of each warp's own runs) and only the block total
+  // goes to FP64: FP64 arithmetic runs at 1/64 of the FP32 rate here
+  C* red = reinterpret_cast<C*>(smem_raw);   // [8][NBP][NBP]
 #pragma unroll
   for (int a = 0; a < TI; ++a)
 #pragma unroll
-    for (int b = 0; b < TJ; ++b)
-      red[((size_t)w * NBP + li + 4 * a) * NBP + lj + 8 * b] =
-          make_double2((double)acc[a][b].x, (double)acc[a][b].y);
+    for (int b = 0; b < TJ; ++b) red[((size_t)w * NBP + li + 4 * a) * NBP + lj + 8 * b] = acc[a][b];
   __syncthreads();
   const int nn = nb * nb;
   for (int e = t; e < nn; e += 256) {
     const int i = e / nb, j = e - i * nb;
-    double2 v = make_double2(0.0, 0.0);
+    C u[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const double2 u = red[((size_t)q * NBP + i) * NBP + j];
-      v.x += u.x;
-      v.y += u.y;
-    }
-    part[(sk * nsplit + split) * nn + e] = v;
+    for (int q = 0; q < 8; ++q) u[q] = red[((size_t)q * NBP + i) * NBP + j];
+#pragma unroll
+    for (int h = 4; h > 0; h >>= 1)
+#pragma unroll
+      for (int q = 0; q < h; ++q) { u[q].x += u[q + h].x; u[q].y += u[q + h].y; }
+    part[(sk * nsplit + split) * nn + e] = make_double2((double)u[0].x, (double)u[0].y);
   }
 }
 
@@ -964,9 +968,17 @@ int launch_gram_tc(int lx, const void* X0, const void* X1, int ly, const void* Y
 int launch_rotate_tc(int out_kind, int lx0, const void* X0a, const void* X0b, const double2* M0,
                      const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng,
                      int nb, double fac, uint32_t* bscratch, cudaStream_t st);
-// tensor-core contractions of the FP32 path: 0 CUDA cores (default), 1
-// mma.sync TF32 x 3 Gram and rotation, 2 tcgen05 TF32 x 3 Gram
+// contraction kernels: 0 CUDA cores (default: thread-per-G rotations of
+// k_rotate_g.cu), 1 mma.sync TF32 x 3 Gram and rotation (FP32 path), 2
+// tcgen05 TF32 x 3 Gram (FP32 path), 3 the register-blocked CUDA-core
+// rotations below
 static int g_tc_mode = 0;
+template <typename R>
+int launch_rotate_g(int out_kind, int lx0, const void* X0a, const void* X0b, const double2* M0, const void* X1,
+                    const double2* M1, void* out0, void* out1, int nsk, int ng, int nb, double fac,
+                    const AdamArgs& adam, const double* tk, int nk, void* kin_part, int sk0, int tri0,
+                    cudaStream_t st);
+constexpr int kTriUpper = 1, kTriLower = 2;   // zero patterns of M0 for launch_rotate_g
 int launch_gram_tc5(int lay, const void* X0, const void* X1, const void* Y0, const void* Y1,
                     double2* part, int nsk, int ng, int nb, int nsplit, int* err, cudaStream_t st);
 static bool g_gram_rb = true;       // register-blocked Gram for B <= 32 (else 32x32 tiles)
@@ -998,8 +1010,9 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
     // partial-sum traffic small
     nsplit = std::max(1, std::min(nsplit, (4 * 152 + nsk - 1) / nsk));
     const int split_len = (ng + nsplit - 1) / nsplit;
+    const bool same = X0 == Y0 && X1 == Y1 && lx == ly;
     auto go = [&](auto kern, int nbp) -> int {
-      const size_t sm = gram_w_smem<R>(nbp);
+      const size_t sm = gram_w_smem<R>(nbp, same);
       if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(gram_w)");
@@ -1010,6 +1023,12 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
     };
     auto pick = [&](auto lxc, auto lyc) -> int {
       constexpr int A = decltype(lxc)::value, B = decltype(lyc)::value;
+      if (same) {
+        if (nb <= 8) return go(k_gram_w<R, A, B, 8, true>, 8);
+        if (nb <= 16) return go(k_gram_w<R, A, B, 16, true>, 16);
+        if (nb <= 24) return go(k_gram_w<R, A, B, 24, true>, 24);
+        return go(k_gram_w<R, A, B, 32, true>, 32);
+      }
       if (nb <= 8) return go(k_gram_w<R, A, B, 8>, 8);
       if (nb <= 16) return go(k_gram_w<R, A, B, 16>, 16);
       if (nb <= 24) return go(k_gram_w<R, A, B, 24>, 24);
@@ -1100,11 +1119,15 @@ static int rotate_out(int lx0, const void* X0a, const void* X0b, const double2* 
 }
 
 // out_kind: ROT_*; lx0: layout of X0 (split: X0a=re, X0b=im; band: X0a); X1 is band-major
+// tri0: zero pattern of M0 (0 full, 1 upper triangular, 2 lower triangular)
 template <typename R>
 int launch_rotate(int out_kind, int lx0, const void* X0a, const void* X0b, const double2* M0,
                   const void* X1, const double2* M1, void* out0, void* out1, int nsk, int ng, int nb,
-                  double fac, void* scratch, cudaStream_t st) {
+                  double fac, void* scratch, cudaStream_t st, int tri0) {
   if (X1 && lx0 != LAYOUT_BAND) return fail(JRG_ERR_INVALID, "launch_rotate: two-term form needs band-major inputs");
+  if (g_tc_mode == 0)
+    return launch_rotate_g<R>(out_kind, lx0, X0a, X0b, M0, X1, M1, out0, out1, nsk, ng, nb, fac, AdamArgs{},
+                              nullptr, 1, nullptr, 0, tri0, st);
   if (sizeof(R) == 4 && g_tc_mode == 1) {
     const int t = launch_rotate_tc(out_kind, lx0, X0a, X0b, M0, X1, M1, out0, out1, nsk, ng, nb, fac,
                                    reinterpret_cast<uint32_t*>(scratch), st);
@@ -1155,6 +1178,11 @@ template <typename R>
 int launch_rotate_kinetic(const void* Wre, const void* Wim, const double2* Ri, void* C, int nsk,
                           int ng, int nb, const double* tk, int nk, void* kin_part,
                           cudaStream_t st, int sk0) {
+  if (g_tc_mode == 0) {
+    const int rc = launch_rotate_g<R>(ROT_BANDMAJOR, LAYOUT_SPLIT, Wre, Wim, Ri, nullptr, nullptr, C, nullptr, nsk,
+                                      ng, nb, 1.0, AdamArgs{}, tk, nk, kin_part, sk0, kTriUpper, st);
+    return rc ? -rc : (ng + 255) / 256;   // the thread-per-G kernel's 256 G vectors per block
+  }
   if (nb > 32 || !g_rotate_rb || (sizeof(R) == 4 && g_tc_mode == 1)) return 0;
   auto go = [&](auto kern, int nbp) -> int {
     const size_t sm = rotate_rb_smem<R>(nb, nbp);
@@ -1179,6 +1207,9 @@ int launch_rotate_kinetic(const void* Wre, const void* Wim, const double2* Ri, v
 template <typename R>
 int launch_rotate_adam(const void* X0, const double2* M0, const void* X1, const double2* M1,
                        const AdamArgs& a, int nsk, int ng, int nb, double fac, cudaStream_t st) {
+  if (g_tc_mode == 0)
+    return launch_rotate_g<R>(ROT_ADAM, LAYOUT_BAND, X0, nullptr, M0, X1, M1, nullptr, nullptr, nsk, ng, nb, fac,
+                              a, nullptr, 1, nullptr, 0, kTriLower, st);
   if (nb > 32) return fail(JRG_ERR_UNSUPPORTED, "k_rotate_rb: num_band > 32");
   auto go = [&](auto kern, int nbp) -> int {
     const size_t sm = rotate_rb_smem<R>(2 * nb, nbp, true);
@@ -1367,7 +1398,7 @@ int launch_reorthonormalise(void* wr, void* wi, double2* scratch, int nsk, int n
                               double2*, double2*, int, int, int, int, cudaStream_t, int*);      \
   template int launch_rotate<R>(int, int, const void*, const void*, const double2*, const void*,  \
                                 const double2*, void*, void*, int, int, int, double, void*,     \
-                                cudaStream_t);
+                                cudaStream_t, int);
 JRG_INST_ORTH(float)
 JRG_INST_ORTH(double)
 
@@ -1375,6 +1406,6 @@ JRG_INST_ORTH(double)
 
 extern "C" int jrg_tensor_core_paths(int enable) {
   const int prev = jrg::g_tc_mode;
-  if (enable >= 0 && enable <= 2) jrg::g_tc_mode = enable;
+  if (enable >= 0 && enable <= 3) jrg::g_tc_mode = enable;
   return prev;
 }

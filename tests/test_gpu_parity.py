@@ -203,7 +203,7 @@ def test_tensor_core_and_cuda_core_contractions_agree(nb, nocc, grid, kgrid):
   out = {}
   prev = lib.jrg_tensor_core_paths(-1)
   try:
-    for tc in (2, 1, 0):
+    for tc in (3, 2, 1, 0):
       lib.jrg_tensor_core_paths(tc)
       e, g1, g2 = plan.energy_and_grad(twr, twi, sysm.occupation)
       out[tc] = (e.cpu().numpy().copy(), g1.cpu().numpy(), g2.cpu().numpy())
@@ -211,7 +211,7 @@ def test_tensor_core_and_cuda_core_contractions_agree(nb, nocc, grid, kgrid):
     lib.jrg_tensor_core_paths(prev)
   tol = TOL[32]
   scale = max(np.abs(gr).max(), np.abs(gi).max())
-  for tc in (2, 1, 0):
+  for tc in (3, 2, 1, 0):
     e, g1, g2 = out[tc]
     assert e[6] == 0.0, (tc, e[6])
     for i, name in enumerate(["kinetic", "external", "hartree", "xc", "total"]):
