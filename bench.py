@@ -303,8 +303,7 @@ def phase_bytes(plan, fused=False):
     "gram": nbt * sph,
     "rotate": 2 * nbt * sph,
     # kinetic partials come out of the forward rotation; this phase sums them
-    "kinetic": nbt * ((plan.num_g + 255) // 256) * r if plan.num_band <= 32 else
-               nbt * sph + plan.num_kpt * plan.num_g * 8,
+    "kinetic": nbt * ((plan.num_g + 255) // 256) * r,
     "plane_inv_sphere": nbt * (sph + planes),
     "line_density": nbt * planes + nsk * ngrid * r,
     "reduce_density": nsk * ngrid * r + ngrid * r,
@@ -416,7 +415,7 @@ def run_ours(args, wl):
   occ = torch.tensor(wl.occupation, dtype=torch.float64, device=dev)
   state = {"t": 0}
 
-  fused = args.step == "fused" and wl.num_band <= 32
+  fused = args.step == "fused"
 
   def step_split(p):
     state["t"] += 1

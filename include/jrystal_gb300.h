@@ -205,7 +205,8 @@ int jrg_band_trace_grad(const jrg_plan* plan, const void* w_re, const void* w_im
  * update element ([2][S][K][G][B] FP32); with mlp_w32/mlp_wb given it is
  * first overwritten with the learned preconditioner's scales
  * (jrg_precond_scale at step fraction t_frac, cap smax) computed inside the
- * step from this step's band kinetic energies.  num_spin 1, num_band <= 32.
+ * step from this step's band kinetic energies.  num_spin 1; more than 32
+ * bands only with the default contraction kernels (jrg_tensor_core_paths 0).
  * With a non-zero status word (energies[6]) no update is applied: params, m
  * and v keep their values. */
 typedef struct {
@@ -330,7 +331,7 @@ int jrg_fast_paths(int enable);
 int jrg_tensor_core_paths(int enable);
 
 /* Two-way k-point pipeline of jrg_energy_grad (enable = 1, the default):
- * with at least two (s,k) blocks, num_band <= 32, the default contraction
+ * with at least two (s,k) blocks, the default contraction
  * and slab kernels and no phase profiling, the blocks are split in two
  * halves that run on the caller's stream and a second stream owned by the
  * plan (joined back before the call returns, in stream order), so that the

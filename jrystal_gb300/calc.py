@@ -79,7 +79,7 @@ class Minimizer:
   ``in_step(minimizer)`` method (precond.GuardedScale) instead hands the
   network to the device step, which evaluates it between the kinetic and the
   density phases.  With ``fused`` (the default where supported: one spin
-  channel, at most 32 bands) each step is one jrg_energy_grad_adam call: with
+  channel; more than 32 bands with the default contraction kernels) each step is one jrg_energy_grad_adam call: with
   the two-stream k-point pipeline each half of the k-points takes its Adam
   step as soon as its gradient is done (1.951 vs 1.963 ms per step for the
   two-call path on the 64^3 Si8 cell); ``grads`` is only filled when
@@ -102,7 +102,7 @@ class Minimizer:
     self.total_steps = total_steps
     self.scale_fn = scale_fn
     self.last_scale = None
-    supported = plan.num_spin == 1 and plan.num_band <= 32
+    supported = plan.num_spin == 1 and (plan.num_band <= 32 or plan.lib.jrg_tensor_core_paths(-1) == 0)
     self.fused = fused and supported
     self.keep_grad = keep_grad
     self.recoveries = 0

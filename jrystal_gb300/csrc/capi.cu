@@ -1028,7 +1028,8 @@ static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re,
 static bool g_pipeline = true;   // two-way k-point pipeline of jrg_energy_grad
 
 static bool pipeline_ok(const jrg_plan* P) {
-  return P->ns * P->nk >= 2 && P->nb <= 32 && P->kchunk >= P->ns * P->nk &&
+  // more than 32 bands: the thread-per-G rotations of mode 0 (fused kinetic partials)
+  return P->ns * P->nk >= 2 && (P->nb <= 32 || jrg_tensor_core_paths(-1) == 0) && P->kchunk >= P->ns * P->nk &&
          (jrg_tensor_core_paths(-1) == 0 || jrg_tensor_core_paths(-1) == 3) &&
          jrg_fast_paths(-1) == 1 && !(P->prof && P->prof->max_calls > 0);
 }
@@ -1234,7 +1235,8 @@ int jrg_energy_grad_adam(const jrg_plan* P, void* params, void* m, void* v, cons
   if (opt->mlp_w32 && (!opt->mlp_wb || !opt->scale))
     return fail(JRG_ERR_INVALID, "jrg_energy_grad_adam: the learned scale needs mlp_wb and a scale buffer");
   if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_adam: spin-polarised LDA is not implemented");
-  if (P->nb > 32) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_adam: num_band > 32");
+  if (P->nb > 32 && jrg_tensor_core_paths(-1) != 0)
+    return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_adam: num_band > 32 needs contraction mode 0");
   const size_t n = (size_t)P->ns * P->nk * P->ng * P->nb;
   const size_t half = n * (P->prec == 64 ? 8 : 4);
   auto hi = [&](void* b) { return b ? (void*)((char*)b + half) : nullptr; };

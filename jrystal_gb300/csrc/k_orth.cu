@@ -981,6 +981,8 @@ int launch_rotate_g(int out_kind, int lx0, const void* X0a, const void* X0b, con
 constexpr int kTriUpper = 1, kTriLower = 2;   // zero patterns of M0 for launch_rotate_g
 int launch_gram_tc5(int lay, const void* X0, const void* X1, const void* Y0, const void* Y1,
                     double2* part, int nsk, int ng, int nb, int nsplit, int* err, cudaStream_t st);
+int launch_gram_big(int lay, const void* X0, const void* X1, const void* Y0, const void* Y1, double2* part,
+                    double2* out, int nsk, int ng, int nb, int max_splits, cudaStream_t st);
 static bool g_gram_rb = true;       // register-blocked Gram for B <= 32 (else 32x32 tiles)
 static bool g_rotate_rb = true;     // register-blocked rotation for B <= 32
 void set_gram_rb(bool on) { g_gram_rb = on; g_rotate_rb = on; }
@@ -1005,6 +1007,8 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
     if (t < 0) return -t;
     if (t > 0) return JRG_OK;
   }
+  if (sizeof(R) == 4 && nb > 32 && g_tc_mode == 0 && lx == ly)   // 64 x 64 upper tiles
+    return launch_gram_big(lx, X0, X1, Y0, Y1, part, out, nsk, ng, nb, nsplit, st);
   if (nb <= 32 && g_gram_rb) {
     // about four blocks per SM in total: long G ranges per block keep the
     // partial-sum traffic small

@@ -24,7 +24,9 @@ def _state(sysm, plan, seed):
 
 
 @pytest.mark.parametrize("prec,nb,nocc,grid", [(64, 4, 2, (16, 16, 16)), (32, 12, 6, (24, 24, 24)),
-                                               (32, 30, 16, (16, 16, 16))])
+                                               (32, 30, 16, (16, 16, 16)),
+                                               # more than 32 bands: pipelined, 40-band tiles of 32 + 8
+                                               (32, 40, 20, (16, 16, 16)), (64, 40, 20, (16, 16, 16))])
 def test_fused_step_matches_two_call_path(prec, nb, nocc, grid):
   import torch
   from jrystal_gb300.engine import adam_update
@@ -100,8 +102,13 @@ def test_fused_step_rejects_bad_arguments():
   plan = _plan(sysm, 32, 40)
   occ = torch.tensor(sysm.occupation, device="cuda")
   p, m, v = _state(sysm, plan, 1)
-  with pytest.raises(NotImplementedError, match="num_band > 32"):
-    plan.energy_grad_adam(p, m, v, occ, 1, 1e-2)
+  lib = _lib.load()
+  prev = lib.jrg_tensor_core_paths(3)   # register-blocked rotations: at most 32 bands
+  try:
+    with pytest.raises(NotImplementedError, match="num_band > 32"):
+      plan.energy_grad_adam(p, m, v, occ, 1, 1e-2)
+  finally:
+    lib.jrg_tensor_core_paths(prev)
   with pytest.raises(ValueError):
     plan.energy_grad_adam(p, m.double(), v, occ, 1, 1e-2)
   with pytest.raises(ValueError, match="bad argument"):
