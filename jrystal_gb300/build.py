@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libjrystal_gb300.so")
-SOURCES = ["k_fft.cu", "k_fft_fast.cu", "k_orth.cu", "k_orth_tc.cu", "k_gram_tc5.cu", "k_grid.cu", "capi.cu", "noalloc.cu", "k_precond.cu", "k_nonlocal.cu", "batch.cu", "k_rotate_g.cu", "k_gram_big.cu"]
+SOURCES = ["k_fft.cu", "k_fft_fast.cu", "k_orth.cu", "k_orth_tc.cu", "k_gram_tc5.cu", "k_grid.cu", "capi.cu", "noalloc.cu", "k_precond.cu", "k_nonlocal.cu", "batch.cu", "k_rotate_g.cu", "k_gram_big.cu", "k_chol_df.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", INCLUDE]
 

@@ -20,7 +20,7 @@ template <typename R> int launch_fft3d_dense(const FftAxis*, const C_t<R>*, int,
 template <typename R> int launch_pack_params(const void*, const void*, void*, int, int, int, bool, cudaStream_t);
 template <typename R> int launch_unpack(const void*, void*, void*, void*, int, int, int, double, cudaStream_t);
 template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t, int* = nullptr);
-int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t, double);
+int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t, double, bool);
 int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t,
                          const double* = nullptr, double* = nullptr);
 template <typename R> int launch_rotate(int, int, const void*, const void*, const double2*, const void*, const double2*, void*, void*, int, int, int, double, void*, cudaStream_t, int = 0);
@@ -594,7 +594,7 @@ static int orthonormalise(const jrg_plan* P, const void* w_re, const void* w_im,
     PHASE(PH_CHOL);
     if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram), (double2*)wsp(ws, w.rmat),
                                   (double2*)wsp(ws, w.rinv), nsk, P->nb, (int*)wsp(ws, w.flags),
-                                  (double*)wsp(ws, w.dinv), st, min_pivot(P))))
+                                  (double*)wsp(ws, w.dinv), st, min_pivot(P), P->prec == 32)))
       return rc;
   }
   PHASE(PH_ROTATE);
@@ -959,7 +959,7 @@ static int phase_forward_range(const jrg_plan* P, const void* w_re, const void* 
     return rc;
   if ((rc = launch_cholesky_inv((double2*)wsp(ws, w.gram) + k0 * nb2, (double2*)wsp(ws, w.rmat) + k0 * nb2,
                                 (double2*)wsp(ws, w.rinv) + k0 * nb2, n, P->nb, flags,
-                                (double*)wsp(ws, w.dinv) + (size_t)k0 * P->nb, st, min_pivot(P))))
+                                (double*)wsp(ws, w.dinv) + (size_t)k0 * P->nb, st, min_pivot(P), P->prec == 32)))
     return rc;
   const int kb = launch_rotate_kinetic<R>(wr, wi, (double2*)wsp(ws, w.rinv) + k0 * nb2,
                                           (C*)wsp(ws, w.c) + co, n, P->ng, P->nb, P->d.tk, P->nk,
