@@ -1,5 +1,5 @@
-// Cholesky factor and inverse of the Gram matrices for more than 32 bands,
-// in double-float arithmetic on the FP32 pipes.
+// Cholesky factor and inverse of the Gram matrices of the FP32 path, in
+// double-float arithmetic on the FP32 pipes.
 //
 // FP64 arithmetic runs at 1/64 of the FP32 rate on this GPU, and a 160-band
 // Cholesky + triangular inverse is ~5.5 million complex multiply-adds per
@@ -9,7 +9,8 @@
 // 160 bands) as double-float pairs (hi + lo, about 48 significant bits: the
 // Dekker/Knuth error-free transformations TwoSum and TwoProd, the latter with
 // an FMA), and both the factorisation and the inversion take one barrier per
-// pivot:
+// pivot (256 threads up to 64 bands, 1024 above; the FP64 element-parallel
+// kernel takes more bands than the shared memory holds):
 //   factorisation (R^H R = S, R upper): at pivot k every thread reads the
 //     unscaled pivot d_k = U[k][k] and updates U[i][j] -= conj(U[k][i])
 //     U[k][j] / d_k for k < i <= j (one warp per row, lanes along j); the rows
@@ -86,10 +87,9 @@ __device__ __forceinline__ df recip(df x) {
 
 }  // namespace dfa
 
-constexpr int kCdThreads = 1024;
 
 __host__ __device__ inline size_t chol_df_smem(int nb) {
-  return (size_t)nb * (nb + 1) / 2 * sizeof(float4) + (size_t)nb * 2 * sizeof(double);
+  return (size_t)nb * (nb + 1) / 2 * sizeof(float4) + (size_t)nb * (sizeof(double) + 3 * sizeof(float));
 }
 
 // the 1/sqrt of the FP64 kernels (FP32 seed, three Newton steps in FP64)
@@ -101,15 +101,20 @@ __device__ __forceinline__ double rsqrt_nr(double d) {
   return r;
 }
 
-__global__ void __launch_bounds__(kCdThreads, 1)
+template <int NT>
+__global__ void __launch_bounds__(NT, 1)
 k_cholesky_inv_df(const double2* __restrict__ S, double2* __restrict__ Ri, int nb, int* __restrict__ flags,
                   double min_pivot) {
   using namespace dfa;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // FP64 work stays off the per-element paths (1/64 of the FP32 rate): the
+  // pivot test compares FP32 values, pivots and their inverse square roots
+  // are kept as double-float pairs, and one lane per row forms 1/sqrt(d_k)
   float4* U = reinterpret_cast<float4*>(smem_raw);                         // packed upper rows
   double* sdiag = reinterpret_cast<double*>(U + (size_t)nb * (nb + 1) / 2);  // S_kk
-  double* dpiv = sdiag + nb;                                                // d_k (after the replacement)
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = kCdThreads / 32;
+  float* thr = reinterpret_cast<float*>(sdiag + nb);                        // min_pivot S_kk
+  df* dpiv = reinterpret_cast<df*>(thr + nb);                               // d_k, then 1/sqrt(d_k)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = NT / 32;
   const size_t off = (size_t)blockIdx.x * nb * nb;
   auto idx = [nb](int i, int j) { return (size_t)i * (2 * nb - i + 1) / 2 + (j - i); };
   // upper triangle of the Hermitian part of S
@@ -118,15 +123,14 @@ k_cholesky_inv_df(const double2* __restrict__ S, double2* __restrict__ Ri, int n
       const double2 a = S[off + (size_t)i * nb + j], b = S[off + (size_t)j * nb + i];
       const double re = 0.5 * (a.x + b.x), im = i == j ? 0.0 : 0.5 * (a.y - b.y);
       st(U + idx(i, j), dc{from_d(re), from_d(im)});
-      if (i == j) sdiag[i] = a.x;
+      if (i == j) { sdiag[i] = a.x; thr[i] = (float)(min_pivot * a.x); }
     }
   __syncthreads();
   // factorisation with unscaled pivot rows
   bool broke = false;
   for (int k = 0; k < nb; ++k) {
     df d = ld(U + idx(k, k)).re;
-    const double dd = to_d(d);
-    if (!(dd > min_pivot * sdiag[k]) || !isfinite(dd)) { d = df{1.0f, 0.f}; broke = true; }
+    if (!(d.hi > thr[k]) || !isfinite(d.hi)) { d = df{1.0f, 0.f}; broke = true; }
     const df invd = recip(d);
     for (int i = k + 1 + warp; i < nb; i += nwarp) {
       const dc a = cscale(conj(ld(U + idx(k, i))), invd);   // conj(U[k][i]) / d_k
@@ -135,27 +139,33 @@ k_cholesky_inv_df(const double2* __restrict__ S, double2* __restrict__ Ri, int n
         st(p, csub(ld(p), cmul(a, ld(U + idx(k, j)))));
       }
     }
-    if (tid == 0) dpiv[k] = to_d(d);
+    if (tid == 0) dpiv[k] = d;
     __syncthreads();
   }
   if (broke && tid == 0) atomicOr(flags, 1);
   // row k scaled by 1/sqrt(d_k): R; sdiag keeps S_kk, dpiv becomes 1/sqrt(d_k)
   __syncthreads();
   for (int k = warp; k < nb; k += nwarp) {
-    const double rs = rsqrt_nr(dpiv[k]);
-    const df s = from_d(rs);
+    df s{0.f, 0.f}, r{0.f, 0.f};   // 1/sqrt(d_k), sqrt(d_k)
+    if (lane == 0) {
+      const double dk = to_d(dpiv[k]), rs = rsqrt_nr(dk);
+      s = from_d(rs);
+      r = from_d(dk * rs);
+    }
+    s.hi = __shfl_sync(0xffffffffu, s.hi, 0); s.lo = __shfl_sync(0xffffffffu, s.lo, 0);
+    r.hi = __shfl_sync(0xffffffffu, r.hi, 0); r.lo = __shfl_sync(0xffffffffu, r.lo, 0);
     for (int j = k + lane; j < nb; j += 32) {
       float4* p = U + idx(k, j);
-      if (j == k) st(p, dc{from_d(dpiv[k] * rs), df{0.f, 0.f}});
+      if (j == k) st(p, dc{r, df{0.f, 0.f}});
       else st(p, cscale(ld(p), s));
     }
     __syncwarp();
-    if (lane == 0) dpiv[k] = rs;
+    if (lane == 0) dpiv[k] = s;
   }
   __syncthreads();
   // inversion in place, bottom-up
   for (int k = nb - 1; k >= 0; --k) {
-    const df dk = from_d(dpiv[k]);   // 1 / R[k][k] = X[k][k]
+    const df dk = dpiv[k];   // 1 / R[k][k] = X[k][k]
     for (int i = warp; i < k; i += nwarp) {
       const dc r = ld(U + idx(i, k));   // R[i][k]
       __syncwarp();                     // every lane has R[i][k] before lane j = k overwrites it
@@ -173,10 +183,10 @@ k_cholesky_inv_df(const double2* __restrict__ S, double2* __restrict__ Ri, int n
   }
   // X[k][j] = a_kj / R[k][k] (j > k), X[k][k] = 1 / R[k][k]; lower part zero
   for (int i = warp; i < nb; i += nwarp) {
-    const df di = from_d(dpiv[i]);
+    const df di = dpiv[i];
     for (int j = lane; j < nb; j += 32) {
       double2 v = make_double2(0.0, 0.0);
-      if (j == i) v = make_double2(dpiv[i], 0.0);
+      if (j == i) v = make_double2(to_d(di), 0.0);
       else if (j > i) {
         const dc x = cscale(ld(U + idx(i, j)), di);
         v = make_double2(to_d(x.re), to_d(x.im));
@@ -187,7 +197,10 @@ k_cholesky_inv_df(const double2* __restrict__ S, double2* __restrict__ Ri, int n
   // condition estimate off the pivot chain: S_kk / d_k = S_kk (1/sqrt(d_k))^2
   if (warp == 0) {
     double c = 0.0;
-    for (int k = lane; k < nb; k += 32) c = fmax(c, fabs(sdiag[k]) * dpiv[k] * dpiv[k]);
+    for (int k = lane; k < nb; k += 32) {
+      const double r = to_d(dpiv[k]);
+      c = fmax(c, fabs(sdiag[k]) * r * r);
+    }
     for (int o = 16; o > 0; o >>= 1) c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
     if (lane == 0) {
       double est = broke ? __longlong_as_double(0x7ff0000000000000LL) : c;
@@ -206,9 +219,15 @@ int launch_cholesky_inv_df(const double2* S, double2* Ri, int nsk, int nb, int* 
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
   if (sm > (size_t)optin) return 0;
-  cudaError_t e = cudaFuncSetAttribute(k_cholesky_inv_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  // one warp per row of the update: 8 warps up to 64 bands, 32 above
+  auto go = [&](auto kern, int nt) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    kern<<<nsk, nt, sm, st>>>(S, Ri, nb, flags, min_pivot);
+    return cudaSuccess;
+  };
+  cudaError_t e = nb <= 64 ? go(k_cholesky_inv_df<256>, 256) : go(k_cholesky_inv_df<1024>, 1024);
   if (e != cudaSuccess) return -cuda_fail(e, "cudaFuncSetAttribute(k_cholesky_inv_df)");
-  k_cholesky_inv_df<<<nsk, kCdThreads, sm, st>>>(S, Ri, nb, flags, min_pivot);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return -cuda_fail(e, "k_cholesky_inv_df");

@@ -1069,11 +1069,11 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
 
 int launch_cholesky_inv_df(const double2* S, double2* Ri, int nsk, int nb, int* flags, double min_pivot,
                            cudaStream_t st);
-// df: the FP32 path may use the double-float kernel for more than 32 bands
-// (R itself is then not written: only R^-1 is consumed)
+// df: the FP32 path uses the double-float kernel (R itself is then not
+// written: only R^-1 is consumed)
 int launch_cholesky_inv(const double2* S, double2* Rm, double2* Ri, int nsk, int nb, int* flags,
                         double* dinv_scratch, cudaStream_t st, double min_pivot, bool df) {
-  if (df && nb > 32 && g_tc_mode == 0) {
+  if (df && g_tc_mode == 0) {
     const int r = launch_cholesky_inv_df(S, Ri, nsk, nb, flags, min_pivot, st);
     if (r < 0) return -r;
     if (r > 0) return JRG_OK;
