@@ -248,6 +248,35 @@ k_rotate_g(const void* __restrict__ X0a, const void* __restrict__ X0b, const dou
     for (int q = 0; q < TG; ++q) {
       if (g[q] >= ng) continue;
       const size_t base = (sk * ng + g[q]) * nb + j0;
+      if constexpr (VOUT && sizeof(R) == 4) {
+        // 16-byte accesses: nb % 4 == 0 and NJ % 4 == 0
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+          float* p = reinterpret_cast<float*>(adam.p[part]) + base;
+          float* m = reinterpret_cast<float*>(adam.m[part]) + base;
+          float* v = reinterpret_cast<float*>(adam.v[part]) + base;
+          float* gout = adam.grad[part] ? reinterpret_cast<float*>(adam.grad[part]) + base : nullptr;
+          const float* sc = adam.scale[part] ? adam.scale[part] + base : nullptr;
+#pragma unroll
+          for (int jj = 0; jj < NJ; jj += 4)
+            if (jj < nj) {
+              float gv[4], mv[4], vv[4], pv[4], sv[4] = {1.f, 1.f, 1.f, 1.f};
+#pragma unroll
+              for (int u = 0; u < 4; ++u) gv[u] = fac * (part ? acc[q][jj + u].y : acc[q][jj + u].x);
+              *reinterpret_cast<float4*>(mv) = *reinterpret_cast<const float4*>(m + jj);
+              *reinterpret_cast<float4*>(vv) = *reinterpret_cast<const float4*>(v + jj);
+              *reinterpret_cast<float4*>(pv) = *reinterpret_cast<const float4*>(p + jj);
+              if (sc) *reinterpret_cast<float4*>(sv) = *reinterpret_cast<const float4*>(sc + jj);
+              if (gout) *reinterpret_cast<float4*>(gout + jj) = *reinterpret_cast<const float4*>(gv);
+#pragma unroll
+              for (int u = 0; u < 4; ++u) pv[u] += sv[u] * adam_one<float>(gv[u], mv[u], vv[u], lr, b1, b2, c1, c2, eps);
+              *reinterpret_cast<float4*>(m + jj) = *reinterpret_cast<const float4*>(mv);
+              *reinterpret_cast<float4*>(v + jj) = *reinterpret_cast<const float4*>(vv);
+              *reinterpret_cast<float4*>(p + jj) = *reinterpret_cast<const float4*>(pv);
+            }
+        }
+        continue;
+      }
 #pragma unroll
       for (int part = 0; part < 2; ++part) {
         R* p = reinterpret_cast<R*>(adam.p[part]) + base;
@@ -283,7 +312,7 @@ static int rg_go(const void* X0a, const void* X0b, const double2* M0, const void
                  const double* tk, int nk, void* kin_part, int sk0, int tri0, cudaStream_t st) {
   const size_t sm = rg_smem<R, NJ>(nb, X1 != nullptr);
   const bool vin = LX0 == RG_SPLIT && nb % 4 == 0 && sizeof(R) == 4;
-  const bool vout = OUT == RG_GMAJOR_SPLIT && nb % 4 == 0 && NJ % 4 == 0 && sizeof(R) == 4;
+  const bool vout = (OUT == RG_GMAJOR_SPLIT || OUT == RG_ADAM) && nb % 4 == 0 && NJ % 4 == 0 && sizeof(R) == 4;
   auto go = [&](auto kern) -> int {
     if (sm > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -298,7 +327,7 @@ static int rg_go(const void* X0a, const void* X0b, const double2* M0, const void
   if constexpr (LX0 == RG_SPLIT && sizeof(R) == 4) {
     if (vin) return go(k_rotate_g<R, LX0, OUT, NJ, TG, true, false, MINB>);
     return go(k_rotate_g<R, LX0, OUT, NJ, TG, false, false, MINB>);
-  } else if constexpr (OUT == RG_GMAJOR_SPLIT && sizeof(R) == 4 && NJ % 4 == 0) {
+  } else if constexpr ((OUT == RG_GMAJOR_SPLIT || OUT == RG_ADAM) && sizeof(R) == 4 && NJ % 4 == 0) {
     if (vout) return go(k_rotate_g<R, LX0, OUT, NJ, TG, false, true, MINB>);
     return go(k_rotate_g<R, LX0, OUT, NJ, TG, false, false, MINB>);
   } else {
