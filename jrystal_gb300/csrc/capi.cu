@@ -19,7 +19,7 @@ template <typename R> int launch_plane_fwd_sphere(const jrg_plan*, const void*, 
 template <typename R> int launch_fft3d_dense(const FftAxis*, const C_t<R>*, int, int, bool, const void*, C_t<R>*, C_t<R>*, double, cudaStream_t);
 template <typename R> int launch_pack_params(const void*, const void*, void*, int, int, int, bool, cudaStream_t);
 template <typename R> int launch_unpack(const void*, void*, void*, void*, int, int, int, double, cudaStream_t);
-template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t, int* = nullptr);
+template <typename R> int launch_gram(int, const void*, const void*, int, const void*, const void*, double2*, double2*, int, int, int, int, cudaStream_t, int* = nullptr, bool = false);
 int launch_cholesky_inv(const double2*, double2*, double2*, int, int, int*, double*, cudaStream_t, double, bool);
 int launch_adjoint_small(const double2*, const double2*, double2*, double2*, int, int, cudaStream_t,
                          const double* = nullptr, double* = nullptr);
@@ -35,6 +35,10 @@ template <typename R> int launch_real_part(const void*, void*, long long, double
 template <typename R> int launch_hartree_g(const void*, const double*, void*, long long, double, cudaStream_t);
 template <typename R> int launch_kinetic(const void*, const double*, const double*, double*, double*, int, int, int, int, cudaStream_t);
 int launch_precond_scale(const float*, const void*, const double*, const double*, const double*, int, int, int, long long, float, float, float*, cudaStream_t);
+int launch_precond_scale_lut(const float*, const void*, const double*, const float*, float, const double*,
+                             const double*, int, int, int, int, long long, float, float, float*, float*,
+                             cudaStream_t);
+size_t precond_lut_floats(int nb, int nbt);
 int launch_sum_slots(const double*, const int*, double*, int, const int*, int, cudaStream_t);
 int nl_splits(int ng, int nsk, int nb, int np);
 int nl_chunks(int nb, int np);
@@ -161,6 +165,7 @@ static void layout_workspace_k(jrg_plan* P, int kc) {
   w.nl_splits = P->nproj > 0 ? nl_splits(P->ng, (int)nsk, P->nb, P->nproj) : 0;
   w.nl_part = P->nproj > 0 ? take(nsk * w.nl_splits * (size_t)P->nb * P->nproj * sizeof(double2)) : 0;
   w.nl_fw = P->nproj > 0 ? take(nbt * (size_t)P->nproj * sizeof(double2)) : 0;
+  w.lut = take(precond_lut_floats(P->nb, (int)nbt) * sizeof(float));   // in-step preconditioner table
   w.total = o;
 }
 
@@ -231,7 +236,7 @@ const char* jrg_last_error(void) { return g_err.c_str(); }
 int jrg_plan_destroy(jrg_plan* P) {
   if (!P) return JRG_OK;
   void* ptrs[] = {P->d.gidx, P->d.sph_yz, P->d.plane_x, P->d.plane_off, P->d.row_off, P->d.rows,
-                  P->d.xact, P->d.tk, P->d.tw, P->d.vext, P->d.ginv, P->d.gvec, P->d.proj,
+                  P->d.xact, P->d.tk, P->d.tkf, P->d.tw, P->d.vext, P->d.ginv, P->d.gvec, P->d.proj,
                   P->d.rowmap};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -367,6 +372,10 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
       tk[(size_t)k * ng + e] = 0.5 * s;
     }
   }
+  // FP32 copy and maximum for the tabulated in-step preconditioner
+  std::vector<float> tkf(tk.size());
+  P->tk_max = 0.f;
+  for (size_t i = 0; i < tk.size(); ++i) { tkf[i] = (float)tk[i]; P->tk_max = std::max(P->tk_max, tkf[i]); }
   // shared-memory limits of the slab kernels
   {
     int dev = 0;
@@ -398,7 +407,7 @@ int jrg_plan_create(const jrg_plan_desc* d, jrg_plan** out) {
 #define UP(field, vec) \
   if (!rc) rc = up((void**)&P->d.field, vec.data(), vec.size() * sizeof(vec[0]));
   UP(gidx, gidx) UP(sph_yz, sph_yz) UP(plane_x, plane_x) UP(plane_off, plane_off)
-  UP(row_off, row_off) UP(rows, rows) UP(xact, xact) UP(tk, tk) UP(rowmap, rowmap)
+  UP(row_off, row_off) UP(rows, rows) UP(xact, xact) UP(tk, tk) UP(tkf, tkf) UP(rowmap, rowmap)
 #undef UP
   // twiddles (host, double precision): x, y, z tables
   if (!rc) {
@@ -799,9 +808,10 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
   if (adam && adam->mlp_w32) {
     // learned update scales from this step's band kinetic energies
     PHASE(PH_PRECOND);
-    if ((rc = launch_precond_scale(adam->mlp_w32, adam->mlp_wb, P->d.tk, (const double*)wsp(ws, w.ekin),
-                                   occ, P->nk, P->ng, P->nb, (long long)nbt * P->ng, adam->t_frac,
-                                   adam->smax, adam->scale[0], st)))
+    if ((rc = launch_precond_scale_lut(adam->mlp_w32, adam->mlp_wb, P->d.tk, P->d.tkf, P->tk_max,
+                                       (const double*)wsp(ws, w.ekin), occ, P->nk, P->ng, P->nb, nbt,
+                                       (long long)nbt * P->ng, adam->t_frac, adam->smax, adam->scale[0],
+                                       (float*)wsp(ws, w.lut), st)))
       return rc;
   }
   if ((rc = nl_forward<R>(P, ws, 0, nsk, occ, band_e ? P->d_ones : occ, st))) return rc;
@@ -909,7 +919,7 @@ static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im
     PHASE(PH_ADJ_GRAM);
     if ((rc = launch_gram<R>(kBand, wsp(ws, w.c), nullptr, kBand, wsp(ws, w.gc), nullptr,
                              (double2*)wsp(ws, w.adj_part), (double2*)wsp(ws, w.adj), nsk, P->ng,
-                             P->nb, w.gram_splits, st, (int*)wsp(ws, w.flags))))
+                             P->nb, w.gram_splits, st, (int*)wsp(ws, w.flags), true)))
       return rc;
   }
   if ((rc = launch_band_trace_sums((const double2*)wsp(ws, w.adj), nsk, P->nb, slots, nbt, out, st)))
@@ -1065,9 +1075,10 @@ static int energy_grad_pipelined(const jrg_plan* P, const void* w_re, const void
                               (double*)wsp(ws, w.ekin), st)))
     return rc;
   if (adam && adam->mlp_w32 &&
-      (rc = launch_precond_scale(adam->mlp_w32, adam->mlp_wb, P->d.tk, (const double*)wsp(ws, w.ekin), occ,
-                                 P->nk, P->ng, P->nb, (long long)nbt * P->ng, adam->t_frac, adam->smax,
-                                 adam->scale[0], st)))
+      (rc = launch_precond_scale_lut(adam->mlp_w32, adam->mlp_wb, P->d.tk, P->d.tkf, P->tk_max,
+                                     (const double*)wsp(ws, w.ekin), occ, P->nk, P->ng, P->nb, nbt,
+                                     (long long)nbt * P->ng, adam->t_frac, adam->smax, adam->scale[0],
+                                     (float*)wsp(ws, w.lut), st)))
     return rc;
   if ((rc = launch_reduce_density<R>(wsp(ws, w.rho_part), wsp(ws, w.rho), P->nk, P->ns, P->ngrid,
                                      (const double*)wsp(ws, w.rho_scale), (double*)wsp(ws, w.rho_q), st)))

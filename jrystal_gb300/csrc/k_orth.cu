@@ -988,9 +988,13 @@ static bool g_rotate_rb = true;     // register-blocked rotation for B <= 32
 void set_gram_rb(bool on) { g_gram_rb = on; g_rotate_rb = on; }
 
 template <typename R>
+// full: every element of S is consumed (the band Hamiltonian C^H H C with
+// band weights); otherwise the upper triangle suffices (W^H W is Hermitian,
+// the energy adjoint reads the upper triangle of C^H g_C) and more than 32
+// bands take the upper-tile kernel
 int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, const void* Y1,
                 double2* part, double2* out, int nsk, int ng, int nb, int nsplit, cudaStream_t st,
-                int* flags) {
+                int* flags, bool full) {
   if (sizeof(R) == 4 && g_tc_mode == 2 && lx == ly) {   // tcgen05 Gram (TF32 x 3)
     const int ns = launch_gram_tc5(lx, X0, X1, Y0, Y1, part, nsk, ng, nb, nsplit, flags, st);
     if (ns < 0) return -ns;
@@ -1007,7 +1011,7 @@ int launch_gram(int lx, const void* X0, const void* X1, int ly, const void* Y0, 
     if (t < 0) return -t;
     if (t > 0) return JRG_OK;
   }
-  if (sizeof(R) == 4 && nb > 32 && g_tc_mode == 0 && lx == ly)   // 64 x 64 upper tiles
+  if (sizeof(R) == 4 && nb > 32 && g_tc_mode == 0 && lx == ly && !full)   // 32 x 32 upper tiles
     return launch_gram_big(lx, X0, X1, Y0, Y1, part, out, nsk, ng, nb, nsplit, st);
   if (nb <= 32 && g_gram_rb) {
     // about four blocks per SM in total: long G ranges per block keep the
@@ -1408,7 +1412,7 @@ int launch_reorthonormalise(void* wr, void* wi, double2* scratch, int nsk, int n
   template int launch_unpack<R>(const void*, void*, void*, void*, int, int, int, double,          \
                                 cudaStream_t);                                                  \
   template int launch_gram<R>(int, const void*, const void*, int, const void*, const void*,       \
-                              double2*, double2*, int, int, int, int, cudaStream_t, int*);      \
+                              double2*, double2*, int, int, int, int, cudaStream_t, int*, bool); \
   template int launch_rotate<R>(int, int, const void*, const void*, const double2*, const void*,  \
                                 const double2*, void*, void*, int, int, int, double, void*,     \
                                 cudaStream_t, int);

@@ -97,10 +97,15 @@ __device__ __forceinline__ void dense_mma(const uint32_t (&a)[4][4], const __nv_
 
 // scale[e] for every parameter element e of (S,K,G,B) (written twice: the
 // real and imaginary parameter share the scale of their coefficient).
+// LUT: the table of the in-step form instead, element e = b * kLutN + i
+// with x1 = i * x1max / (kLutN - 1) (x1max in hdr[0]), x2 = b / nb.
+constexpr int kLutN = 4096;
+template <bool LUT>
 __global__ void __launch_bounds__(128) k_precond_scale(
     const float* __restrict__ wf, const __nv_bfloat16* __restrict__ wb,
     const double* __restrict__ tk, const double* __restrict__ ekin, const double* __restrict__ occ,
-    int nk, int ng, int nb, long long total, float t_frac, float smax, float* __restrict__ out) {
+    int nk, int ng, int nb, long long total, float t_frac, float smax, float* __restrict__ out,
+    const float* __restrict__ hdr = nullptr) {
   __shared__ __align__(16) __nv_bfloat16 w2[kH * kWPitch];
   __shared__ __align__(16) __nv_bfloat16 w3[kH * kWPitch];
   __shared__ float w1[kH * 3], b1[kH], b2[kH], b3[kH], w4[kH];
@@ -129,6 +134,13 @@ __global__ void __launch_bounds__(128) k_precond_scale(
       const long long e = tile * 16 + g + 8 * h;
       live[h] = e < total;
       const long long ee = live[h] ? e : 0;
+      if constexpr (LUT) {
+        const int b = (int)(ee / kLutN), i = (int)(ee % kLutN);
+        x[h][0] = hdr[0] * (float)i / (float)(kLutN - 1);
+        x[h][1] = (float)b / (float)nb;
+        x[h][2] = t_frac;
+        continue;
+      }
       const int b = (int)(ee % nb);
       const long long rest = ee / nb;
       const int gg = (int)(rest % ng);
@@ -179,9 +191,13 @@ __global__ void __launch_bounds__(128) k_precond_scale(
       for (int h = 0; h < 2; ++h) {
         if (!live[h]) continue;
         const long long e = tile * 16 + g + 8 * h;
-        const long long band = e / ((long long)nb * ng) * nb + e % nb;
         float s = softplus((h ? p1 : p0) + b4);
         s = fminf(s, smax);
+        if constexpr (LUT) {
+          out[e] = s;
+          continue;
+        }
+        const long long band = e / ((long long)nb * ng) * nb + e % nb;
         if (occ[band] == 0.0) s = 1.0f;
         out[e] = s;
         out[total + e] = s;
@@ -321,9 +337,92 @@ int launch_precond_scale(const float* wf, const void* wb, const double* tk, cons
   const long long ntiles = (total + 15) / 16;
   long long blocks = (ntiles + 3) / 4;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  k_precond_scale<<<(unsigned)blocks, 128, 0, st>>>(wf, reinterpret_cast<const __nv_bfloat16*>(wb), tk,
-                                                    ekin, occ, nk, ng, nb, total, t_frac, smax, out);
+  k_precond_scale<false><<<(unsigned)blocks, 128, 0, st>>>(wf, reinterpret_cast<const __nv_bfloat16*>(wb), tk,
+                                                           ekin, occ, nk, ng, nb, total, t_frac, smax, out);
   JRG_LAUNCH_CHECK("k_precond_scale");
+  return JRG_OK;
+}
+
+// ---- in-step form: the network tabulated in x1 ---------------------------
+// The features of a coefficient are x1 = |G+k|^2/2 / E_kin(band), x2 = band/B
+// and the step fraction x3, so within one call the scale is a function of x1
+// for each band b.  The in-step form evaluates the network (the same BF16
+// tensor-core inference) on kLutN points x1_i = i x1max / (kLutN - 1) per
+// band, x1max the largest x1 of the occupied bands, and every coefficient
+// interpolates linearly in its band's table: nb * kLutN network evaluations
+// instead of one per coefficient (the inference of 11 M coefficients at the
+// 64^3 Si8 cell took ~0.6 ms per step; the table and the interpolation pass,
+// a read of the FP32 kinetic table and a write of the scales, take a few
+// percent of that).  Workspace: precond_lut_floats(nb, nbt) floats.
+size_t precond_lut_floats(int nb, int nbt) { return 4 + (size_t)nb * kLutN + (size_t)nbt; }
+
+// hdr[0] = x1max = tk_max / (smallest occupied-band E_kin); invek[band] =
+// 1 / E_kin(band), -1 for an empty band
+__global__ void __launch_bounds__(1024) k_precond_prep(float tmax, const double* __restrict__ ekin,
+                                                       const double* __restrict__ occ, int nbt,
+                                                       float* __restrict__ hdr, float* __restrict__ invek) {
+  __shared__ float red[32];
+  float emin = 3.0e38f;
+  for (int b = threadIdx.x; b < nbt; b += blockDim.x) {
+    const double ek = ekin[b];
+    const bool on = occ[b] != 0.0;
+    const float e = (float)(ek > 1e-30 ? ek : 1e-30);
+    invek[b] = on ? 1.0f / e : -1.0f;
+    if (on) emin = fminf(emin, e);
+  }
+  for (int o = 16; o > 0; o >>= 1) emin = fminf(emin, __shfl_xor_sync(0xffffffffu, emin, o));
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) red[w] = emin;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) emin = fminf(emin, red[i]);
+    hdr[0] = emin < 3.0e38f ? fmaxf(tmax / emin, 1e-6f) * 1.0001f : 1.0f;
+  }
+}
+
+// out[e] (and out[total + e]): the band's table at x1 = tkf[k][g] * invek[band]
+__global__ void k_precond_apply(const float* __restrict__ hdr, const float* __restrict__ lut,
+                                const float* __restrict__ invek, const float* __restrict__ tkf, int nk, int ng,
+                                int nb, long long total, float* __restrict__ out) {
+  const float pos = (float)(kLutN - 1) / hdr[0];
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(e % nb);
+    const long long rest = e / nb;
+    const int gg = (int)(rest % ng);
+    const long long sk = rest / ng;
+    const float ie = invek[sk * nb + b];
+    float s = 1.0f;
+    if (ie >= 0.f) {
+      const float u = fminf(tkf[(size_t)(sk % nk) * ng + gg] * ie * pos, (float)(kLutN - 1));
+      const int i0 = min((int)u, kLutN - 2);
+      const float f = u - (float)i0;
+      const float* tb = lut + (size_t)b * kLutN;
+      s = fmaf(f, tb[i0 + 1] - tb[i0], tb[i0]);
+    }
+    out[e] = s;
+    out[total + e] = s;
+  }
+}
+
+int launch_precond_scale_lut(const float* wf, const void* wb, const double* tk, const float* tkf, float tk_max,
+                             const double* ekin, const double* occ, int nk, int ng, int nb, int nbt,
+                             long long total, float t_frac, float smax, float* out, float* lutws,
+                             cudaStream_t st) {
+  float* hdr = lutws;
+  float* lut = lutws + 4;
+  float* invek = lut + (size_t)nb * kLutN;
+  k_precond_prep<<<1, 1024, 0, st>>>(tk_max, ekin, occ, nbt, hdr, invek);
+  JRG_LAUNCH_CHECK("k_precond_prep");
+  const long long n = (long long)nb * kLutN;
+  const long long blocks = ((n + 15) / 16 + 3) / 4;
+  k_precond_scale<true><<<(unsigned)blocks, 128, 0, st>>>(wf, reinterpret_cast<const __nv_bfloat16*>(wb), tk,
+                                                          ekin, occ, nk, ng, nb, n, t_frac, smax, lut, hdr);
+  JRG_LAUNCH_CHECK("k_precond_scale(table)");
+  long long ab = (total + 255) / 256;
+  if (ab > 152 * 8) ab = 152 * 8;
+  k_precond_apply<<<(unsigned)ab, 256, 0, st>>>(hdr, lut, invek, tkf, nk, ng, nb, total, out);
+  JRG_LAUNCH_CHECK("k_precond_apply");
   return JRG_OK;
 }
 

@@ -338,12 +338,17 @@ static int rg_go(const void* X0a, const void* X0b, const double2* M0, const void
 // Tile shapes: the band count rounded up to 8, at most 32 (FP32) or 16
 // (FP64) columns per tile, one G vector per thread (two G vectors per thread
 // with 8- or 12-column tiles measured within 1 % at 24 bands and slower at
-// 160 bands, where more tiles re-read X).
+// 160 bands, where more tiles re-read X; 16-column tiles at three CTAs per
+// SM slower at 24 bands).
 template <typename R, int LX0, int OUT>
 static int rg_pick(const void* X0a, const void* X0b, const double2* M0, const void* X1, const double2* M1,
                    void* out0, void* out1, int nsk, int ng, int nb, double fac, const AdamArgs& adam,
                    const double* tk, int nk, void* kin_part, int sk0, int tri0, cudaStream_t st) {
 #define RG_ARGS X0a, X0b, M0, X1, M1, out0, out1, nsk, ng, nb, fac, adam, tk, nk, kin_part, sk0, tri0, st
+  // the forward rotation (one term, triangular) is latency-bound: 8-column
+  // tiles at four CTAs per SM (0.083 -> 0.067 ms at 24 bands); the two-term
+  // adjoint keeps one tile
+  if (sizeof(R) == 4 && OUT == RG_BANDMAJOR && nb <= 32) return rg_go<R, LX0, OUT, 8, 1, 4>(RG_ARGS);
   if (nb <= 8) return rg_go<R, LX0, OUT, 8, 1, 2>(RG_ARGS);
   if (sizeof(R) == 8 || nb <= 16) return rg_go<R, LX0, OUT, 16, 1, 2>(RG_ARGS);
   if (nb <= 24) return rg_go<R, LX0, OUT, 24, 1, 2>(RG_ARGS);

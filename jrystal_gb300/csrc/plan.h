@@ -57,6 +57,7 @@ struct PlanTables {
   int* rowmap = nullptr;      // [total active rows][nz]: sphere index of (row, z), or -1
   int* xact = nullptr;        // [nx] active-plane slot of x, or -1
   double* tk = nullptr;       // [nk][ng] |G+k|^2 / 2
+  float* tkf = nullptr;       // the same in FP32 (tabulated preconditioner)
   void* tw = nullptr;         // twiddles: x table, y table, z table (C_t<R>)
   void* vext = nullptr;       // [ngrid] complex V_ext(G) in precision R
   double2* vext64 = nullptr;  // [ngrid] the same table in FP64 (= vext at FP64)
@@ -98,7 +99,7 @@ struct AdamArgs {
 // Workspace offsets (bytes) of one plan.
 struct Workspace {
   size_t wc, c, gram_part, gram, rmat, rinv, t, u, rho_part, rho_scale, rho_q, rho, rhog, fft_scratch, vr,
-      gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, kin_part, nl_part, nl_fw,
+      gc, adj_part, adj, kmat, epart, flags, ekin, dinv, rot_scratch, gga, kin_part, nl_part, nl_fw, lut,
       total;
   size_t t_bytes; // plane buffer
   int gram_splits;
@@ -127,6 +128,7 @@ struct jrg_plan {
   int nproj = 0;            // beta-projector rows of the pseudopotential (0: all-electron)
   size_t mem_limit = 0;     // workspace bound set by jrg_plan_set_memory_limit (0: none)
   int kchunk = 0;           // (s,k) blocks whose plane buffers are resident at once
+  float tk_max = 0.f;       // largest |G+k|^2 / 2 of the plan
   jrg::FftAxis ax[3];
   jrg::PlanTables d;
   jrg::Workspace ws;

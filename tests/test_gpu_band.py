@@ -26,6 +26,8 @@ def _veff(sysm, seed=1):
   dict(kind="si2", grid=(16, 16, 16), kgrid=(2, 1, 1), nb=4, nocc=2),
   dict(kind="si8", grid=(24, 24, 24), kgrid=(1, 1, 2), nb=12, nocc=8),
   dict(kind="diamond", grid=(14, 15, 16), kgrid=(1, 1, 1), nb=5, nocc=3),
+  # more than 32 bands: the full band Hamiltonian (not the upper-tile Gram)
+  dict(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 1), nb=36, nocc=20),
 ])
 def test_band_trace_grad_matches_oracle(prec, case):
   import torch

@@ -88,10 +88,11 @@ def test_fused_learned_step_matches_host_scaled_step():
     es = [float(mini.step()[4]) for _ in range(6)]
     runs[fused] = (mini.params.cpu().numpy(), es, mini.last_scale.cpu().numpy())
   np.testing.assert_allclose(runs[True][1], runs[False][1], rtol=1e-6)
-  # BF16 inference: FP32-rounding differences of the inputs can move a hidden
-  # activation across a BF16 rounding boundary
+  # the in-step form interpolates the network tabulated in x1 (4096 points
+  # per band); BF16 inference: FP32-rounding differences of the inputs can
+  # also move a hidden activation across a BF16 rounding boundary
   np.testing.assert_allclose(runs[True][2], runs[False][2], rtol=1e-3)
-  np.testing.assert_allclose(runs[True][0], runs[False][0], rtol=1e-4, atol=1e-6)
+  np.testing.assert_allclose(runs[True][0], runs[False][0], rtol=1e-3, atol=1e-6)
   plan.close()
 
 
