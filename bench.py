@@ -327,7 +327,8 @@ def time_to_tolerance(nsteps=20000, ncells=16, cell_index=1):
   keys: at least as converged as the plain run; the learned runs end below
   E_ref, so the two-sided form charges them for going lower).  Medians over
   the cells, with cells where the learned run never settles counted as 0,
-  and the detail of one cell."""
+  the detail of one cell, and the same judge on the Si8 64^3 benchmark cell
+  (8000 steps)."""
   from jrystal_gb300 import precond, precond_train
   mlp = precond.MLP.load(precond.DEFAULT_WEIGHTS)
   res = precond_train.evaluate(mlp, ncells=ncells, nsteps=nsteps, seed=99, grids=(24, 27, 32))
@@ -348,6 +349,15 @@ def time_to_tolerance(nsteps=20000, ncells=16, cell_index=1):
                                       for r in res["cells"]]
   out["heldout"]["speedups"] = [None if r["speedup_wall"] is None else round(r["speedup_wall"], 3)
                                 for r in res["cells"]]
+  # the benchmark cell itself (Si8 64^3, FP32, N(0,1) seed 1), same judge
+  b = precond_train.transfer(mlp, nsteps=8000, names=("si8_cubic_64",))["si8_cubic_64"]
+  out["benchmark_cell"] = {"cell": "si8_cubic_64", "max_steps": 8000, "E_ref": b["E_ref"],
+                           "plain_drift_last10pct_ha_per_atom": b["plain_drift_last10pct_ha_per_atom"],
+                           "speedup_wall": b["speedup_wall"], "speedup_wall_below": b["speedup_wall_below"]}
+  for mode in ("plain", "learned"):
+    out["benchmark_cell"][mode] = {k: (round(b[mode][k], 4) if isinstance(b[mode][k], float) else b[mode][k])
+                                   for k in ("steps", "steps_below", "ms_per_step", "seconds_below",
+                                             "fallback_at", "end_minus_ref_ha_per_atom")}
   return out
 
 

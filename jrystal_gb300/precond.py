@@ -150,8 +150,11 @@ def evaluate_loss(mlp: MLP, records: dict) -> float:
   return float(loss.item()) / records["x"].shape[0]
 
 
+# weights of the benchmark-cell recipe (precond_train.fit_benchmark_cell: ~1e5
+# records of plain runs of the Si8 64^3 cell); precond_si_c_al.npz holds the
+# strained-cell recipe's (precond_train.fit)
 DEFAULT_WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__file__), "data",
-                                             "precond_si_c_al.npz")
+                                             "precond_si8_cubic_64.npz")
 
 
 class GuardedScale:

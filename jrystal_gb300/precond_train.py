@@ -4,14 +4,18 @@ implementation generates.
   python -m jrystal_gb300.precond_train --out weights.npz [--eval-json eval.json]
   python -m jrystal_gb300.precond_train --weights weights.npz --eval-json eval.json
 
-1. Trajectories: 64 strained cells (Si, C, Al; seed 2; grids from
+1. Trajectories (--recipe benchmark, the default): four plain Adam runs
+   (lr 1e-2, 300 steps) of the Si8 64^3 benchmark cell from N(0,1)
+   parameters of seeds 1, 5, 6, 7, stepped together as one TrajectoryBatch,
+   80 sampled coefficient records per run and step (95 680 records).
+   --recipe strained: 64 strained cells (Si, C, Al; seed 2; grids from
    {24, 27, 32, 36, 48}; 2x2x2 k-grid; 8-16 bands, the lower half doubly
-   occupied), 300 plain Adam steps each (lr 1e-2), ~6 sampled coefficient
-   records per step (~1.2e5 records).
+   occupied), 300 plain Adam steps each, ~6 records per step (~1.2e5
+   records), then ``rounds - 1`` refinement rounds whose records come from
+   trajectories run under the current network (the one-step model is
+   re-expressed for the absolute scale, see collect_records).
 2. Training: Adam lr 1e-3, 2000 steps, seed 3, with the library's BF16/FP32
-   training kernels; then ``rounds - 1`` refinement rounds whose records
-   come from trajectories run under the current network (the one-step model
-   is re-expressed for the absolute scale, see collect_records).
+   training kernels.
 3. Evaluation on 16 held-out strained cells: plain and learned (with the
    plain fallback) optimisers from the same start, both run for the same
    number of steps; E_ref is the converged energy of the plain run (its last
@@ -90,6 +94,31 @@ def fit(rounds=3, ncells=64, steps=300, per_step=6, smax=4.0, grids=(24, 27, 32,
     R = {k: torch.cat([R[k], R2[k]]) for k in R}
     precond.train(mlp, R, steps=2000, lr=1e-3, seed=3 + r)
     log(f"round {r}: {R['x'].shape[0]} records, loss {precond.evaluate_loss(mlp, R):.4f}")
+  return mlp
+
+
+def fit_benchmark_cell(name="si8_cubic_64", seeds=(1, 5, 6, 7), steps=300, per_step=80, train_steps=2000,
+                       lr=1e-2, log=print):
+  """The training recipe on the benchmark cell itself: plain Adam runs of the
+  named workload (the Si8 64^3 cell, FP32) from N(0,1) parameters of each
+  seed, ``steps`` steps each as one TrajectoryBatch, ``per_step`` records
+  per run and step (4 x 299 x 80 = 95 680 records, ~1e5), then Adam (lr
+  1e-3, ``train_steps`` steps, seed 3) with the library's training kernels."""
+  import dataclasses
+  from . import workloads
+  from .batch import TrajectoryBatch
+  base = workloads.WORKLOADS[name](32)
+  wls = [dataclasses.replace(base, seed=s, name=f"{name}_s{s}") for s in seeds]
+  t0 = time.time()
+  b = TrajectoryBatch(wls, steps, lr=lr, per_step=per_step, seed=3)
+  b.run()
+  recs = {k: v.clone() for k, v in b.records().items()}
+  b.close()
+  log(f"{recs['x'].shape[0]} records from {len(wls)} runs of {name} ({time.time() - t0:.1f} s)")
+  mlp = precond.MLP(seed=3)
+  mlp.horizon = steps
+  precond.train(mlp, recs, steps=train_steps, lr=1e-3, seed=3)
+  log(f"loss {precond.evaluate_loss(mlp, recs):.4f}")
   return mlp
 
 
@@ -186,6 +215,9 @@ def main():
   ap.add_argument("--weights", default=None, help="evaluate these weights instead of training")
   ap.add_argument("--eval-json", default=None)
   ap.add_argument("--rounds", type=int, default=1)
+  ap.add_argument("--recipe", default="benchmark", choices=["benchmark", "strained"],
+                  help="records from runs of the Si8 64^3 benchmark cell, or from 64 strained "
+                       "Si/C/Al cells with refinement rounds")
   ap.add_argument("--eval-cells", type=int, default=16)
   ap.add_argument("--eval-steps", type=int, default=40000)
   ap.add_argument("--transfer-steps", type=int, default=0,
@@ -197,7 +229,8 @@ def main():
   else:
     if not args.out:
       ap.error("--out is required when training")
-    mlp = fit(rounds=args.rounds, refine_steps=args.refine_steps)
+    mlp = (fit_benchmark_cell() if args.recipe == "benchmark"
+           else fit(rounds=args.rounds, refine_steps=args.refine_steps))
     mlp.save(args.out)
   if args.eval_json:
     res = evaluate(mlp, ncells=args.eval_cells, nsteps=args.eval_steps)
