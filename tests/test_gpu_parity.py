@@ -46,6 +46,9 @@ CASES = [
   dict(kind="si8", grid=(32, 32, 32), kgrid=(2, 1, 1), nb=4, nocc=2),
   # the band count of the Si64 supercell workload (160 bands, 128 occupied)
   dict(kind="si8", grid=(32, 32, 32), kgrid=(1, 1, 1), nb=160, nocc=128),
+  # more than 32 bands, not a multiple of 4 (scalar loads and stores, a
+  # partial last tile), two k-points (pipelined step)
+  dict(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 2), nb=37, nocc=18),
 ]
 
 
