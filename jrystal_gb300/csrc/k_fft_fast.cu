@@ -15,9 +15,19 @@
 #include <cstdlib>
 
 #include "plan.h"
+#include <type_traits>
 
 namespace jrg {
 namespace fast {
+
+// kinetic table |G+k|^2/2 in the path's precision: the FP32 copy of the plan
+// for the FP32 kernels (the same values as an FP32 cast of the FP64 table,
+// without a conversion per coefficient and band)
+template <typename R> using TK_t = std::conditional_t<sizeof(R) == 4, float, double>;
+template <typename R> const TK_t<R>* tk_table(const jrg_plan* P) {
+  if constexpr (sizeof(R) == 4) return P->d.tkf;
+  else return P->d.tk;
+}
 
 using reg::Split;
 
@@ -378,7 +388,7 @@ __global__ void __launch_bounds__(threads_for<N>(), min_blocks_for<R, N>()) k_li
 template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
     const C_t<R>* __restrict__ planes, const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ gcoef,
-    const double* __restrict__ wband, const double* __restrict__ tk, int nb_per_k, int band0,
+    const double* __restrict__ wband, const TK_t<R>* __restrict__ tk, int nb_per_k, int band0,
     const int* __restrict__ plane_off, const int* __restrict__ sph_yz, const int* __restrict__ row_off,
     const int* __restrict__ rows, const C_t<R>* __restrict__ tw_g, int ng, int nact, int nk,
     double scale) {
@@ -436,7 +446,7 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
   const int kidx = (gb / nb_per_k) % nk;
   const R w = (R)wband[gb];
   const R sc = (R)scale;
-  const double* tkk = tk + (size_t)kidx * ng;
+  const TK_t<R>* tkk = tk + (size_t)kidx * ng;
   const C* cb = coef + (size_t)band * ng;
   C* gout = gcoef + (size_t)band * ng;
   for (int e = plane_off[p] + tid; e < plane_off[p + 1]; e += blockDim.x) {
@@ -458,7 +468,7 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere(
 template <typename R, int N, bool PR>
 __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere_rp(
     const C_t<R>* __restrict__ planes, const C_t<R>* __restrict__ coef, C_t<R>* __restrict__ gcoef,
-    const double* __restrict__ wband, const double* __restrict__ tk, int nb_per_k, int band0,
+    const double* __restrict__ wband, const TK_t<R>* __restrict__ tk, int nb_per_k, int band0,
     const int* __restrict__ plane_off, const int* __restrict__ sph_yz, const int* __restrict__ row_off,
     const int* __restrict__ rows, const C_t<R>* __restrict__ tw_g, int ng, int nact, int nk,
     double scale, int nbands, int bpc) {
@@ -495,7 +505,7 @@ __global__ void __launch_bounds__(threads_for<N>()) k_plane_fwd_sphere_rp(
   for (int band = b_begin; band < b_end; ++band) {
     const int gb = band0 + band;
     const int kidx = (gb / nb_per_k) % nk;
-    const double* tkk = tk + (size_t)kidx * ng;
+    const TK_t<R>* tkk = tk + (size_t)kidx * ng;
     const C* cb = coef + (size_t)band * ng;
     C c0 = czero<C>();
     R t0 = (R)0;
@@ -743,14 +753,14 @@ static int plane_fwd_launch(const jrg_plan* P, const Args& a, const C_t<R>* tw, 
     if ((rc = prep(k_plane_fwd_sphere_rp<R, N, PR>, sm)) <= 0) return rc;
     k_plane_fwd_sphere_rp<R, N, PR><<<dim3(P->nact, (a.nbands + bpc - 1) / bpc), T, sm, st>>>(
         reinterpret_cast<const C*>(a.in), reinterpret_cast<const C*>(a.aux), reinterpret_cast<C*>(a.out),
-        a.w, P->d.tk, P->nb, a.band0, P->d.plane_off, P->d.sph_yz, P->d.row_off, P->d.rows, tw, P->ng,
+        a.w, tk_table<R>(P), P->nb, a.band0, P->d.plane_off, P->d.sph_yz, P->d.row_off, P->d.rows, tw, P->ng,
         P->nact, P->nk, a.wscale, a.nbands, bpc);
     FAST_LAUNCHED("fast::k_plane_fwd_sphere_rp");
   }
   if ((rc = prep(k_plane_fwd_sphere<R, N, PR>, sm)) <= 0) return rc;
   k_plane_fwd_sphere<R, N, PR><<<dim3(P->nact, a.nbands), T, sm, st>>>(
       reinterpret_cast<const C*>(a.in), reinterpret_cast<const C*>(a.aux), reinterpret_cast<C*>(a.out),
-      a.w, P->d.tk, P->nb, a.band0, P->d.plane_off, P->d.sph_yz, P->d.row_off, P->d.rows, tw, P->ng,
+      a.w, tk_table<R>(P), P->nb, a.band0, P->d.plane_off, P->d.sph_yz, P->d.row_off, P->d.rows, tw, P->ng,
       P->nact, P->nk, a.wscale);
   FAST_LAUNCHED("fast::k_plane_fwd_sphere");
 }
