@@ -163,7 +163,13 @@ int jrg_density(const jrg_plan* plan, const void* coeff, const double* occupatio
  *   the call: it is left on the device (reading it would synchronise) for
  *   the caller to act on, e.g. with jrg_reorthonormalise.
  * grad_re/grad_im: [S][K][G][B] d total / d w_re, d w_im (may be NULL for
- * energy only). */
+ * energy only).
+ * num_spin 2 (spin-polarised, LDA only): occupation [2][K][B] holds each
+ * channel's occupations; Hartree and external terms act on the total
+ * density, E_xc = vol/N sum eps_xc(rho_up, rho_dn) (rho_up + rho_dn) with the
+ * polarised LDA of jrg_lda_polarized (jrystal/_src/xc.py:40-64,
+ * energy.py:185-211), and each channel's bands see their own potential
+ * V_H + V_ext + d(eps_xc rho)/d rho_s. */
 int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
                     const double* occupation, double* energies, void* grad_re,
                     void* grad_im, void* workspace, cudaStream_t stream);
@@ -173,7 +179,7 @@ int jrg_energy_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
  * double[S*K*B]), the occupation gradient the reference driver takes with
  * value_and_grad over its occupation parameters
  * (jrystal/calc/calc_ground_state_energy_all_electrons.py:119-147,175-181).
- * num_spin 1. */
+ * num_spin 1 or 2 as jrg_energy_grad. */
 int jrg_energy_grad_bands(const jrg_plan* plan, const void* w_re, const void* w_im,
                           const double* occupation, double* energies, double* band_energies,
                           void* grad_re, void* grad_im, void* workspace, cudaStream_t stream);
@@ -205,8 +211,9 @@ int jrg_band_trace_grad(const jrg_plan* plan, const void* w_re, const void* w_im
  * update element ([2][S][K][G][B] FP32); with mlp_w32/mlp_wb given it is
  * first overwritten with the learned preconditioner's scales
  * (jrg_precond_scale at step fraction t_frac, cap smax) computed inside the
- * step from this step's band kinetic energies.  num_spin 1; more than 32
- * bands only with the default contraction kernels (jrg_tensor_core_paths 0).
+ * step from this step's band kinetic energies.  num_spin 1 or 2 as
+ * jrg_energy_grad; more than 32 bands only with the default contraction
+ * kernels (jrg_tensor_core_paths 0).
  * With a non-zero status word (energies[6]) no update is applied: params, m
  * and v keep their values. */
 typedef struct {
@@ -235,10 +242,13 @@ int jrg_energy_grad_adam(const jrg_plan* plan, void* params, void* m, void* v,
 int jrg_reorthonormalise(const jrg_plan* plan, void* w_re, void* w_im, void* workspace,
                          cudaStream_t stream);
 
-/* Effective potential from a density [S][nx][ny][nz] (S must be 1):
- * out [3][nx][ny][nz] real = Hartree, external, xc parts (split form) with
- * jrystal's conventions: kohn_sham=0 halves Hartree and gives the xc energy
- * density, kohn_sham=1 gives the full Hartree and v_xc. */
+/* Effective potential from a density [S][nx][ny][nz]:
+ * out [2+S][nx][ny][nz] real = Hartree, external, then the xc part per spin
+ * (split form) with jrystal's conventions: kohn_sham=0 halves Hartree and
+ * gives the xc energy density, kohn_sham=1 gives the full Hartree and v_xc.
+ * S = 2 (LDA only): Hartree of the total density; the xc part is vxc_lda's
+ * eps + rho_s d eps / d rho_s per spin (kohn_sham=1) or eps in both grids
+ * (jrystal/_src/potential.py:203-279 broadcasts it over the spin axis). */
 int jrg_potential(const jrg_plan* plan, const void* density, int kohn_sham, void* out,
                   void* workspace, cudaStream_t stream);
 
@@ -248,6 +258,18 @@ int jrg_potential(const jrg_plan* plan, const void* density, int kohn_sham, void
  * (jax_xc lda_x and lda_c_vwn, unpolarised). */
 int jrg_lda(int precision, int64_t n, int xc, int kohn_sham, const void* rho, void* out,
             cudaStream_t stream);
+
+/* Spin-polarised LDA of a [2][n] density (up, down): eps_xc per particle of
+ * the total density ([n], kohn_sham = 0), vxc_lda's per-spin field
+ * eps_xc + rho_s d eps_xc / d rho_s ([2][n], kohn_sham = 1), or the
+ * derivative of the energy density eps_xc (rho_up + rho_dn),
+ * eps_xc + (rho_up + rho_dn) d eps_xc / d rho_s ([2][n], kohn_sham = 2: the
+ * potential of jrg_energy_grad's polarised path).  Exchange by
+ * jrystal's scaling (e_x(2 rho_up) + e_x(2 rho_dn)) / 2, correlation the VWN
+ * spin interpolation of jax_xc's lda_c_vwn "pol" form;
+ * jrystal/_src/xc.py:40-64,109-124. */
+int jrg_lda_polarized(int precision, int64_t n, int xc, int kohn_sham, const void* rho, void* out,
+                      cudaStream_t stream);
 
 /* Batched complex 3-D FFT over the last three axes of [batch][nx][ny][nz].
  * direction -1: forward (unnormalised, jnp.fft.fftn); +1: inverse with the

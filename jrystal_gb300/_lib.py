@@ -101,6 +101,7 @@ _SIGS = {
   "jrg_fft3d_noalloc": ([ct.c_int, ct.POINTER(ct.c_int), ct.c_int, ct.c_int, _vp, _vp, _vp],
                         ct.c_int),
   "jrg_lda": ([ct.c_int, ct.c_int64, ct.c_int, ct.c_int, _vp, _vp, _vp], ct.c_int),
+  "jrg_lda_polarized": ([ct.c_int, ct.c_int64, ct.c_int, ct.c_int, _vp, _vp, _vp], ct.c_int),
   "jrg_adam_update": ([ct.c_int, ct.c_int64, _vp, _vp, _vp, _vp, _vp, ct.c_int,
                        ct.c_double, ct.c_double, ct.c_double, ct.c_double, _vp], ct.c_int),
   "jrg_ewald": ([_vp, ct.c_double, ct.c_double, _vp, _vp, _vp], ct.c_int),

@@ -153,6 +153,48 @@ def _lda_raw(rho: torch.Tensor, xc: str, kohn_sham: bool) -> torch.Tensor:
   return out
 
 
+def lda_pol_raw(rho: torch.Tensor, xc: str, mode: int) -> torch.Tensor:
+  """Spin-polarised LDA of a (2, ...) density on the device (jrg_lda_polarized):
+  mode 0 eps (...), 1 vxc_lda's eps + rho_s d eps/d rho_s (2, ...), 2 the
+  derivative of eps (rho_up + rho_dn), eps + rho d eps/d rho_s (2, ...)."""
+  lib = _lib.load()
+  rho = rho.contiguous()
+  if torch.is_complex(rho) or rho.shape[0] != 2:
+    raise TypeError("a polarised density is real with 2 channels")
+  out = torch.empty(rho.shape[1:] if mode == 0 else rho.shape, dtype=rho.dtype, device=rho.device)
+  st = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+  _lib.check(lib.jrg_lda_polarized(precision_of(rho), rho[0].numel(), xc_flags(xc), int(mode),
+                                   ct.c_void_p(rho.data_ptr()), ct.c_void_p(out.data_ptr()), st),
+             "jrg_lda_polarized")
+  return out
+
+
+class _LdaEpsPol(torch.autograd.Function):
+  """Polarised LDA energy per particle eps(rho_up, rho_dn); d eps / d rho_s =
+  (v_s - eps) / rho with v_s the library's derivative of eps rho."""
+
+  @staticmethod
+  def forward(ctx, rho, xc):
+    eps = lda_pol_raw(rho, xc, 0)
+    ctx.save_for_backward(rho, eps)
+    ctx.xc = xc
+    return eps
+
+  @staticmethod
+  def backward(ctx, g):
+    rho, eps = ctx.saved_tensors
+    v = lda_pol_raw(rho, ctx.xc, 2)
+    tot = rho.sum(0)
+    ok = tot > 1e-15
+    d = torch.where(ok, (v - eps) / torch.where(ok, tot, torch.ones_like(tot)), torch.zeros_like(v))
+    return g * d, None
+
+
+def lda_eps_pol(rho: torch.Tensor, xc: str) -> torch.Tensor:
+  """Differentiable polarised LDA energy per particle of a (2, ...) density."""
+  return _LdaEpsPol.apply(rho, xc)
+
+
 def safe_real(x: torch.Tensor, tol: float = 1e-8) -> torch.Tensor:
   """jrystal/_src/utils.py:25-59."""
   if torch.is_complex(x):

@@ -78,8 +78,9 @@ class Minimizer:
   diagonal preconditioner) or None for the plain update.  A scale_fn with an
   ``in_step(minimizer)`` method (precond.GuardedScale) instead hands the
   network to the device step, which evaluates it between the kinetic and the
-  density phases.  With ``fused`` (the default where supported: one spin
-  channel; more than 32 bands with the default contraction kernels) each step is one jrg_energy_grad_adam call: with
+  density phases.  With ``fused`` (the default where supported: more than
+  32 bands with the default contraction kernels) each step is one
+  jrg_energy_grad_adam call: with
   the two-stream k-point pipeline each half of the k-points takes its Adam
   step as soon as its gradient is done (1.951 vs 1.963 ms per step for the
   two-call path on the 64^3 Si8 cell); ``grads`` is only filled when
@@ -102,7 +103,7 @@ class Minimizer:
     self.total_steps = total_steps
     self.scale_fn = scale_fn
     self.last_scale = None
-    supported = plan.num_spin == 1 and (plan.num_band <= 32 or plan.lib.jrg_tensor_core_paths(-1) == 0)
+    supported = plan.num_band <= 32 or plan.lib.jrg_tensor_core_paths(-1) == 0
     self.fused = fused and supported
     self.keep_grad = keep_grad
     self.recoveries = 0
@@ -255,10 +256,19 @@ def attach_pseudopotential(plan: PlaneWavePlan, pp, kmax: Optional[float] = None
   return plan
 
 
-def _make_plan(su: _Setup, cfg, kpts=None, num_bands=None, kmax=None) -> PlaneWavePlan:
+def _num_spin(cfg) -> int:
+  """1 spin channel (restricted) or 2; the polarised path is LDA only."""
+  if cfg["spin_restricted"]:
+    return 1
+  if "gga" in cfg["xc"]:
+    raise NotImplementedError("spin-polarised PBE is not implemented")
+  return 2
+
+
+def _make_plan(su: _Setup, cfg, kpts=None, num_bands=None, kmax=None, num_spin=1) -> PlaneWavePlan:
   c = su.crystal
   plan = PlaneWavePlan(c.cell_vectors, c.positions, c.charges, su.grid_sizes, su.mask,
-                       su.kpts if kpts is None else kpts, num_bands or su.num_bands, 1,
+                       su.kpts if kpts is None else kpts, num_bands or su.num_bands, num_spin,
                        su.precision, cfg["xc"])
   if su.pseudo is not None:
     attach_pseudopotential(plan, su.pseudo, kmax=kmax)
@@ -296,8 +306,7 @@ def _ground_state(cfg, pseudo: bool) -> GroundStateEnergyOutput:
     return _energy_learnable_occupation(cfg, pseudo)
   if cfg["occupation"] not in ("uniform", "gamma"):
     raise ValueError(f"Invalid method: {cfg['occupation']}")
-  if not cfg["spin_restricted"]:
-    raise NotImplementedError("spin-polarised LDA is not implemented")
+  ns = _num_spin(cfg)
   su = _setup(cfg, pseudo)
   crystal, kpts, mask, nelec = su.crystal, su.kpts, su.mask, su.nelec
   num_bands = su.num_bands
@@ -310,11 +319,12 @@ def _ground_state(cfg, pseudo: bool) -> GroundStateEnergyOutput:
     occ = np.zeros((2, K, num_bands))
     occ[0, 0, :(nelec + crystal.spin) // 2] = 1
     occ[1, 0, :(nelec - crystal.spin) // 2] = 1
-  occ = occ.sum(0, keepdims=True)
+  if ns == 1:
+    occ = occ.sum(0, keepdims=True)
   if "occupation_array" in cfg:
     occ = np.asarray(cfg["occupation_array"], dtype=np.float64)
     num_bands = occ.shape[-1]
-  plan = _make_plan(su, cfg, num_bands=num_bands)
+  plan = _make_plan(su, cfg, num_bands=num_bands, num_spin=ns)
   ew = plan.ewald(cfg["ewald_args"]["ewald_eta"], cfg["ewald_args"]["ewald_cutoff"])
   ng = int(mask.sum())
   gen = torch.Generator(device=plan.device)
@@ -323,7 +333,7 @@ def _ground_state(cfg, pseudo: bool) -> GroundStateEnergyOutput:
     w_re, w_im = cfg["init_params"]
     params = torch.tensor(np.stack([w_re, w_im]), dtype=plan.rdtype, device=plan.device)
   else:
-    params = torch.rand((2, 1, K, ng, num_bands), generator=gen, device=plan.device,
+    params = torch.rand((2, ns, K, ng, num_bands), generator=gen, device=plan.device,
                         dtype=plan.rdtype)
   oa = cfg["optimizer_args"]
   mini = Minimizer(plan, occ, params, lr=oa.get("learning_rate", 1e-2), b1=oa.get("b1", 0.9),
@@ -376,12 +386,12 @@ def _energy_learnable_occupation(cfg, pseudo: bool = False) -> GroundStateEnergy
   parameter sets take Adam steps with the same hyper-parameters."""
   from . import entropy as _entropy
   from . import occupation as _occupation
-  if not cfg["spin_restricted"]:
-    raise NotImplementedError("spin-polarised LDA is not implemented")
+  ns = _num_spin(cfg)
+  restricted = ns == 1
   su = _setup(cfg, pseudo)
   crystal, kpts, mask, nelec, num_bands = su.crystal, su.kpts, su.mask, su.nelec, su.num_bands
   K = kpts.shape[0]
-  plan = _make_plan(su, cfg)
+  plan = _make_plan(su, cfg, num_spin=ns)
   ew = plan.ewald(cfg["ewald_args"]["ewald_eta"], cfg["ewald_args"]["ewald_cutoff"])
   ng = int(mask.sum())
   gen = torch.Generator(device=plan.device)
@@ -390,12 +400,12 @@ def _energy_learnable_occupation(cfg, pseudo: bool = False) -> GroundStateEnergy
     w_re, w_im = cfg["init_params"]
     params = torch.tensor(np.stack([w_re, w_im]), dtype=plan.rdtype, device=plan.device)
   else:
-    params = torch.rand((2, 1, K, ng, num_bands), generator=gen, device=plan.device,
+    params = torch.rand((2, ns, K, ng, num_bands), generator=gen, device=plan.device,
                         dtype=plan.rdtype)
   method = cfg["occupation"]
   spin = int(crystal.spin)
   if method == "idempotent":
-    occ_params = _occupation.idempotent_param_init(gen, num_bands, nelec, K, spin)
+    occ_params = _occupation.idempotent_param_init(gen, num_bands, nelec, K, spin, restricted)
     leaves = [occ_params["param_up"]["w_re"]]
     if occ_params["param_down"] is not occ_params["param_up"]:
       leaves.append(occ_params["param_down"]["w_re"])
@@ -406,7 +416,7 @@ def _energy_learnable_occupation(cfg, pseudo: bool = False) -> GroundStateEnergy
     t.requires_grad_(True)
 
   def occ_of():
-    return _occupation.occupation(occ_params, K, nelec, spin, method, True)
+    return _occupation.occupation(occ_params, K, nelec, spin, method, restricted)
 
   oa = cfg["optimizer_args"]
   lr, b1, b2, eps = (oa.get("learning_rate", 1e-2), oa.get("b1", 0.9), oa.get("b2", 0.999),
@@ -515,6 +525,8 @@ def _band_structure(config: dict, pseudo: bool) -> BandStructureOutput:
   from .pseudopotential.beta import max_gk_radius
   cfg = dict(BAND_DEFAULTS)
   cfg.update(_merge(config))
+  if not cfg["spin_restricted"]:
+    raise NotImplementedError("the band-structure drivers take one spin channel")
   gs = _ground_state(cfg, pseudo)
   su = _setup(cfg, pseudo)
   crystal, mask = su.crystal, su.mask

@@ -31,6 +31,8 @@ template <typename R> int launch_reduce_density(const void*, void*, int, int, lo
 template <typename R> int launch_recip_terms(const void*, const double*, void*, double*, int, long long, double, const ChargeFix&, cudaStream_t);
 template <typename R> int launch_potential(const void*, const void*, double, void*, double*, int, long long, int, double, const double*, const double*, double*, cudaStream_t);
 template <typename R> int launch_xc_field(const void*, void*, long long, int, int, cudaStream_t);
+template <typename R> int launch_potential_pol(const void*, const void*, double, void*, double*, int, long long, int, double, const double*, const double*, double*, cudaStream_t);
+template <typename R> int launch_spin_total(const void*, void*, long long, cudaStream_t);
 template <typename R> int launch_real_part(const void*, void*, long long, double, cudaStream_t);
 template <typename R> int launch_hartree_g(const void*, const double*, void*, long long, double, cudaStream_t);
 template <typename R> int launch_kinetic(const void*, const double*, const double*, double*, double*, int, int, int, int, cudaStream_t);
@@ -61,6 +63,7 @@ template <typename R> int launch_reorthonormalise(void*, void*, double2*, int, i
 int launch_dft_axis_inv_f64(const double2*, double2*, int, int, int, int, const double2*, cudaStream_t);
 template <typename R> int launch_rotate_adam(const void*, const double2*, const void*, const double2*, const AdamArgs&, int, int, int, double, cudaStream_t);
 int launch_lda(int prec, long long n, int xc, int ks, const void* rho, void* out, cudaStream_t st);
+int launch_lda_pol(int prec, long long n, int xc, int ks, const void* rho, void* out, cudaStream_t st);
 
 static thread_local std::string g_err;
 static std::atomic<long long> g_launches{0};
@@ -148,10 +151,12 @@ static void layout_workspace_k(jrg_plan* P, int kc) {
   w.rho_part = take((size_t)w.ngroups * P->ngrid * Rz);
   w.rho_scale = take((size_t)w.ngroups * sizeof(double));
   w.rho_q = take((kQParts + 1) * sizeof(double));
-  w.rho = take((size_t)P->ns * P->ngrid * Rz);
+  // spin-polarised: [up][down][total] (the total is transformed for the
+  // Hartree term); the potential per spin
+  w.rho = take((size_t)(P->ns == 2 ? 3 : 1) * P->ngrid * Rz);
   w.rhog = take((size_t)P->ngrid * C);
   w.fft_scratch = take((size_t)P->ngrid * C);
-  w.vr = take((size_t)P->ngrid * Rz);
+  w.vr = take((size_t)P->ns * P->ngrid * Rz);
   w.gc = take(nbt * P->ng * C);
   w.adj_part = w.gram_part;
   w.epart = take((size_t)w.nepart * sizeof(double));
@@ -766,7 +771,13 @@ static int grid_phase(const jrg_plan* P, const double* occ, double* slots, void*
   double* slot_h = slots + nbt + kRecipBlocks;
   double* slot_x = slots + nbt + 2 * kRecipBlocks;
   int rc;
-  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+  const void* rho_t = rho;   // the density the Hartree term transforms
+  if (P->ns == 2) {
+    void* tot = (char*)rho + 2 * (size_t)P->ngrid * rsize(P->prec);
+    if ((rc = launch_spin_total<R>(rho, tot, P->ngrid, st))) return rc;
+    rho_t = tot;
+  }
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho_t, scratch, rhog, 1.0, st))) return rc;
   const bool gga = (P->xc & kXcGga) != 0;
   if (gga && (rc = gga_gradients<R>(P, rhog, ws, st))) return rc;
   // Hartree energy and V_H(G) (in place)
@@ -777,8 +788,32 @@ static int grid_phase(const jrg_plan* P, const double* occ, double* slots, void*
   if (gga)
     return gga_potential<R>(P, rho, rhog, 1.0, wsp(ws, w.vr), slot_x, 0, ws, st, cf.scale, P->d.vext_r,
                             slot_e);
+  if (P->ns == 2)
+    return launch_potential_pol<R>(rho, rhog, 1.0, wsp(ws, w.vr), slot_x, kXcBlocks, P->ngrid, P->xc,
+                                   P->vol / N, cf.scale, P->d.vext_r, slot_e, st);
   return launch_potential<R>(rho, rhog, 1.0, wsp(ws, w.vr), slot_x, kXcBlocks, P->ngrid, P->xc, P->vol / N,
                              cf.scale, P->d.vext_r, slot_e, st);
+}
+
+// Adjoint line pass over the (s,k) blocks k0 .. k0+n-1 held in the plane
+// buffers t_in / t_out (block k0 first), with the potential of each block's
+// spin (vr: [ns][grid]); one launch per spin.
+template <typename R>
+static int apply_v_blocks(const jrg_plan* P, void* t_in, void* t_out, const void* vr, int k0, int n,
+                          cudaStream_t st) {
+  using C = C_t<R>;
+  const size_t per_block = (size_t)P->nb * P->nact * P->ny * P->nz;   // plane elements of one block
+  int rc;
+  for (int b = k0; b < k0 + n;) {
+    const int s = b / P->nk;
+    const int e = std::min(k0 + n, (s + 1) * P->nk);
+    const size_t off = (size_t)(b - k0) * per_block;
+    if ((rc = launch_line_apply_v<R>(P, (C*)t_in + off, (C*)t_out + off,
+                                     (const R*)vr + (size_t)s * P->ngrid, (e - b) * P->nb, P->nb, st)))
+      return rc;
+    b = e;
+  }
+  return JRG_OK;
 }
 
 template <typename R>
@@ -835,8 +870,7 @@ static int energy_grad_impl(const jrg_plan* P, const void* w_re, const void* w_i
     }
     {
       PHASE(PH_LINE_APPLY_V);
-      if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), wsp(ws, w.vr), n * P->nb, P->nb, st)))
-        return rc;
+      if ((rc = apply_v_blocks<R>(P, wsp(ws, w.t), wsp(ws, w.u), wsp(ws, w.vr), k0, n, st))) return rc;
     }
     {
       // with band energies requested, g_C = H c unweighted; the occupations
@@ -1002,7 +1036,7 @@ static int phase_adjoint_range(const jrg_plan* P, const double* occ, void* g_re,
   C* c = (C*)wsp(ws, w.c) + co;
   C* gc = (C*)wsp(ws, w.gc) + co;
   int rc;
-  if ((rc = launch_line_apply_v<R>(P, t, t, wsp(ws, w.vr), n * P->nb, P->nb, st))) return rc;
+  if ((rc = apply_v_blocks<R>(P, t, t, wsp(ws, w.vr), k0, n, st))) return rc;
   if ((rc = launch_plane_fwd_sphere<R>(P, t, c, gc, occ, k0 * P->nb, n * P->nb, 1.0 / N, st))) return rc;
   if ((rc = nl_adjoint<R>(P, ws, k0, n, st))) return rc;
   if ((rc = launch_gram<R>(kBand, c, nullptr, kBand, gc, nullptr,
@@ -1158,7 +1192,13 @@ static int potential_entry(const jrg_plan* P, const void* rho, int ks, void* out
   const C* tw = (const C*)P->d.tw;
   R* o = (R*)out;
   int rc;
-  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
+  const void* rho_t = rho;   // the density of the Hartree term
+  if (P->ns == 2) {
+    R* tot = (R*)wsp(ws, w.rho) + 2 * (size_t)P->ngrid;
+    if ((rc = launch_spin_total<R>(rho, tot, P->ngrid, st))) return rc;
+    rho_t = tot;
+  }
+  if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho_t, scratch, rhog, 1.0, st))) return rc;
   if ((rc = launch_hartree_g<R>(rhog, P->d.ginv, rhog, P->ngrid, ks ? 1.0 : 0.5, st))) return rc;
   if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, +1, false, rhog, scratch, rhog, 1.0 / N, st))) return rc;
   if ((rc = launch_real_part<R>(rhog, o, P->ngrid, 1.0, st))) return rc;
@@ -1168,6 +1208,14 @@ static int potential_entry(const jrg_plan* P, const void* rho, int ks, void* out
     if ((rc = launch_fft3d_dense<R>(P->ax, tw, 1, -1, true, rho, scratch, rhog, 1.0, st))) return rc;
     if ((rc = gga_gradients<R>(P, rhog, ws, st))) return rc;
     return gga_potential<R>(P, rho, nullptr, 0.0, o + 2 * P->ngrid, nullptr, ks ? 0 : 1, ws, st);
+  }
+  if (P->ns == 2) {
+    // xc part per spin: vxc_lda's field (Kohn-Sham), or eps in both grids
+    if ((rc = launch_lda_pol(P->prec, P->ngrid, P->xc, ks, rho, o + 2 * P->ngrid, st))) return rc;
+    if (!ks)
+      JRG_CUDA(cudaMemcpyAsync(o + 3 * P->ngrid, o + 2 * P->ngrid, sizeof(R) * (size_t)P->ngrid,
+                               cudaMemcpyDeviceToDevice, st));
+    return JRG_OK;
   }
   return launch_xc_field<R>(rho, o + 2 * P->ngrid, P->ngrid, P->xc, ks, st);
 }
@@ -1202,7 +1250,8 @@ int jrg_energy_grad(const jrg_plan* P, const void* w_re, const void* w_im, const
                     double* energies, void* g_re, void* g_im, void* ws, cudaStream_t st) {
   if (!P || !w_re || !w_im || !occ || !energies || !ws)
     return fail(JRG_ERR_INVALID, "jrg_energy_grad: null argument");
-  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad: spin-polarised LDA is not implemented");
+  if (P->ns == 2 && (P->xc & kXcGga))
+    return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad: spin-polarised PBE is not implemented");
   return P->prec == 64 ? energy_grad<double>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st)
                        : energy_grad<float>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st);
 }
@@ -1212,7 +1261,8 @@ int jrg_energy_grad_bands(const jrg_plan* P, const void* w_re, const void* w_im,
                           cudaStream_t st) {
   if (!P || !w_re || !w_im || !occ || !energies || !band_energies || !g_re || !g_im || !ws)
     return fail(JRG_ERR_INVALID, "jrg_energy_grad_bands: null argument");
-  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_bands: spin-polarised LDA is not implemented");
+  if (P->ns == 2 && (P->xc & kXcGga))
+    return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_bands: spin-polarised PBE is not implemented");
   int rc = P->prec == 64
                ? energy_grad_impl<double>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st, nullptr, band_energies)
                : energy_grad_impl<float>(P, w_re, w_im, occ, energies, g_re, g_im, ws, st, nullptr, band_energies);
@@ -1245,7 +1295,8 @@ int jrg_energy_grad_adam(const jrg_plan* P, void* params, void* m, void* v, cons
     return fail(JRG_ERR_INVALID, "jrg_energy_grad_adam: bad argument");
   if (opt->mlp_w32 && (!opt->mlp_wb || !opt->scale))
     return fail(JRG_ERR_INVALID, "jrg_energy_grad_adam: the learned scale needs mlp_wb and a scale buffer");
-  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_adam: spin-polarised LDA is not implemented");
+  if (P->ns == 2 && (P->xc & kXcGga))
+    return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_adam: spin-polarised PBE is not implemented");
   if (P->nb > 32 && jrg_tensor_core_paths(-1) != 0)
     return fail(JRG_ERR_UNSUPPORTED, "jrg_energy_grad_adam: num_band > 32 needs contraction mode 0");
   const size_t n = (size_t)P->ns * P->nk * P->ng * P->nb;
@@ -1288,7 +1339,8 @@ int jrg_reorthonormalise(const jrg_plan* P, void* w_re, void* w_im, void* ws, cu
 
 int jrg_potential(const jrg_plan* P, const void* rho, int ks, void* out, void* ws, cudaStream_t st) {
   if (!P || !rho || !out || !ws) return fail(JRG_ERR_INVALID, "jrg_potential: null argument");
-  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_potential: spin-polarised LDA is not implemented");
+  if (P->ns == 2 && (P->xc & kXcGga))
+    return fail(JRG_ERR_UNSUPPORTED, "jrg_potential: spin-polarised PBE is not implemented");
   return P->prec == 64 ? potential_entry<double>(P, rho, ks, out, ws, st)
                        : potential_entry<float>(P, rho, ks, out, ws, st);
 }
@@ -1365,6 +1417,13 @@ int jrg_lda(int prec, int64_t n, int xc, int kohn_sham, const void* rho, void* o
   if (!rho || !out || n < 0 || (prec != 32 && prec != 64) || (xc & ~3) || !xc)
     return fail(JRG_ERR_INVALID, "jrg_lda: bad argument");
   return launch_lda(prec, n, xc, kohn_sham ? 1 : 0, rho, out, st);
+}
+
+int jrg_lda_polarized(int prec, int64_t n, int xc, int kohn_sham, const void* rho, void* out, cudaStream_t st) {
+  if (!rho || !out || n < 0 || (prec != 32 && prec != 64) || (xc & ~3) || !xc)
+    return fail(JRG_ERR_INVALID, "jrg_lda_polarized: bad argument");
+  if (kohn_sham < 0 || kohn_sham > 2) return fail(JRG_ERR_INVALID, "jrg_lda_polarized: kohn_sham must be 0, 1 or 2");
+  return launch_lda_pol(prec, n, xc, kohn_sham, rho, out, st);
 }
 
 int jrg_adam_update(int prec, int64_t n, void* param, const void* grad, void* m, void* v,

@@ -186,6 +186,159 @@ template <typename R> __device__ __forceinline__ void lda_eps_v_t(R rho, int xc,
 }
 
 // ------------------------------------------------------------------------
+// Spin-polarised LDA (jrystal/_src/xc.py:40-64, polarised branches).
+// Exchange by jrystal's scaling: eps_x = (e_x(2 rho_up) + e_x(2 rho_dn)) / 2
+// per particle of the total density.  Correlation: the VWN (1980)
+// interpolation of jax_xc's lda_c_vwn "pol" form,
+//   eps_c = eps_P + alpha f(z) (1 - z^4) / f''(0) + (eps_F - eps_P) f(z) z^4,
+// z = (rho_up - rho_dn) / rho, f(z) = ((1+z)^(4/3) + (1-z)^(4/3) - 2) /
+// (2^(4/3) - 2), with the paramagnetic, ferromagnetic and spin-stiffness
+// fits of the VWN5 parameterisation.  lda_pol gives eps and d eps / d rho_s;
+// the energy path's potential is eps + rho d eps / d rho_s (the derivative
+// of eps rho), the Kohn-Sham field of vxc_lda eps + rho_s d eps / d rho_s.
+// T is the arithmetic type of the correlation (float on the FP32 path: it is
+// about 1% of E_xc); exchange takes rho^(1/3) in FP64 on both paths.
+// ------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void vwn_fit(T x, T A, T b, T c, T x0, T q, T* f, T* df) {
+  const T xx0 = x0 * x0 + b * x0 + c;
+  const T xx = x * x + b * x + c;
+  const T at = atan(q / (T(2) * x + b));
+  *f = A * (log(x * x / xx) + T(2) * b / q * at -
+            b * x0 / xx0 * (log((x - x0) * (x - x0) / xx) + T(2) * (b + T(2) * x0) / q * at));
+  const T den = (T(2) * x + b) * (T(2) * x + b) + q * q;
+  *df = A * (T(2) / x - (T(2) * x + b) / xx - T(4) * b / den -
+             b * x0 / xx0 * (T(2) / (x - x0) - (T(2) * x + b) / xx - T(4) * (b + T(2) * x0) / den));
+}
+
+// rho^(1/3) to FP64 accuracy: cbrtf plus one Newton step on the FP32 path
+template <typename R> __device__ __forceinline__ double cbrt_t(R r) {
+  if constexpr (sizeof(R) == 4) {
+    double y = (double)cbrtf(r);
+    return y - (y * y * y - (double)r) / (3.0 * y * y);
+  } else {
+    return cbrt((double)r);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void lda_pol(R ru, R rd, int xc, double* eps, double* du, double* dd) {
+  using T = R;
+  double e = 0.0, a = 0.0, b = 0.0;
+  if (xc & JRG_XC_LDA_X) {
+    constexpr double cx = 0.7385587663820224;   // (3/4) (3/pi)^(1/3)
+    const R r2[2] = {R(2) * ru, R(2) * rd};
+    double d[2] = {0.0, 0.0};
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+      if (r2[s] > R(1e-15)) {
+        const double ex = -cx * cbrt_t<R>(r2[s]);   // e_x(2 rho_s)
+        e += 0.5 * ex;
+        d[s] = ex / (3.0 * (double)r2[s]);         // e_x'(2 rho_s)
+      }
+    a += d[0];
+    b += d[1];
+  }
+  const R rt = ru + rd;
+  if ((xc & JRG_XC_LDA_C_VWN) && rt > R(1e-15)) {
+    constexpr double kPi = 3.14159265358979323846;
+    T z = (ru - rd) / rt;
+    z = z > T(1) ? T(1) : (z < T(-1) ? T(-1) : z);
+    const T x = sqrt(T(0.6203504908994001 / cbrt_t<R>(rt)));   // sqrt(rs), rs = (3/(4 pi rho))^(1/3)
+    T ep, dep, ef, def, al, dal;
+    vwn_fit<T>(x, T(0.0310907), T(3.72744), T(12.9352), T(-0.10498), T(6.15199081975907951), &ep, &dep);
+    vwn_fit<T>(x, T(0.01554535), T(7.06042), T(18.0578), T(-0.32500), T(4.730926909560114), &ef, &def);
+    vwn_fit<T>(x, T(-1.0 / (6.0 * kPi * kPi)), T(1.13107), T(13.0045), T(-0.0047584), T(7.123108917818118),
+               &al, &dal);
+    const T norm = T(0.5198420997897464);        // 2^(4/3) - 2
+    const T fpp = T(1.7099209341613653);         // f''(0) = 4 / (9 (2^(1/3) - 1))
+    const T cp = cbrt(T(1) + z), cm = cbrt(T(1) - z);
+    const T fz = ((T(1) + z) * cp + (T(1) - z) * cm - T(2)) / norm;
+    const T dfz = T(4) / T(3) * (cp - cm) / norm;
+    const T z3 = z * z * z, z4 = z3 * z;
+    const T ec = ep + al * fz * (T(1) - z4) / fpp + (ef - ep) * fz * z4;
+    const T dx = dep + dal * fz * (T(1) - z4) / fpp + (def - dep) * fz * z4;
+    const T dz = al / fpp * (dfz * (T(1) - z4) - T(4) * z3 * fz) + (ef - ep) * (dfz * z4 + T(4) * z3 * fz);
+    // rho d eps / d rho_s = -(x/6) d eps/dx + (+-1 - z) d eps/dz
+    const T t = -x / T(6) * dx;
+    e += (double)ec;
+    a += (double)(t + (T(1) - z) * dz) / (double)rt;
+    b += (double)(t - (T(1) + z) * dz) / (double)rt;
+  }
+  *eps = e;
+  *du = a;
+  *dd = b;
+}
+
+// polarised form of k_potential: rho and vr are [2][ngrid]; the Hartree and
+// external parts act on the total density, V_s = V_H + V_ext + eps + rho
+// d eps / d rho_s; E_xc = vol/N sum eps rho, E_ext = vol/N sum V_ext rho
+template <typename R>
+__global__ void __launch_bounds__(256) k_potential_pol(const R* __restrict__ rho,
+                                                       const C_t<R>* __restrict__ vri, double vscale,
+                                                       R* __restrict__ vr, double* __restrict__ slot_x,
+                                                       long long ngrid, int xc, double pref,
+                                                       const double* __restrict__ qscale,
+                                                       const double* __restrict__ vext_r,
+                                                       double* __restrict__ slot_e) {
+  __shared__ double red[32];
+  const double s = qscale ? *qscale : 1.0;
+  double ex = 0.0, ee = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double ru = s * (double)rho[i], rd = s * (double)rho[ngrid + i];
+    const double rt = ru + rd;
+    double eps, du, dd;
+    lda_pol<R>((R)ru, (R)rd, xc, &eps, &du, &dd);
+    ex += eps * rt;
+    double ve = 0.0;
+    if (vext_r) {
+      ve = vext_r[i];
+      ee += ve * rt;
+    }
+    const double base = (double)vri[i].x * vscale + eps + ve;
+    vr[i] = (R)(base + rt * du);
+    vr[ngrid + i] = (R)(base + rt * dd);
+  }
+  ex = block_sum(ex, red);
+  if (threadIdx.x == 0) slot_x[blockIdx.x] = ex * pref;
+  if (slot_e) {
+    ee = block_sum(ee, red);
+    if (threadIdx.x == 0) slot_e[blockIdx.x] = ee * pref;
+  }
+}
+
+// polarised xc field of a [2][ngrid] density: eps (kohn_sham = 0, one grid),
+// vxc_lda's eps + rho_s d eps / d rho_s per spin (kohn_sham = 1, two grids)
+// or the derivative of eps rho, eps + rho d eps / d rho_s (kohn_sham = 2)
+template <typename R>
+__global__ void k_xc_field_pol(const R* __restrict__ rho, R* __restrict__ out, long long ngrid, int xc,
+                               int kohn_sham) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
+       i += (long long)gridDim.x * blockDim.x) {
+    const R ru = rho[i], rd = rho[ngrid + i];
+    double eps, du, dd;
+    lda_pol<R>(ru, rd, xc, &eps, &du, &dd);
+    if (kohn_sham) {
+      const double wu = kohn_sham == 2 ? (double)ru + (double)rd : (double)ru;
+      const double wd = kohn_sham == 2 ? (double)ru + (double)rd : (double)rd;
+      out[i] = (R)(eps + wu * du);
+      out[ngrid + i] = (R)(eps + wd * dd);
+    } else {
+      out[i] = (R)eps;
+    }
+  }
+}
+
+// total density of a [2][ngrid] spin density
+template <typename R>
+__global__ void k_spin_total(const R* __restrict__ rho, R* __restrict__ out, long long ngrid) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = (R)((double)rho[i] + (double)rho[ngrid + i]);
+}
+
+// ------------------------------------------------------------------------
 // PBE (Perdew, Burke & Ernzerhof 1996), unpolarised, libxc parameters:
 // f(rho, sigma) = rho (eps_x + eps_c) with exact partials f_rho, f_sigma from
 // forward-mode dual numbers (value and the two partials carried together).
@@ -772,6 +925,34 @@ int launch_potential(const void* rho, const void* vri, double vscale, void* vr, 
 }
 
 template <typename R>
+int launch_potential_pol(const void* rho, const void* vri, double vscale, void* vr, double* slot_x,
+                         int nblocks, long long ngrid, int xc, double pref, const double* qscale,
+                         const double* vext_r, double* slot_e, cudaStream_t st) {
+  k_potential_pol<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const R*>(rho),
+                                              reinterpret_cast<const C_t<R>*>(vri), vscale,
+                                              reinterpret_cast<R*>(vr), slot_x, ngrid, xc, pref, qscale,
+                                              vext_r, slot_e);
+  JRG_LAUNCH_CHECK("k_potential_pol");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_xc_field_pol(const void* rho, void* out, long long ngrid, int xc, int ks, cudaStream_t st) {
+  k_xc_field_pol<R><<<grid_for(ngrid), 256, 0, st>>>(reinterpret_cast<const R*>(rho),
+                                                     reinterpret_cast<R*>(out), ngrid, xc, ks);
+  JRG_LAUNCH_CHECK("k_xc_field_pol");
+  return JRG_OK;
+}
+
+template <typename R>
+int launch_spin_total(const void* rho, void* out, long long ngrid, cudaStream_t st) {
+  k_spin_total<R><<<grid_for(ngrid), 256, 0, st>>>(reinterpret_cast<const R*>(rho),
+                                                   reinterpret_cast<R*>(out), ngrid);
+  JRG_LAUNCH_CHECK("k_spin_total");
+  return JRG_OK;
+}
+
+template <typename R>
 int launch_xc_field(const void* rho, void* out, long long ngrid, int xc, int ks, cudaStream_t st) {
   k_xc_field<R><<<grid_for(ngrid), 256, 0, st>>>(reinterpret_cast<const R*>(rho),
                                                  reinterpret_cast<R*>(out), ngrid, xc, ks);
@@ -910,6 +1091,11 @@ int launch_lda(int prec, long long n, int xc, int ks, const void* rho, void* out
   return launch_xc_field<float>(rho, out, n, xc, ks, st);
 }
 
+int launch_lda_pol(int prec, long long n, int xc, int ks, const void* rho, void* out, cudaStream_t st) {
+  if (prec == 64) return launch_xc_field_pol<double>(rho, out, n, xc, ks, st);
+  return launch_xc_field_pol<float>(rho, out, n, xc, ks, st);
+}
+
 int launch_twiddles(int n, int prec, void* out, cudaStream_t st) {
   if (prec == 64) k_twiddles<double><<<1, 128, 0, st>>>(n, reinterpret_cast<double2*>(out));
   else k_twiddles<float><<<1, 128, 0, st>>>(n, reinterpret_cast<float2*>(out));
@@ -926,6 +1112,10 @@ int launch_twiddles(int n, int prec, void* out, cudaStream_t st) {
                                    long long, int, double, const double*, const double*, double*, \
                                    cudaStream_t);                                               \
   template int launch_xc_field<R>(const void*, void*, long long, int, int, cudaStream_t);         \
+  template int launch_potential_pol<R>(const void*, const void*, double, void*, double*, int,     \
+                                       long long, int, double, const double*, const double*,     \
+                                       double*, cudaStream_t);                                  \
+  template int launch_spin_total<R>(const void*, void*, long long, cudaStream_t);                 \
   template int launch_real_part<R>(const void*, void*, long long, double, cudaStream_t);          \
   template int launch_hartree_g<R>(const void*, const double*, void*, long long, double,          \
                                    cudaStream_t);                                               \

@@ -348,13 +348,14 @@ class PlaneWavePlan:
     return out
 
   def potential(self, density: torch.Tensor, kohn_sham: bool = False) -> torch.Tensor:
-    """(3, nx, ny, nz): Hartree, external and xc parts (real)."""
+    """(2 + S, nx, ny, nz): Hartree, external, then the xc part of each of
+    the plan's S spin channels (real)."""
     rho = density.to(device=self.device, dtype=self.rdtype).contiguous()
     if rho.dim() == 3:
       rho = rho[None]
-    if tuple(rho.shape) != (1,) + self.grid:
-      raise ValueError(f"density shape {tuple(rho.shape)} not supported")
-    out = torch.empty((3,) + self.grid, dtype=self.rdtype, device=self.device)
+    if tuple(rho.shape) != (self.num_spin,) + self.grid:
+      raise ValueError(f"density shape {tuple(rho.shape)} != {(self.num_spin,) + self.grid}")
+    out = torch.empty((2 + self.num_spin,) + self.grid, dtype=self.rdtype, device=self.device)
     st = self.lib.jrg_potential(self._h, _ptr(rho), int(bool(kohn_sham)), _ptr(out),
                                 _ptr(self.workspace), _stream())
     _lib.check(st, "jrg_potential")

@@ -488,6 +488,102 @@ def gga_energy_potential(rho, g_vector_grid, vol, xc_type):
 
 _XC = {"lda_x": lda_x, "lda_c_vwn": lda_c_vwn}
 
+# --------------------------------------------------------------------------
+# spin-polarised LDA (jrystal/_src/xc.py:40-64, polarised branches).
+# Exchange: jrystal applies the unpolarised functional to 2 rho_s and takes
+# eps_x = (e_x(2 rho_up) + e_x(2 rho_dn)) / 2 per particle of the TOTAL
+# density (xc.py:57-60; xc_energy multiplies by rho_up + rho_dn,
+# energy.py:205-211).  Correlation: jax_xc's lda_c_vwn "pol" form, the VWN
+# (1980) interpolation between the paramagnetic (P) and ferromagnetic (F)
+# fits with the spin-stiffness fit alpha:
+#   eps_c = eps_P + alpha f(z) (1 - z^4) / f''(0) + (eps_F - eps_P) f(z) z^4,
+#   f(z) = ((1 + z)^(4/3) + (1 - z)^(4/3) - 2) / (2^(4/3) - 2),
+#   f''(0) = 4 / (9 (2^(1/3) - 1)),
+# each fit A (ln(x^2/X) + 2b/Q atan(Q/(2x+b)) - b x0/X(x0) (ln((x-x0)^2/X)
+# + 2(b+2x0)/Q atan(Q/(2x+b)))), x = sqrt(rs), with the published VWN5
+# parameters (P above; F: 0.01554535, 7.06042, 18.0578, -0.32500; alpha:
+# -1/(6 pi^2), 1.13107, 13.0045, -0.0047584).  Parity unpinned, as the
+# unpolarised forms.  Each function returns eps and d eps / d rho_s.
+# --------------------------------------------------------------------------
+VWN_PARA = (VWN_A, VWN_B, VWN_C, VWN_X0)
+VWN_FERRO = (0.01554535, 7.06042, 18.0578, -0.32500)
+VWN_STIFF = (-1.0 / (6.0 * np.pi**2), 1.13107, 13.0045, -0.0047584)
+VWN_FPP = 4.0 / (9.0 * (2.0**(1.0 / 3.0) - 1.0))
+
+
+def _vwn_fit(x, a, b, c, x0):
+  """One VWN fit F(x) and dF/dx, x = sqrt(rs)."""
+  q = math.sqrt(4 * c - b * b)
+  xx0 = x0 * x0 + b * x0 + c
+  xx = x * x + b * x + c
+  at = np.arctan(q / (2 * x + b))
+  f = a * (np.log(x * x / xx) + 2 * b / q * at - b * x0 / xx0 *
+           (np.log((x - x0)**2 / xx) + 2 * (b + 2 * x0) / q * at))
+  den = (2 * x + b)**2 + q * q
+  df = a * (2 / x - (2 * x + b) / xx - 4 * b / den - b * x0 / xx0 *
+            (2 / (x - x0) - (2 * x + b) / xx - 4 * (b + 2 * x0) / den))
+  return f, df
+
+
+def lda_x_pol(rho_up, rho_dn):
+  """Polarised Slater exchange by jrystal's scaling (xc.py:57-60)."""
+  eps = np.zeros(np.shape(rho_up))
+  ds = []
+  for r in (np.asarray(rho_up, np.float64), np.asarray(rho_dn, np.float64)):
+    e, _ = lda_x(2.0 * r)
+    eps = eps + 0.5 * e
+    ok = 2.0 * r > DENS_THRESHOLD
+    # d/d rho_s of e_x(2 rho_s)/2 = e_x'(2 rho_s) = e_x(2 rho_s) / (3 * 2 rho_s)
+    ds.append(np.where(ok, e / (6.0 * np.where(ok, r, 1.0)), 0.0))
+  return eps, ds[0], ds[1]
+
+
+def lda_c_vwn_pol(rho_up, rho_dn):
+  """VWN5 correlation, spin-interpolated (jax_xc lda_c_vwn pol)."""
+  up = np.asarray(rho_up, np.float64)
+  dn = np.asarray(rho_dn, np.float64)
+  rho = up + dn
+  ok = rho > DENS_THRESHOLD
+  r = np.where(ok, rho, 1.0)
+  z = np.clip((up - dn) / r, -1.0, 1.0)
+  x = np.sqrt(np.cbrt(3.0 / (4.0 * np.pi * r)))
+  ep, dep = _vwn_fit(x, *VWN_PARA)
+  ef, def_ = _vwn_fit(x, *VWN_FERRO)
+  al, dal = _vwn_fit(x, *VWN_STIFF)
+  norm = 2.0**(4.0 / 3.0) - 2.0
+  cp, cm = np.cbrt(1.0 + z), np.cbrt(1.0 - z)
+  fz = ((1.0 + z) * cp + (1.0 - z) * cm - 2.0) / norm
+  dfz = 4.0 / 3.0 * (cp - cm) / norm
+  z3 = z**3
+  z4 = z3 * z
+  eps = ep + al * fz * (1.0 - z4) / VWN_FPP + (ef - ep) * fz * z4
+  deps_dx = dep + dal * fz * (1.0 - z4) / VWN_FPP + (def_ - dep) * fz * z4
+  deps_dz = (al / VWN_FPP * (dfz * (1.0 - z4) - 4.0 * z3 * fz) +
+             (ef - ep) * (dfz * z4 + 4.0 * z3 * fz))
+  # rho d/d rho_s = -(x/6) d/dx + (+-1 - z) d/dz   (rs ~ rho^(-1/3), z = (up - dn)/rho)
+  t = -x / 6.0 * deps_dx
+  d_up = (t + (1.0 - z) * deps_dz) / r
+  d_dn = (t - (1.0 + z) * deps_dz) / r
+  return (np.where(ok, eps, 0.0), np.where(ok, d_up, 0.0), np.where(ok, d_dn, 0.0))
+
+
+_XC_POL = {"lda_x": lda_x_pol, "lda_c_vwn": lda_c_vwn_pol}
+
+
+def xc_eps_pol(rho, xc_type="lda_x"):
+  """Polarised sum over the '+'-separated parts: eps (x,y,z) and
+  d eps / d rho_s (2,x,y,z) of a (2,x,y,z) density."""
+  eps = np.zeros(rho.shape[1:], dtype=np.float64)
+  d = np.zeros(rho.shape, dtype=np.float64)
+  for name in xc_type.split("+"):
+    if name not in _XC_POL:
+      raise NotImplementedError(f"polarised xc functional {name!r} is not restated")
+    e, du, dd = _XC_POL[name](rho[0], rho[1])
+    eps += e
+    d[0] += du
+    d[1] += dd
+  return eps, d
+
 
 def xc_eps_v(rho, xc_type="lda_x"):
   """Sum over the '+'-separated parts (jrystal/_src/xc.py:242-253)."""
@@ -503,9 +599,13 @@ def xc_eps_v(rho, xc_type="lda_x"):
 
 
 def xc_density(density_grid, kohn_sham=False, xc_type="lda_x"):
-  """jrystal/_src/xc.py:222-253 (LDA branch, unpolarised)."""
+  """jrystal/_src/xc.py:222-253 (LDA branch).  Polarised, the Kohn-Sham
+  form is vxc_lda's (xc.py:109-124): eps + rho_s d eps / d rho_s per spin."""
+  if density_grid.shape[0] == 2:
+    eps, d = xc_eps_pol(density_grid, xc_type)
+    return eps[None] + d * density_grid if kohn_sham else eps
   if density_grid.shape[0] != 1:
-    raise NotImplementedError("polarised xc is not restated")
+    raise ValueError("density_grid must have 1 or 2 spin channels")
   eps, v = xc_eps_v(density_grid[0], xc_type)
   return v[None] if kohn_sham else eps
 
@@ -843,6 +943,8 @@ def energy_terms(w_re, w_im, sysm: System, with_grad=True):
   e_nl = energy_nonlocal(dense, sysm.proj, vol, occ) if sysm.proj is not None else 0.0
   e_har = hartree_energy(rho_g, gvec, vol, False)
   if is_gga(sysm.xc):
+    if rho.shape[0] != 1:
+      raise NotImplementedError("polarised GGA is not restated")
     e_xc, v_xc_gga, _ = gga_energy_potential(rho[0], gvec, vol, sysm.xc)
   else:
     e_xc = xc_energy(rho, vol, sysm.xc, False)
@@ -851,11 +953,17 @@ def energy_terms(w_re, w_im, sysm: System, with_grad=True):
   terms["total"] = e_kin + e_ext + e_nl + e_har + e_xc
   if not with_grad:
     return terms
-  # dE/d rho(r) = (vol/N) V(r)
+  # dE/d rho_s(r) = (vol/N) V_s(r)
   v_g = hartree_reciprocal(rho_g, gvec, kohn_sham=True) + v_ext
-  v_xc = v_xc_gga if is_gga(sysm.xc) else xc_eps_v(rho[0], sysm.xc)[1]
-  v_r = np.real(_ifftn(v_g)) + v_xc
-  hpsi = _fftn(v_r[None, None, None] * wave)
+  if rho.shape[0] == 2:
+    # d (eps rho_tot) / d rho_s = eps + rho_tot d eps / d rho_s
+    eps, d = xc_eps_pol(rho, sysm.xc)
+    v_xc = eps[None] + rho.sum(0)[None] * d
+  else:
+    v_xc = v_xc_gga if is_gga(sysm.xc) else xc_eps_v(rho[0], sysm.xc)[1]
+  v_r = np.real(_ifftn(v_g)) + v_xc                # (x,y,z), or (2,x,y,z) polarised
+  v_s = v_r if v_r.ndim == 4 else v_r[None]
+  hpsi = _fftn(v_s[:, None, None] * wave)
   hpsi = hpsi[..., mask] * (np.sqrt(vol) / n)     # (s,k,b,g)
   tk = kinetic_operator(gvec, sysm.kpts)[:, mask]  # (k,g)
   g_c = occ[..., None] * (tk[None, :, None, :] * np.swapaxes(c, -1, -2) + hpsi)

@@ -1,0 +1,232 @@
+"""Spin-polarised (num_spin 2) LDA on the CUDA path against the FP64 oracle
+(jrystal/_src/xc.py:40-64 polarised branches, energy.py:185-211,
+potential.py:24-77 spin-summed Hartree): energies and gradients through the
+two-stream pipeline, the single-stream path and the bounded workspace (chunks
+of (s,k) blocks that straddle the spin boundary), the fused Adam step, the
+split potential and the elementwise polarised LDA."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from oracle import restatement as R
+from tests.systems import make_system, random_params
+
+pytestmark = pytest.mark.gpu
+
+# the unpolarised parity tolerances (FP64: rounding; FP32: the benchmarked
+# mixed-precision path)
+TOL = {64: dict(e_rel=1e-10, g_rel=1e-9), 32: dict(e_rel=2e-6, g_rel=1e-4)}
+
+CASES = [
+  dict(sys=dict(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 2), nb=6, nocc=3), occ=(4, 2)),
+  # register-resident slab kernels (24^3) and the pruned 32^3 transforms
+  dict(sys=dict(kind="diamond", grid=(24, 24, 24), kgrid=(1, 1, 1), nb=5, nocc=2), occ=(3, 1)),
+  dict(sys=dict(kind="si8", grid=(32, 32, 32), kgrid=(2, 1, 1), nb=20, nocc=16), occ=(17, 15)),
+  # more than 32 bands (tiled Gram, thread-per-G rotations)
+  dict(sys=dict(kind="si2", grid=(16, 16, 16), kgrid=(1, 1, 2), nb=40, nocc=20), occ=(22, 18)),
+]
+
+
+def _spin_system(case):
+  sysm = make_system(**case["sys"])
+  K, B = sysm.kpts.shape[0], case["sys"]["nb"]
+  occ = np.zeros((2, K, B))
+  occ[0, :, :case["occ"][0]] = 1.0 / K
+  occ[1, :, :case["occ"][1]] = 1.0 / K
+  return dataclasses.replace(sysm, occupation=occ)
+
+
+def _plan(sysm, prec):
+  from jrystal_gb300.engine import PlaneWavePlan
+  return PlaneWavePlan(sysm.cell_vectors, sysm.positions, sysm.charges, sysm.grid, sysm.mask,
+                       sysm.kpts, sysm.occupation.shape[-1], 2, prec, sysm.xc)
+
+
+def _check(e, tgr, tgi, terms, gr, gi, prec):
+  tol = TOL[prec]
+  for i, name in enumerate(["kinetic", "external", "hartree", "xc", "total"]):
+    ref = terms[name]
+    assert abs(e[i] - ref) <= tol["e_rel"] * max(1.0, abs(ref)), (name, e[i], ref)
+  assert e[6] == 0.0
+  scale = max(np.abs(gr).max(), np.abs(gi).max())
+  err = max(np.abs(tgr - gr).max(), np.abs(tgi - gi).max())
+  assert err <= tol["g_rel"] * scale, (err, scale)
+
+
+@pytest.mark.parametrize("pipeline", [1, 0])
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_polarised_energy_and_grad(case, prec, pipeline):
+  import torch
+  sysm = _spin_system(CASES[case])
+  wr, wi = random_params(sysm, seed=20 + case, ns=2)
+  terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+  plan = _plan(sysm, prec)
+  dt = torch.float64 if prec == 64 else torch.float32
+  prev = plan.lib.jrg_pipeline(pipeline)
+  try:
+    e, tgr, tgi = plan.energy_and_grad(torch.tensor(wr, dtype=dt, device="cuda"),
+                                       torch.tensor(wi, dtype=dt, device="cuda"), sysm.occupation)
+    e = e.cpu().numpy()
+  finally:
+    plan.lib.jrg_pipeline(prev)
+  _check(e, tgr.cpu().numpy(), tgi.cpu().numpy(), terms, gr, gi, prec)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_polarised_bounded_workspace_chunks_cross_the_spin_boundary(prec):
+  import torch
+  sysm = _spin_system(CASES[0])   # K = 2: four (s,k) blocks
+  wr, wi = random_params(sysm, seed=31, ns=2)
+  terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+  plan = _plan(sysm, prec)
+  full = plan.workspace_bytes
+  kc = None
+  for frac in np.linspace(0.55, 0.999, 60):
+    kc = plan.set_memory_limit(int(full * frac))
+    if kc == 3:
+      break
+  assert kc == 3, kc    # chunks {0,1,2} and {3}: the first holds both spins
+  dt = torch.float64 if prec == 64 else torch.float32
+  e, tgr, tgi = plan.energy_and_grad(torch.tensor(wr, dtype=dt, device="cuda"),
+                                     torch.tensor(wi, dtype=dt, device="cuda"), sysm.occupation)
+  _check(e.cpu().numpy(), tgr.cpu().numpy(), tgi.cpu().numpy(), terms, gr, gi, prec)
+
+
+def test_two_equal_channels_match_the_restricted_plan():
+  import torch
+  sysm = make_system(kind="si2", grid=(24, 24, 24), kgrid=(1, 1, 2), nb=6, nocc=3)
+  wr, wi = random_params(sysm, seed=33)
+  from jrystal_gb300.engine import PlaneWavePlan
+  p1 = PlaneWavePlan(sysm.cell_vectors, sysm.positions, sysm.charges, sysm.grid, sysm.mask,
+                     sysm.kpts, 6, 1, 64, sysm.xc)
+  s2 = dataclasses.replace(sysm, occupation=np.concatenate([sysm.occupation / 2] * 2))
+  p2 = _plan(s2, 64)
+  a = torch.tensor(wr, device="cuda")
+  b = torch.tensor(wi, device="cuda")
+  e1, g1r, g1i = p1.energy_and_grad(a, b, sysm.occupation)
+  e2, g2r, g2i = p2.energy_and_grad(torch.cat([a, a]).contiguous(), torch.cat([b, b]).contiguous(),
+                                    s2.occupation)
+  e1, e2 = e1.cpu().numpy(), e2.cpu().numpy()
+  assert np.abs(e1[:5] - e2[:5]).max() <= 1e-11 * np.abs(e1[:5]).max()
+  for s in range(2):
+    assert torch.allclose(g2r[s], g1r[0] / 2, rtol=0, atol=1e-11 * float(g1r.abs().max()))
+    assert torch.allclose(g2i[s], g1i[0] / 2, rtol=0, atol=1e-11 * float(g1i.abs().max()))
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_polarised_fused_adam_step(prec):
+  import torch
+  sysm = _spin_system(CASES[0])
+  wr, wi = random_params(sysm, seed=34, ns=2)
+  terms, gr, gi, _ = R.energy_terms(wr, wi, sysm)
+  plan = _plan(sysm, prec)
+  dt = torch.float64 if prec == 64 else torch.float32
+  p = torch.tensor(np.stack([wr, wi]), dtype=dt, device="cuda")
+  m, v = torch.zeros_like(p), torch.zeros_like(p)
+  e = plan.energy_grad_adam(p, m, v, sysm.occupation, 1, 1e-2).cpu().numpy()
+  ref_p = np.stack([wr, wi])
+  ref_m, ref_v = np.zeros_like(ref_p), np.zeros_like(ref_p)
+  ref_p, ref_m, ref_v = R.adam_update(ref_p, np.stack([gr, gi]), ref_m, ref_v, 1, 1e-2)
+  tol = TOL[prec]
+  assert abs(e[4] - terms["total"]) <= tol["e_rel"] * abs(terms["total"])
+  # the first Adam step moves each element by about lr sign(g): compare where
+  # |g| is not negligible (the sign is then defined in both precisions)
+  g = np.stack([gr, gi])
+  big = np.abs(g) > 1e-3 * np.abs(g).max()
+  np.testing.assert_allclose(p.cpu().numpy()[big], ref_p[big], rtol=0, atol=1e-6 if prec == 64 else 1e-4)
+
+
+@pytest.mark.parametrize("kohn_sham", [False, True])
+def test_polarised_split_potential(kohn_sham):
+  import torch
+  sysm = _spin_system(CASES[0])
+  wr, wi = random_params(sysm, seed=35, ns=2)
+  dense = R.coeff(wr, wi, sysm.mask)
+  rho = R.density_grid(dense, sysm.vol, sysm.occupation)          # (2,x,y,z)
+  v_h, v_e, v_xc = R.effective(rho, sysm.positions, sysm.charges, sysm.g_vector_grid, sysm.vol,
+                               split=True, xc_type=sysm.xc, kohn_sham=kohn_sham)
+  plan = _plan(sysm, 64)
+  out = plan.potential(torch.tensor(rho, device="cuda"), kohn_sham=kohn_sham).cpu().numpy()
+  assert out.shape == (4,) + tuple(sysm.grid)
+  scale = max(np.abs(np.real(v_h)).max(), np.abs(np.real(v_e)).max(), np.abs(v_xc).max())
+  np.testing.assert_allclose(out[0], np.real(v_h), atol=1e-11 * scale)
+  np.testing.assert_allclose(out[1], np.real(v_e), atol=1e-11 * scale)
+  xc = np.broadcast_to(v_xc, (2,) + tuple(sysm.grid))
+  np.testing.assert_allclose(out[2:], xc, atol=1e-11 * scale)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_polarised_lda_elementwise(prec):
+  import torch
+  from jrystal_gb300._ops import lda_pol_raw
+  rng = np.random.default_rng(36)
+  up = np.geomspace(1e-6, 50, 4000) * rng.uniform(0.0, 1.0, 4000)
+  dn = np.geomspace(1e-6, 50, 4000)[::-1] * rng.uniform(0.0, 1.0, 4000)
+  up[:5] = 0.0          # fully polarised points
+  dn[-5:] = 0.0
+  rho = np.stack([up, dn])
+  xc = "lda_x+lda_c_vwn"
+  dt = torch.float64 if prec == 64 else torch.float32
+  t = torch.tensor(rho, dtype=dt, device="cuda")
+  tol = 1e-12 if prec == 64 else 2e-6
+  # the oracle at the densities the kernel sees (FP32-rounded on that path)
+  r = rho.astype(np.float32).astype(np.float64) if prec == 32 else rho
+  e_r, d_r = R.xc_eps_pol(r, xc)
+  e0 = lda_pol_raw(t, xc, 0).double().cpu().numpy()
+  np.testing.assert_allclose(e0, e_r, rtol=tol, atol=1e-300)
+  v1 = lda_pol_raw(t, xc, 1).double().cpu().numpy()
+  np.testing.assert_allclose(v1, e_r[None] + r * d_r, rtol=tol, atol=1e-300)
+  v2 = lda_pol_raw(t, xc, 2).double().cpu().numpy()
+  np.testing.assert_allclose(v2, e_r[None] + r.sum(0)[None] * d_r, rtol=tol, atol=1e-300)
+
+
+def test_polarised_xc_energy_autograd():
+  import torch
+  from jrystal_gb300 import energy
+  sysm = _spin_system(CASES[0])
+  wr, wi = random_params(sysm, seed=37, ns=2)
+  rho = R.density_grid(R.coeff(wr, wi, sysm.mask), sysm.vol, sysm.occupation)
+  ref = R.xc_energy(rho, sysm.vol, sysm.xc)
+  eps, d = R.xc_eps_pol(rho, sysm.xc)
+  n = np.prod(sysm.grid)
+  ref_grad = (eps[None] + rho.sum(0)[None] * d) * sysm.vol / n
+  t = torch.tensor(rho, device="cuda", requires_grad=True)
+  e = energy.xc_energy(t, torch.tensor(sysm.g_vector_grid, device="cuda"), sysm.vol, sysm.xc)
+  (g,) = torch.autograd.grad(e, t)
+  assert abs(float(e.detach()) - ref) <= 1e-11 * abs(ref)
+  np.testing.assert_allclose(g.cpu().numpy(), ref_grad, rtol=1e-10, atol=1e-14)
+
+
+def test_spin_unrestricted_driver(tmp_path):
+  """calc.energy_all_electrons with spin_restricted False (two channels,
+  (nelec +- spin)/2 occupied bands each, two empty bands so that the up
+  channel's 15 fit): the energy decreases and the
+  reported terms are the oracle's at the returned parameters."""
+  import jrystal_gb300 as jr
+  xyz = tmp_path / "si2.xyz"
+  a = 10.26 * 0.529177249
+  xyz.write_text("2\nLattice=\"0 {0} {0} {0} 0 {0} {0} {0} 0\" Properties=species:S:1:pos:R:3\n"
+                 "Si 0 0 0\nSi {1} {1} {1}\n".format(a / 2, a / 4))
+  out = jr.calc.energy_all_electrons({
+    "crystal_file_path_path": str(xyz), "grid_sizes": 16, "k_grid_sizes": [1, 1, 1],
+    "cutoff_energy": 10.0, "epoch": 60, "convergence_condition": 1e-12, "empty_bands": 2,
+    "spin": 2, "spin_restricted": False,
+    "optimizer_args": {"learning_rate": 0.01, "b1": 0.9, "b2": 0.99}})
+  h = out.total_energy_history
+  assert h[-1] < h[0]
+  p = out.params_pw
+  assert tuple(p["w_re"].shape[:2]) == (2, 1)
+  c = out.crystal
+  nb = p["w_re"].shape[-1]
+  mask = jr.grid.spherical_mask(c.cell_vectors, (16, 16, 16), 10.0)
+  kpts = jr.grid.k_vectors(c.cell_vectors, (1, 1, 1))
+  occ = np.zeros((2, 1, nb))
+  occ[0, 0, :(28 + 2) // 2] = 1.0
+  occ[1, 0, :(28 - 2) // 2] = 1.0
+  sysm = R.System(c.cell_vectors, c.positions, np.asarray(c.charges, float), (16, 16, 16), mask,
+                  kpts, occ, "lda_x+lda_c_vwn")
+  ref = R.energy_terms(p["w_re"].cpu().numpy(), p["w_im"].cpu().numpy(), sysm, with_grad=False)
+  assert abs(out.energy_terms["total"] - ref["total"]) < 1e-8 * abs(ref["total"])
+  assert tuple(out.density_grid.shape) == (2, 16, 16, 16)
