@@ -75,6 +75,138 @@ __global__ void __launch_bounds__(256) k_reduce_density(const R* __restrict__ pa
   }
 }
 
+// k_reduce_density with 16-byte loads and stores (4 FP32 or 2 FP64 points
+// per thread) and the group loop unrolled by four with its loads issued
+// together, so that each thread keeps several loads in flight: the partials
+// are read once from HBM and the kernel sits between the two forks of the
+// pipelined step, where nothing else hides its latency.  Same arithmetic
+// per point as k_reduce_density.  Needs ngrid % (16 / sizeof(R)) == 0 and
+// 16-byte aligned part and rho.
+template <typename R> struct Vec16;
+template <> struct Vec16<float> { using T = float4; static constexpr int n = 4; };
+template <> struct Vec16<double> { using T = double2; static constexpr int n = 2; };
+
+// one float-float accumulation step: (sh, sl) += x * (f.x + f.y)
+__device__ __forceinline__ void ff_acc(float& sh, float& sl, float x, float2 f) {
+  const float p = x * f.x;
+  const float pe = fmaf(x, f.y, fmaf(x, f.x, -p));   // exact low part of x*hi, plus x*lo
+  const float t = sh + p;                            // two-sum of sh and p
+  const float bb = t - sh;
+  const float te = (sh - (t - bb)) + (p - bb);
+  sh = t;
+  sl += te + pe;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_reduce_density_v(const R* __restrict__ part, R* __restrict__ rho,
+                                                          int groups_per_spin, int ns, long long ngrid,
+                                                          const double* __restrict__ gscale,
+                                                          double* __restrict__ qpart) {
+  using V = typename Vec16<R>::T;
+  constexpr int W = Vec16<R>::n;
+  constexpr int U = 4;   // groups per unrolled step
+  __shared__ double red[32];
+  __shared__ float2 sg[kMaxReduceGroups];
+  const int ngr = groups_per_spin * ns;
+  const bool staged = ngr <= kMaxReduceGroups;
+  if (staged)
+    for (int g = threadIdx.x; g < ngr; g += blockDim.x) {
+      const float h = (float)gscale[g];
+      sg[g] = make_float2(h, (float)(gscale[g] - (double)h));
+    }
+  __syncthreads();
+  const long long ngv = ngrid / W, n = (long long)ns * ngv;
+  const V* src = reinterpret_cast<const V*>(part);
+  V* dst = reinterpret_cast<V*>(rho);
+  double q = 0.0;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long s = e / ngv, iv = e % ngv;
+    const long long g0 = s * groups_per_spin;
+    V o;
+    if constexpr (sizeof(R) == 4) {
+      float h0 = 0.f, h1 = 0.f, h2 = 0.f, h3 = 0.f, l0 = 0.f, l1 = 0.f, l2 = 0.f, l3 = 0.f;
+      int g = 0;
+      for (; g + U <= groups_per_spin; g += U) {
+        V x[U];
+        float2 f[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) x[u] = src[(g0 + g + u) * ngv + iv];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const long long gg = g0 + g + u;
+          if (staged) {
+            f[u] = sg[gg];
+          } else {
+            f[u].x = (float)gscale[gg];
+            f[u].y = (float)(gscale[gg] - (double)f[u].x);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          ff_acc(h0, l0, x[u].x, f[u]);
+          ff_acc(h1, l1, x[u].y, f[u]);
+          ff_acc(h2, l2, x[u].z, f[u]);
+          ff_acc(h3, l3, x[u].w, f[u]);
+        }
+      }
+      for (; g < groups_per_spin; ++g) {
+        const long long gg = g0 + g;
+        const V x = src[gg * ngv + iv];
+        float2 f;
+        if (staged) {
+          f = sg[gg];
+        } else {
+          f.x = (float)gscale[gg];
+          f.y = (float)(gscale[gg] - (double)f.x);
+        }
+        ff_acc(h0, l0, x.x, f);
+        ff_acc(h1, l1, x.y, f);
+        ff_acc(h2, l2, x.z, f);
+        ff_acc(h3, l3, x.w, f);
+      }
+      o.x = (float)((double)h0 + (double)l0);
+      o.y = (float)((double)h1 + (double)l1);
+      o.z = (float)((double)h2 + (double)l2);
+      o.w = (float)((double)h3 + (double)l3);
+      q += ((double)o.x + (double)o.y) + ((double)o.z + (double)o.w);
+    } else {
+      double a0 = 0.0, a1 = 0.0;
+      int g = 0;
+      for (; g + U <= groups_per_spin; g += U) {
+        V x[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) x[u] = src[(g0 + g + u) * ngv + iv];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const double f = gscale[g0 + g + u];
+          a0 += f * x[u].x;
+          a1 += f * x[u].y;
+        }
+      }
+      for (; g < groups_per_spin; ++g) {
+        const V x = src[(g0 + g) * ngv + iv];
+        const double f = gscale[g0 + g];
+        a0 += f * x.x;
+        a1 += f * x.y;
+      }
+      o.x = a0;
+      o.y = a1;
+      q += o.x + o.y;
+    }
+    dst[e] = o;
+  }
+  if (qpart) {
+    q = block_sum(q, red);
+    if (threadIdx.x == 0) qpart[blockIdx.x] = q;
+  }
+}
+
+// threads per CTA of the single-grid energy kernels (k_recip_terms,
+// k_potential, k_potential_pol; their CTA count is the number of energy
+// slots)
+constexpr int kGridThreads = 256;   // 512: k_recip_terms 34 vs 19 us, k_potential 28 vs 19 us (64^3)
+
 // the charge factor s of ChargeFix (every thread of the block gets it)
 __device__ __forceinline__ double charge_scale(const ChargeFix& cf, double* red) {
   if (!cf.qpart) return 1.0;
@@ -93,7 +225,7 @@ __device__ __forceinline__ double charge_scale(const ChargeFix& cf, double* red)
 // The external energy and potential are taken in real space from the FP64
 // V_ext(r) table by the potential kernels (Parseval: the same sum).
 template <typename R>
-__global__ void __launch_bounds__(256) k_recip_terms(const C_t<R>* __restrict__ rhog,
+__global__ void __launch_bounds__(kGridThreads) k_recip_terms(const C_t<R>* __restrict__ rhog,
                                                      const double* __restrict__ ginv,
                                                      C_t<R>* __restrict__ vg, double* __restrict__ slot_h,
                                                      long long ngrid, double pref, ChargeFix cf) {
@@ -101,6 +233,7 @@ __global__ void __launch_bounds__(256) k_recip_terms(const C_t<R>* __restrict__ 
   const double s = charge_scale(cf, red);
   if (cf.scale && blockIdx.x == 0 && threadIdx.x == 0) *cf.scale = s;
   double eh = 0.0;
+#pragma unroll 4
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ngrid;
        i += (long long)gridDim.x * blockDim.x) {
     const C_t<R> r = rhog[i];
@@ -147,13 +280,26 @@ __device__ __forceinline__ void lda_eps_v(double rho, int xc, double* eps, doubl
   *v = vv;
 }
 
-// FP32 path: rho^(1/3) from cbrtf refined by one Newton step in FP64 (the
-// exchange term dominates E_xc), the VWN correlation (about 1% of it) in FP32.
+// rho^(1/3) to about FP64 accuracy from FP32 arithmetic: y = cbrtf(rho)
+// and one Newton step y - (y^3 - rho) / (3 y^2), whose residual y^3 - rho is
+// formed exactly (y^2 and y^2 * y as float-float products by FMA; p3 - rho
+// is exact because p3 and rho agree to a few ulps) and whose correction,
+// ~1e-7 of y, needs only FP32 precision.  Two FP64 operations instead of an
+// FP64 Newton step with its division (the GPU's FP64 rate is 1/64 of FP32).
+__device__ __forceinline__ double cbrt_ff(float rho) {
+  const float y = cbrtf(rho);
+  const float p2 = y * y, e2 = fmaf(y, y, -p2);
+  const float p3 = p2 * y, e3 = fmaf(p2, y, -p3);
+  const float res = (p3 - rho) + fmaf(e2, y, e3);
+  return (double)y - (double)__fdividef(res, 3.0f * p2);   // 2-ulp quotient of a ~1e-7 correction
+}
+
+// FP32 path: rho^(1/3) by cbrt_ff (the exchange term dominates E_xc), the
+// VWN correlation (about 1% of it) in FP32.
 __device__ __forceinline__ void lda_eps_v_f32(float rho, int xc, double* eps, double* v) {
   double e = 0.0, vv = 0.0;
   if (rho > 1e-15f) {
-    double y = (double)cbrtf(rho);
-    y -= (y * y * y - (double)rho) / (3.0 * y * y);
+    const double y = cbrt_ff(rho);
     if (xc & JRG_XC_LDA_X) {
       const double ex = -0.7385587663820224 * y;   // (3/4) (3/pi)^(1/3) rho^(1/3)
       e += ex;
@@ -163,7 +309,7 @@ __device__ __forceinline__ void lda_eps_v_f32(float rho, int xc, double* eps, do
       const float A = 0.0310907f, b = 3.72744f, c = 12.9352f, x0 = -0.10498f;
       const float q = 6.15199081975907951f;        // sqrt(4c - b^2)
       const float xx0 = x0 * x0 + b * x0 + c;
-      const float rs = (float)(0.62035049089940001 / y);   // (3/(4 pi))^(1/3) / rho^(1/3)
+      const float rs = 0.620350491f / (float)y;   // (3/(4 pi))^(1/3) / rho^(1/3)
       const float x = sqrtf(rs);
       const float xx = x * x + b * x + c;
       const float at = atanf(q / (2.0f * x + b));
@@ -211,14 +357,10 @@ __device__ __forceinline__ void vwn_fit(T x, T A, T b, T c, T x0, T q, T* f, T* 
              b * x0 / xx0 * (T(2) / (x - x0) - (T(2) * x + b) / xx - T(4) * (b + T(2) * x0) / den));
 }
 
-// rho^(1/3) to FP64 accuracy: cbrtf plus one Newton step on the FP32 path
+// rho^(1/3) to FP64 accuracy (cbrt_ff on the FP32 path)
 template <typename R> __device__ __forceinline__ double cbrt_t(R r) {
-  if constexpr (sizeof(R) == 4) {
-    double y = (double)cbrtf(r);
-    return y - (y * y * y - (double)r) / (3.0 * y * y);
-  } else {
-    return cbrt((double)r);
-  }
+  if constexpr (sizeof(R) == 4) return cbrt_ff(r);
+  else return cbrt((double)r);
 }
 
 template <typename R>
@@ -244,7 +386,7 @@ __device__ __forceinline__ void lda_pol(R ru, R rd, int xc, double* eps, double*
     constexpr double kPi = 3.14159265358979323846;
     T z = (ru - rd) / rt;
     z = z > T(1) ? T(1) : (z < T(-1) ? T(-1) : z);
-    const T x = sqrt(T(0.6203504908994001 / cbrt_t<R>(rt)));   // sqrt(rs), rs = (3/(4 pi rho))^(1/3)
+    const T x = sqrt(T(0.6203504908994001) / T(cbrt_t<R>(rt)));   // sqrt(rs), rs = (3/(4 pi rho))^(1/3)
     T ep, dep, ef, def, al, dal;
     vwn_fit<T>(x, T(0.0310907), T(3.72744), T(12.9352), T(-0.10498), T(6.15199081975907951), &ep, &dep);
     vwn_fit<T>(x, T(0.01554535), T(7.06042), T(18.0578), T(-0.32500), T(4.730926909560114), &ef, &def);
@@ -274,7 +416,7 @@ __device__ __forceinline__ void lda_pol(R ru, R rd, int xc, double* eps, double*
 // external parts act on the total density, V_s = V_H + V_ext + eps + rho
 // d eps / d rho_s; E_xc = vol/N sum eps rho, E_ext = vol/N sum V_ext rho
 template <typename R>
-__global__ void __launch_bounds__(256) k_potential_pol(const R* __restrict__ rho,
+__global__ void __launch_bounds__(kGridThreads) k_potential_pol(const R* __restrict__ rho,
                                                        const C_t<R>* __restrict__ vri, double vscale,
                                                        R* __restrict__ vr, double* __restrict__ slot_x,
                                                        long long ngrid, int xc, double pref,
@@ -495,7 +637,7 @@ __global__ void k_potential_gga(const C_t<R>* __restrict__ vri, double vscale, R
 // v_xc + V_ext(r) (when vr is given), E_xc = vol/N sum eps s rho and, with
 // vext_r, E_ext = vol/N sum V_ext(r) s rho (FP64 table, real-space form).
 template <typename R>
-__global__ void __launch_bounds__(256) k_potential(const R* __restrict__ rho,
+__global__ void __launch_bounds__(kGridThreads, 4) k_potential(const R* __restrict__ rho,
                                                    const C_t<R>* __restrict__ vri, double vscale,
                                                    R* __restrict__ vr, double* __restrict__ slot_x,
                                                    long long ngrid, int xc, double pref,
@@ -609,40 +751,57 @@ __global__ void k_kin_reduce(const R* __restrict__ part, int nblk, int nb, int n
   }
 }
 
+constexpr int kSumThreads = 512;
 // energies[t] = sum of its slots, t = 0..3; energies[4] = total
 // energies[t] = sum of slots [slot_begin[t], slot_begin[t+1]) for t < nterms;
 // with extra_term >= 0 the range [slot_begin[nterms], slot_begin[nterms+1])
 // (the nonlocal pseudopotential energy) is added to term extra_term and also
 // reported alone in energies[nterms + 3]; energies[nterms] = total.
-__global__ void k_sum_slots(const double* __restrict__ slots, const int* __restrict__ slot_begin,
-                            double* __restrict__ energies, int nterms, const int* __restrict__ flags,
-                            int extra_term) {
-  __shared__ double red[32];
-  __shared__ double tot, extra;
-  if (threadIdx.x == 0) { tot = 0.0; extra = 0.0; }
-  if (extra_term >= 0) {
-    double acc = 0.0;
-    for (int i = slot_begin[nterms] + threadIdx.x; i < slot_begin[nterms + 1]; i += blockDim.x) acc += slots[i];
-    acc = block_sum(acc, red);
-    if (threadIdx.x == 0) extra = acc;
+__global__ void __launch_bounds__(kSumThreads) k_sum_slots(const double* __restrict__ slots,
+                                                           const int* __restrict__ slot_begin,
+                                                           double* __restrict__ energies, int nterms,
+                                                           const int* __restrict__ flags, int extra_term) {
+  // every thread sums its share of all ranges at once, then one two-level
+  // reduction of the (nterms + 1) partial sums (one barrier)
+  constexpr int kMaxT = 5;
+  __shared__ double part[kSumThreads / 32][kMaxT];
+  const int nt = nterms + (extra_term >= 0 ? 1 : 0);   // the extra range last
+  double acc[kMaxT];
+#pragma unroll
+  for (int t = 0; t < kMaxT; ++t) {
+    acc[t] = 0.0;
+    if (t < nt)
+      for (int i = slot_begin[t] + threadIdx.x; i < slot_begin[t + 1]; i += blockDim.x) acc[t] += slots[i];
   }
-  for (int t = 0; t < nterms; ++t) {
-    double acc = 0.0;
-    for (int i = slot_begin[t] + threadIdx.x; i < slot_begin[t + 1]; i += blockDim.x) acc += slots[i];
-    acc = block_sum(acc, red);
-    if (threadIdx.x == 0) {
-      if (t == extra_term) acc += extra;
-      energies[t] = acc;
-      tot += acc;
-    }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < kMaxT; ++t) {
+    double v = acc[t];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) part[wid][t] = v;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    energies[nterms] = tot;
-    // the largest Gram condition estimate of the call (note_condition)
-    energies[nterms + 1] = flags ? __longlong_as_double(*reinterpret_cast<const long long*>(flags + 2)) : 0.0;
-    energies[nterms + 2] = flags ? (double)flags[0] : 0.0;
-    energies[nterms + 3] = extra;
+  if (wid == 0) {
+#pragma unroll
+    for (int t = 0; t < kMaxT; ++t) {
+      double v = lane < kSumThreads / 32 ? part[lane][t] : 0.0;
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      acc[t] = v;
+    }
+    if (lane == 0) {
+      const double extra = extra_term >= 0 ? acc[nterms] : 0.0;
+      double tot = 0.0;
+      for (int t = 0; t < nterms; ++t) {
+        const double e = acc[t] + (t == extra_term ? extra : 0.0);
+        energies[t] = e;
+        tot += e;
+      }
+      energies[nterms] = tot;
+      // the largest Gram condition estimate of the call (note_condition)
+      energies[nterms + 1] = flags ? __longlong_as_double(*reinterpret_cast<const long long*>(flags + 2)) : 0.0;
+      energies[nterms + 2] = flags ? (double)flags[0] : 0.0;
+      energies[nterms + 3] = extra;
+    }
   }
 }
 
@@ -897,6 +1056,13 @@ static inline unsigned grid_for(long long n, int per = 256, int cap = 4096) {
 template <typename R>
 int launch_reduce_density(const void* part, void* rho, int groups_per_spin, int ns, long long ngrid,
                           const double* gscale, double* qpart, cudaStream_t st) {
+  constexpr int W = Vec16<R>::n;
+  if (ngrid % W == 0 && ((reinterpret_cast<uintptr_t>(part) | reinterpret_cast<uintptr_t>(rho)) & 15) == 0) {
+    k_reduce_density_v<R><<<kQParts, 256, 0, st>>>(reinterpret_cast<const R*>(part), reinterpret_cast<R*>(rho),
+                                                   groups_per_spin, ns, ngrid, gscale, qpart);
+    JRG_LAUNCH_CHECK("k_reduce_density_v");
+    return JRG_OK;
+  }
   k_reduce_density<R><<<kQParts, 256, 0, st>>>(reinterpret_cast<const R*>(part), reinterpret_cast<R*>(rho),
                                                groups_per_spin, ns, ngrid, gscale, qpart);
   JRG_LAUNCH_CHECK("k_reduce_density");
@@ -906,7 +1072,7 @@ int launch_reduce_density(const void* part, void* rho, int groups_per_spin, int 
 template <typename R>
 int launch_recip_terms(const void* rhog, const double* ginv, void* vg, double* slot_h, int nblocks,
                        long long ngrid, double pref, const ChargeFix& cf, cudaStream_t st) {
-  k_recip_terms<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const C_t<R>*>(rhog), ginv,
+  k_recip_terms<R><<<nblocks, kGridThreads, 0, st>>>(reinterpret_cast<const C_t<R>*>(rhog), ginv,
                                             reinterpret_cast<C_t<R>*>(vg), slot_h, ngrid, pref, cf);
   JRG_LAUNCH_CHECK("k_recip_terms");
   return JRG_OK;
@@ -916,7 +1082,7 @@ template <typename R>
 int launch_potential(const void* rho, const void* vri, double vscale, void* vr, double* slot_x,
                      int nblocks, long long ngrid, int xc, double pref, const double* qscale,
                      const double* vext_r, double* slot_e, cudaStream_t st) {
-  k_potential<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const R*>(rho),
+  k_potential<R><<<nblocks, kGridThreads, 0, st>>>(reinterpret_cast<const R*>(rho),
                                           reinterpret_cast<const C_t<R>*>(vri), vscale,
                                           reinterpret_cast<R*>(vr), slot_x, ngrid, xc, pref, qscale,
                                           vext_r, slot_e);
@@ -928,7 +1094,7 @@ template <typename R>
 int launch_potential_pol(const void* rho, const void* vri, double vscale, void* vr, double* slot_x,
                          int nblocks, long long ngrid, int xc, double pref, const double* qscale,
                          const double* vext_r, double* slot_e, cudaStream_t st) {
-  k_potential_pol<R><<<nblocks, 256, 0, st>>>(reinterpret_cast<const R*>(rho),
+  k_potential_pol<R><<<nblocks, kGridThreads, 0, st>>>(reinterpret_cast<const R*>(rho),
                                               reinterpret_cast<const C_t<R>*>(vri), vscale,
                                               reinterpret_cast<R*>(vr), slot_x, ngrid, xc, pref, qscale,
                                               vext_r, slot_e);
@@ -1047,7 +1213,8 @@ int launch_band_trace_sums(const double2* A, int nsk, int nb, const double* slot
 
 int launch_sum_slots(const double* slots, const int* slot_begin, double* energies, int nterms,
                      const int* flags, int extra_term, cudaStream_t st) {
-  k_sum_slots<<<1, 256, 0, st>>>(slots, slot_begin, energies, nterms, flags, extra_term);
+  if (nterms < 1 || nterms + (extra_term >= 0 ? 1 : 0) > 5) return fail(JRG_ERR_INVALID, "k_sum_slots: too many terms");
+  k_sum_slots<<<1, kSumThreads, 0, st>>>(slots, slot_begin, energies, nterms, flags, extra_term);
   JRG_LAUNCH_CHECK("k_sum_slots");
   return JRG_OK;
 }
