@@ -201,9 +201,46 @@ k_gram_w(const void* __restrict__ X0, const void* __restrict__ X1, const void* _
   for (int e = t; e < 2 * CG * LD; e += 256) {
     if (e % LD >= nb) { xs[e] = czero<C>(); ys[e] = czero<C>(); }
   }
+  // parameter layout: the chunk's CG x nb values are contiguous in global
+  // memory (element e of the chunk at offset e), and the shared-memory slot
+  // of element e (column e / nb, band e % nb) is the same in every chunk: it
+  // is computed once per thread instead of per copy
+  constexpr int EPT = (CG * NBP + 255) / 256;   // staged elements per thread
+  int soff[EPT];
+  if constexpr (LX == LAYOUT_SPLIT) {
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+      const int e = t + 256 * k;
+      soff[k] = e < CG * nb ? (e / nb) * LD + e % nb : -1;
+    }
+  }
   auto stage = [&](int buf, int g0) {
     C* xd = xs + buf * CG * LD;
     C* yd = ys + buf * CG * LD;
+    if constexpr (LX == LAYOUT_SPLIT && LY == LAYOUT_SPLIT) {
+      const size_t base = (sk * ng + g0) * (size_t)nb;
+      const int lim = (g_end - g0) * nb;   // elements of the chunk inside the split
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        if (soff[k] < 0) continue;
+        const int e = t + 256 * k;
+        C* dx = xd + soff[k];
+        C* dy = yd + soff[k];
+        if (e >= lim) {
+          *dx = czero<C>();
+          if (!SAME) *dy = czero<C>();
+        } else {
+          cp_async<sizeof(R)>(&dx->x, reinterpret_cast<const R*>(X0) + base + e);
+          cp_async<sizeof(R)>(&dx->y, reinterpret_cast<const R*>(X1) + base + e);
+          if (!SAME) {
+            cp_async<sizeof(R)>(&dy->x, reinterpret_cast<const R*>(Y0) + base + e);
+            cp_async<sizeof(R)>(&dy->y, reinterpret_cast<const R*>(Y1) + base + e);
+          }
+        }
+      }
+      cp_async_commit();
+      return;
+    }
     for (int e = t; e < CG * nb; e += 256) {
       int r, c;   // band, chunk column
       if (LX == LAYOUT_SPLIT) { r = e % nb; c = e / nb; }
