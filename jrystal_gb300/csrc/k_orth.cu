@@ -525,12 +525,16 @@ __global__ void __launch_bounds__(1024) k_cholesky_inv_big(const double2* __rest
   }
 }
 
-// Adjoint small matrices per (s,k), one CTA each:
+// Adjoint small matrices per (s,k):
 //   Rh = R^{-H};  K from A;  M2 = K R^{-H}  (stored negated: -M2)
 // With occupations f given, A holds C^H (H C) (unweighted): the band energies
 // Re A_bb are written to eps and the occupations are folded in as
 // A diag(f) (for K) and diag(f) R^{-H} (for Rh).
-__global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict__ A,
+// Grid (nsk, parts): CTA (sk, p) takes elements p*blockDim .. of the nb x nb
+// matrices, so that the FP64 sums of -M2 (1/64 of the FP32 rate) spread over
+// all SMs instead of one CTA per (s,k).
+constexpr int kAdjSmallThreads = 64;
+__global__ void __launch_bounds__(kAdjSmallThreads) k_adjoint_small(const double2* __restrict__ A,
                                                        const double2* __restrict__ Ri,
                                                        double2* __restrict__ Rh,
                                                        double2* __restrict__ negM2, int nb,
@@ -542,16 +546,17 @@ __global__ void __launch_bounds__(256) k_adjoint_small(const double2* __restrict
   const double2* ri = Ri + off;
   const double* fb = f ? f + (size_t)sk * nb : nullptr;
   auto fw = [&](int j) { return fb ? fb[j] : 1.0; };
+  const int e0 = blockIdx.y * blockDim.x + threadIdx.x, es = gridDim.y * blockDim.x;
   if (eps)
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) eps[(size_t)sk * nb + b] = a[b * nb + b].x;
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    for (int b = e0; b < nb; b += es) eps[(size_t)sk * nb + b] = a[b * nb + b].x;
+  for (int e = e0; e < nb * nb; e += es) {
     const int i = e / nb, j = e % nb;
     const double2 v = ri[j * nb + i];
     const double s = fw(i);
     Rh[off + e] = make_double2(s * v.x, -s * v.y);
   }
   if (!with_m2) return;   // formed by k_adjoint_m2_tiled
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+  for (int e = e0; e < nb * nb; e += es) {
     const int i = e / nb, j = e % nb;
     // (K R^{-H})[i][j] = sum_l K[i][l] conj(Ri[j][l]),  Ri upper => l >= j
     double sx = 0.0, sy = 0.0;
@@ -1131,7 +1136,8 @@ int launch_cholesky_inv(const double2* S, double2* Rm, double2* Ri, int nsk, int
 int launch_adjoint_small(const double2* A, const double2* Ri, double2* Rh, double2* negM2, int nsk,
                          int nb, cudaStream_t st, const double* f, double* eps) {
   const bool tiled = nb > 32;
-  k_adjoint_small<<<nsk, 256, 0, st>>>(A, Ri, Rh, negM2, nb, f, eps, !tiled);
+  const unsigned parts = (unsigned)((nb * nb + kAdjSmallThreads - 1) / kAdjSmallThreads);
+  k_adjoint_small<<<dim3(nsk, parts), kAdjSmallThreads, 0, st>>>(A, Ri, Rh, negM2, nb, f, eps, !tiled);
   JRG_LAUNCH_CHECK("k_adjoint_small");
   if (tiled) {
     const unsigned nt = (unsigned)((nb + 31) / 32);
