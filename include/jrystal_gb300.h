@@ -192,10 +192,11 @@ int jrg_energy_grad_bands(const jrg_plan* plan, const void* w_re, const void* w_
  * its gradient with respect to {w_re, w_im} (optional, both or neither), and
  * optionally the band Hamiltonian hmat[s,k][i][j] = w_skj <psi_i| T + V_eff |psi_j>
  * (jrystal/_src/hamiltonian.py:171-240; complex FP64 [S*K][B][B]).
- * v_eff: device [nx][ny][nz] real grid in the plan's precision (V_H + V_ext
- * + v_xc, e.g. the three parts of jrg_potential with kohn_sham = 1 summed);
+ * v_eff: device [S][nx][ny][nz] real grids in the plan's precision, each
+ * spin's V_H + V_ext + v_xc (e.g. the parts of jrg_potential with
+ * kohn_sham = 1 summed per spin); the bands of spin s see grid s.
  * weights: device double [S*K*B] (ones for the band structure); out: device
- * double[2].  num_spin 1. */
+ * double[2]. */
 int jrg_band_trace_grad(const jrg_plan* plan, const void* w_re, const void* w_im,
                         const void* v_eff, const double* weights, double* out, void* hmat,
                         void* grad_re, void* grad_im, void* workspace, cudaStream_t stream);

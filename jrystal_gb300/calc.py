@@ -472,7 +472,7 @@ class BandStructureOutput:
   ground_state: GroundStateEnergyOutput
   band_trace: float = 0.0
   train_time: float = 0.0
-  effective_potential: Optional[torch.Tensor] = None   # V_H + V_ext + v_xc (nx, ny, nz)
+  effective_potential: Optional[torch.Tensor] = None   # V_H + V_ext + v_xc (nx, ny, nz), or (S, ...) for S = 2
 
 
 BAND_DEFAULTS = {
@@ -525,8 +525,7 @@ def _band_structure(config: dict, pseudo: bool) -> BandStructureOutput:
   from .pseudopotential.beta import max_gk_radius
   cfg = dict(BAND_DEFAULTS)
   cfg.update(_merge(config))
-  if not cfg["spin_restricted"]:
-    raise NotImplementedError("the band-structure drivers take one spin channel")
+  ns = _num_spin(cfg)
   gs = _ground_state(cfg, pseudo)
   su = _setup(cfg, pseudo)
   crystal, mask = su.crystal, su.mask
@@ -539,16 +538,18 @@ def _band_structure(config: dict, pseudo: bool) -> BandStructureOutput:
   kmax = max_gk_radius(_grid.g_vectors(crystal.cell_vectors, su.grid_sizes), k_path) if pseudo else None
 
   def make_plan(kpts):
-    return _make_plan(su, cfg, kpts=kpts, num_bands=num_bands, kmax=kmax)
+    return _make_plan(su, cfg, kpts=kpts, num_bands=num_bands, kmax=kmax, num_spin=ns)
 
   t_start = time.perf_counter()
   plan0 = make_plan(k_path[:1])
-  v_h, v_ext, v_xc = plan0.potential(gs.density_grid, kohn_sham=True)
-  v_eff = (v_h + v_ext + v_xc).contiguous()
+  parts = plan0.potential(gs.density_grid, kohn_sham=True)   # V_H, V_ext, v_xc per spin
+  v_eff = (parts[0] + parts[1] + parts[2:]).contiguous()     # (S, x, y, z)
+  if ns == 1:
+    v_eff = v_eff[0]
   gen = torch.Generator(device=plan0.device)
   gen.manual_seed(int(cfg["seed"]))
   ng = int(mask.sum())
-  p0 = torch.rand((2, 1, 1, ng, num_bands), generator=gen, device=plan0.device,
+  p0 = torch.rand((2, ns, 1, ng, num_bands), generator=gen, device=plan0.device,
                   dtype=plan0.rdtype)
   m0, v0 = torch.zeros_like(p0), torch.zeros_like(p0)
   t = _band_minimise(plan0, v_eff, p0, m0, v0, int(cfg["band_structure_epoch"]), lr, b1, b2, eps)
@@ -558,7 +559,7 @@ def _band_structure(config: dict, pseudo: bool) -> BandStructureOutput:
   nk = k_path.shape[0]
   if nk > 1:
     plan1 = make_plan(k_path[1:])
-    rep = lambda x: x.expand(2, 1, nk - 1, ng, num_bands).contiguous()
+    rep = lambda x: x.expand(2, ns, nk - 1, ng, num_bands).contiguous()
     if cfg["k_path_fine_tuning"]:
       p1, m1, v1 = rep(p0), rep(m0), rep(v0)
       steps = int(cfg["k_path_fine_tuning_epoch"])

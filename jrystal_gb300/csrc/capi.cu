@@ -939,7 +939,7 @@ static int band_trace_impl(const jrg_plan* P, const void* w_re, const void* w_im
     }
     {
       PHASE(PH_LINE_APPLY_V);
-      if ((rc = launch_line_apply_v<R>(P, wsp(ws, w.t), wsp(ws, w.u), v_eff, n * P->nb, P->nb, st))) return rc;
+      if ((rc = apply_v_blocks<R>(P, wsp(ws, w.t), wsp(ws, w.u), v_eff, k0, n, st))) return rc;
     }
     {
       PHASE(PH_PLANE_FWD);
@@ -1281,7 +1281,6 @@ int jrg_band_trace_grad(const jrg_plan* P, const void* w_re, const void* w_im, c
                         void* ws, cudaStream_t st) {
   if (!P || !w_re || !w_im || !v_eff || !weights || !out || !ws)
     return fail(JRG_ERR_INVALID, "jrg_band_trace_grad: null argument");
-  if (P->ns != 1) return fail(JRG_ERR_UNSUPPORTED, "jrg_band_trace_grad: num_spin must be 1");
   int rc = P->prec == 64 ? band_trace_impl<double>(P, w_re, w_im, v_eff, weights, out, hmat, grad_re, grad_im, ws, st)
                          : band_trace_impl<float>(P, w_re, w_im, v_eff, weights, out, hmat, grad_re, grad_im, ws, st);
   profile_call_done(P);

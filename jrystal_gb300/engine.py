@@ -218,14 +218,17 @@ class PlaneWavePlan:
     """Band trace sum w <psi|T + V_eff|psi> for a fixed effective potential
     (device float64[2]: trace, kinetic part), its gradient with respect to
     {w_re, w_im}, and optionally the band Hamiltonian (S,K,B,B) complex128
-    with entries w_j <psi_i|H|psi_j>.  ``weights`` (S,K,B) default to ones."""
+    with entries w_j <psi_i|H|psi_j>.  ``v_eff`` is one grid or one per spin
+    (S,x,y,z); ``weights`` (S,K,B) default to ones."""
     self._check_param(w_re, "w_re")
     self._check_param(w_im, "w_im")
     v = torch.as_tensor(v_eff, device=self.device).to(self.rdtype)
-    if v.dim() == 4 and v.shape[0] == 1:
-      v = v[0]
-    if tuple(v.shape) != self.grid:
-      raise ValueError(f"v_eff has shape {tuple(v.shape)}, expected {self.grid}")
+    if v.dim() == 3:
+      v = v[None]
+    if v.shape[0] == 1 and self.num_spin == 2:
+      v = v.expand(2, *self.grid)
+    if tuple(v.shape) != (self.num_spin,) + self.grid:
+      raise ValueError(f"v_eff has shape {tuple(v.shape)}, expected {(self.num_spin,) + self.grid}")
     v = v.contiguous()
     wts = self._occ(torch.ones((self.num_spin, self.num_kpt, self.num_band), dtype=torch.float64)
                     if weights is None else weights)

@@ -772,7 +772,8 @@ def band_trace_terms(w_re, w_im, v_eff, sysm, weights=None, with_grad=True):
   hamiltonian_matrix_trace, kohn_sham=True): trace = sum w <psi|T+V|psi>,
   its kinetic part, the weighted band Hamiltonian A_ij = w_j <psi_i|H|psi_j>
   and d trace / d {w_re, w_im} through the same orthonormalisation adjoint as
-  energy_terms (g_C = w (T c + sqrt(vol)/N FFT(V psi))|_sphere)."""
+  energy_terms (g_C = w (T c + sqrt(vol)/N FFT(V psi))|_sphere).  v_eff is
+  one grid or one per spin channel (the bands of spin s see grid s)."""
   vol = sysm.vol
   gvec = sysm.g_vector_grid
   mask = sysm.mask
@@ -782,8 +783,8 @@ def band_trace_terms(w_re, w_im, v_eff, sysm, weights=None, with_grad=True):
     weights = np.ones(c.shape[:2] + c.shape[-1:])
   dense = expand_coefficient(c, mask)
   wave = _ifftn(dense) * n / np.sqrt(vol)
-  v = np.asarray(v_eff).reshape(sysm.grid)
-  hpsi = _fftn(v[None, None, None] * wave)[..., mask] * (np.sqrt(vol) / n)
+  v = np.asarray(v_eff).reshape((-1,) + tuple(sysm.grid))      # (1 or S, x, y, z)
+  hpsi = _fftn(v[:, None, None] * wave)[..., mask] * (np.sqrt(vol) / n)
   tk = kinetic_operator(gvec, sysm.kpts)[:, mask]  # (k,g)
   hc = tk[None, :, None, :] * np.swapaxes(c, -1, -2) + hpsi   # (s,k,b,g) = H c_b
   if sysm.proj is not None:      # + V_nl c_b (nloc.py:251-303)

@@ -230,3 +230,58 @@ def test_spin_unrestricted_driver(tmp_path):
   ref = R.energy_terms(p["w_re"].cpu().numpy(), p["w_im"].cpu().numpy(), sysm, with_grad=False)
   assert abs(out.energy_terms["total"] - ref["total"]) < 1e-8 * abs(ref["total"])
   assert tuple(out.density_grid.shape) == (2, 16, 16, 16)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_polarised_band_trace_matches_oracle(prec):
+  """jrg_band_trace_grad with one effective potential per spin channel."""
+  import torch
+  sysm = _spin_system(CASES[0])
+  wr, wi = random_params(sysm, seed=38, ns=2)
+  rho = R.density_grid(R.coeff(wr, wi, sysm.mask), sysm.vol, sysm.occupation)
+  v = np.real(R.effective(rho, sysm.positions, sysm.charges, sysm.g_vector_grid, sysm.vol,
+                          False, sysm.xc, True))                       # (2, x, y, z)
+  assert v.shape[0] == 2 and not np.allclose(v[0], v[1])
+  pr, pi = random_params(sysm, seed=39, ns=2)
+  wts = np.random.default_rng(40).uniform(0.5, 2.0, size=sysm.occupation.shape)
+  ref = R.band_trace_terms(pr, pi, v, sysm, weights=wts)
+  plan = _plan(sysm, prec)
+  dt = torch.float64 if prec == 64 else torch.float32
+  out, gr, gi, hm = plan.band_trace_grad(torch.tensor(pr, dtype=dt, device="cuda"),
+                                         torch.tensor(pi, dtype=dt, device="cuda"),
+                                         torch.tensor(v, device="cuda"), weights=wts, hmat=True)
+  out = out.cpu().numpy()
+  tol = dict(e=1e-10, g=1e-9) if prec == 64 else dict(e=2e-6, g=2e-4)
+  assert abs(out[0] - ref["trace"]) <= tol["e"] * abs(ref["trace"])
+  assert abs(out[1] - ref["kinetic"]) <= tol["e"] * abs(ref["kinetic"])
+  hmax = np.abs(ref["hmat"]).max()
+  assert np.abs(hm.cpu().numpy() - ref["hmat"]).max() <= tol["e"] * 10 * hmax
+  scale = max(np.abs(ref["grad_re"]).max(), np.abs(ref["grad_im"]).max())
+  err = max(np.abs(gr.cpu().numpy() - ref["grad_re"]).max(),
+            np.abs(gi.cpu().numpy() - ref["grad_im"]).max())
+  assert err <= tol["g"] * scale, (err, scale)
+
+
+def test_spin_unrestricted_band_driver(tmp_path):
+  """calc.band_structure_all_electrons with spin_restricted False: eigenvalues
+  per spin channel, each channel's band Hamiltonian in its own potential."""
+  import jrystal_gb300 as jr
+  xyz = tmp_path / "si2.xyz"
+  a = 10.26 * 0.529177249
+  xyz.write_text("2\nLattice=\"0 {0} {0} {0} 0 {0} {0} {0} 0\" Properties=species:S:1:pos:R:3\n"
+                 "Si 0 0 0\nSi {1} {1} {1}\n".format(a / 2, a / 4))
+  out = jr.calc.band_structure_all_electrons({
+    "crystal_file_path_path": str(xyz), "grid_sizes": 16, "k_grid_sizes": [1, 1, 1],
+    "cutoff_energy": 10.0, "epoch": 40, "convergence_condition": 1e-12, "empty_bands": 2,
+    "spin": 2, "spin_restricted": False, "k_path_special_points": "GX", "num_kpoints": 3,
+    "band_structure_epoch": 60, "k_path_fine_tuning_epoch": 20,
+    "optimizer_args": {"learning_rate": 0.01, "b1": 0.9, "b2": 0.99}})
+  assert out.eigenvalues.shape[0] == 2 and out.eigenvalues.shape[-1] == 14
+  assert np.isfinite(out.eigenvalues).all()
+  assert tuple(out.effective_potential.shape) == (2, 16, 16, 16)
+  assert not torch_allclose(out.effective_potential[0], out.effective_potential[1])
+
+
+def torch_allclose(a, b):
+  import torch
+  return bool(torch.allclose(a, b))

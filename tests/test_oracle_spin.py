@@ -109,3 +109,22 @@ def test_polarised_gradient_central_differences(occ):
       em = R.energy_terms(p[0], p[1], s2, with_grad=False)["total"]
       fd = (ep - em) / (2 * h)
       assert abs(fd - g[idx]) <= 1e-6 * max(1.0, abs(g[idx])), (idx, part, fd, g[idx])
+
+
+def test_band_trace_per_spin_potential():
+  """Two spin channels in their own potentials: the trace, band Hamiltonian
+  and gradient are those of each channel alone in its potential."""
+  sysm = make_system(kind="si2", grid=(12, 12, 12), kgrid=(1, 1, 2), nb=4, nocc=2)
+  K = sysm.kpts.shape[0]
+  s2 = _spin_system(sysm, np.ones((1, K, 4)), np.ones((1, K, 4)))
+  rng = np.random.default_rng(21)
+  v = rng.normal(size=(2,) + tuple(sysm.grid))
+  wr, wi = random_params(s2, seed=22, ns=2)
+  both = R.band_trace_terms(wr, wi, v, s2)
+  one = dataclasses.replace(sysm, occupation=np.ones((1, K, 4)))
+  parts = [R.band_trace_terms(wr[s:s + 1], wi[s:s + 1], v[s], one) for s in range(2)]
+  assert abs(both["trace"] - sum(p["trace"] for p in parts)) < 1e-11 * abs(both["trace"])
+  for s in range(2):
+    np.testing.assert_allclose(both["hmat"][s], parts[s]["hmat"][0], atol=1e-12)
+    np.testing.assert_allclose(both["grad_re"][s], parts[s]["grad_re"][0], atol=1e-12)
+    np.testing.assert_allclose(both["grad_im"][s], parts[s]["grad_im"][0], atol=1e-12)
