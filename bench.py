@@ -320,21 +320,21 @@ def phase_bytes(plan, fused=False):
 
 def time_to_tolerance(nsteps=20000, ncells=16, cell_index=1):
   """Learned vs plain optimiser on the held-out strained cells of the
-  preconditioner's evaluation sequence (seed 99), judged against the
+  preconditioner's evaluation sequence (seed 99), measured against the
   converged plain energy E_ref (the plain run's energy after nsteps): wall
   time until E stays within 1e-5 Ha/atom of E_ref (two-sided: |E - E_ref|)
   and until E stays below E_ref + 1e-5 Ha/atom (one-sided, the "_below"
   keys: at least as converged as the plain run; the learned runs end below
   E_ref, so the two-sided form charges them for going lower).  Medians over
   the cells, with cells where the learned run never settles counted as 0,
-  the detail of one cell, and the same judge on the Si8 64^3 benchmark cell
+  the detail of one cell, and the same reference energy on the Si8 64^3 benchmark cell
   (8000 steps)."""
   from jrystal_gb300 import precond, precond_train
   mlp = precond.MLP.load(precond.DEFAULT_WEIGHTS)
   res = precond_train.evaluate(mlp, ncells=ncells, nsteps=nsteps, seed=99, grids=(24, 27, 32))
   row = res["cells"][cell_index]
   out = {"cell": row["cell"], "tol_ha_per_atom": 1e-5, "max_steps": nsteps,
-         "judge": "converged plain energy (the plain run's energy after max_steps)",
+         "reference_energy": "converged plain energy (the plain run's energy after max_steps)",
          "E_ref": row["E_ref"], "plain_drift_last10pct_ha_per_atom": row["plain_drift_last10pct_ha_per_atom"]}
   for mode in ("plain", "learned"):
     r = row[mode]
@@ -349,7 +349,7 @@ def time_to_tolerance(nsteps=20000, ncells=16, cell_index=1):
                                       for r in res["cells"]]
   out["heldout"]["speedups"] = [None if r["speedup_wall"] is None else round(r["speedup_wall"], 3)
                                 for r in res["cells"]]
-  # the benchmark cell itself (Si8 64^3, FP32, N(0,1) seed 1), same judge
+  # the benchmark cell itself (Si8 64^3, FP32, N(0,1) seed 1), same reference energy
   b = precond_train.transfer(mlp, nsteps=8000, names=("si8_cubic_64",))["si8_cubic_64"]
   out["benchmark_cell"] = {"cell": "si8_cubic_64", "max_steps": 8000, "E_ref": b["E_ref"],
                            "plain_drift_last10pct_ha_per_atom": b["plain_drift_last10pct_ha_per_atom"],

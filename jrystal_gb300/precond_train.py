@@ -11,7 +11,7 @@ implementation generates.
    --recipe strained: 64 strained cells (Si, C, Al; seed 2; grids from
    {24, 27, 32, 36, 48}; 2x2x2 k-grid; 8-16 bands, the lower half doubly
    occupied), 300 plain Adam steps each, ~6 records per step (~1.2e5
-   records), then ``rounds - 1`` refinement rounds whose records come from
+   records), then ``passes - 1`` refinement passes whose records come from
    trajectories run under the current network (the one-step model is
    re-expressed for the absolute scale, see collect_records).
 2. Training: Adam lr 1e-3, 2000 steps, seed 3, with the library's BF16/FP32
@@ -77,23 +77,23 @@ def generate(ncells=64, steps=300, per_step=6, seed=2, grids=(24, 27, 32, 36, 48
   return {k: torch.cat([r[k] for r in recs]) for k in recs[0]}
 
 
-def fit(rounds=3, ncells=64, steps=300, per_step=6, smax=4.0, grids=(24, 27, 32, 36, 48),
+def fit(passes=3, ncells=64, steps=300, per_step=6, smax=4.0, grids=(24, 27, 32, 36, 48),
         refine_steps=1500, log=print):
-  """Round 1 on plain trajectories of ``steps`` steps; refinement rounds on
+  """Pass 1 on plain trajectories of ``steps`` steps; refinement passes on
   trajectories of ``refine_steps`` steps run under the current network (the
-  horizon of the step feature x3 is refine_steps from round 2 on)."""
+  horizon of the step feature x3 is refine_steps from pass 2 on)."""
   mlp = precond.MLP(seed=3)
-  mlp.horizon = steps if rounds == 1 else refine_steps
+  mlp.horizon = steps if passes == 1 else refine_steps
   t0 = time.time()
   R = generate(ncells, steps, per_step, 2, grids)
-  log(f"round 1: {R['x'].shape[0]} records from plain trajectories ({time.time() - t0:.1f} s)")
+  log(f"pass 1: {R['x'].shape[0]} records from plain trajectories ({time.time() - t0:.1f} s)")
   precond.train(mlp, R, steps=2000, lr=1e-3, seed=3)
-  for r in range(2, rounds + 1):
+  for r in range(2, passes + 1):
     R2 = generate(ncells // 4, refine_steps, max(1, per_step * steps // refine_steps * 2),
                   2 + 10 * r, grids, mlp=mlp, smax=smax)
     R = {k: torch.cat([R[k], R2[k]]) for k in R}
     precond.train(mlp, R, steps=2000, lr=1e-3, seed=3 + r)
-    log(f"round {r}: {R['x'].shape[0]} records, loss {precond.evaluate_loss(mlp, R):.4f}")
+    log(f"pass {r}: {R['x'].shape[0]} records, loss {precond.evaluate_loss(mlp, R):.4f}")
   return mlp
 
 
@@ -144,7 +144,7 @@ def run_pair(wl, mlp, nsteps, smax=4.0, total=None, lr=1e-2):
   return out
 
 
-def judge_pair(res, natom, tol=1e-5):
+def score_pair(res, natom, tol=1e-5):
   """Time to tolerance of a run_pair result against the converged plain
   energy E_ref (the plain run's last energy), two ways:
     * |E - E_ref| < tol Ha/atom holding for the rest of the run (steps,
@@ -173,20 +173,20 @@ def judge_pair(res, natom, tol=1e-5):
 
 def evaluate(mlp, ncells=16, nsteps=40000, seed=99, grids=(24, 27, 32), smax=4.0, tol=1e-5,
              total=None):
-  """Learned vs plain on ``ncells`` held-out strained cells (judge_pair)."""
+  """Learned vs plain on ``ncells`` held-out strained cells (score_pair)."""
   rng = np.random.default_rng(seed)
   rows = []
   for j in range(ncells):
     wl = cells.strained_cell(rng, grids=grids)
     res = run_pair(wl, mlp, nsteps, smax, total)
     row = {"cell": wl.name}
-    row.update(judge_pair(res, wl.positions.shape[0], tol))
+    row.update(score_pair(res, wl.positions.shape[0], tol))
     rows.append(row)
   return summarise(rows, nsteps, tol)
 
 
 def summarise(rows, nsteps, tol):
-  out = {"cells": rows, "nsteps": nsteps, "tol": tol, "judge": "converged plain energy"}
+  out = {"cells": rows, "nsteps": nsteps, "tol": tol, "reference_energy": "converged plain energy"}
   for suffix in ("", "_below"):
     sp = [r["speedup_wall" + suffix] for r in rows if r["speedup_wall" + suffix] is not None]
     # cells where the learned run never settled count as no gain (0)
@@ -199,13 +199,13 @@ def summarise(rows, nsteps, tol):
 
 
 def transfer(mlp, nsteps=20000, smax=4.0, tol=1e-5, names=("si2_fcc_48", "si8_cubic_64")):
-  """The same judge on the named benchmark cells (FP32)."""
+  """The same reference energy on the named benchmark cells (FP32)."""
   from . import workloads
   out = {}
   for name in names:
     wl = workloads.WORKLOADS[name](32)
     res = run_pair(wl, mlp, nsteps, smax)
-    out[name] = judge_pair(res, wl.positions.shape[0], tol)
+    out[name] = score_pair(res, wl.positions.shape[0], tol)
   return out
 
 
@@ -214,14 +214,14 @@ def main():
   ap.add_argument("--out", default=None)
   ap.add_argument("--weights", default=None, help="evaluate these weights instead of training")
   ap.add_argument("--eval-json", default=None)
-  ap.add_argument("--rounds", type=int, default=1)
+  ap.add_argument("--passes", type=int, default=1)
   ap.add_argument("--recipe", default="benchmark", choices=["benchmark", "strained"],
                   help="records from runs of the Si8 64^3 benchmark cell, or from 64 strained "
-                       "Si/C/Al cells with refinement rounds")
+                       "Si/C/Al cells with refinement passes")
   ap.add_argument("--eval-cells", type=int, default=16)
   ap.add_argument("--eval-steps", type=int, default=40000)
   ap.add_argument("--transfer-steps", type=int, default=0,
-                  help="also judge the benchmark cells (Si2 48^3, Si8 64^3) over this many steps")
+                  help="also score the benchmark cells (Si2 48^3, Si8 64^3) over this many steps")
   ap.add_argument("--refine-steps", type=int, default=1500)
   args = ap.parse_args()
   if args.weights:
@@ -230,7 +230,7 @@ def main():
     if not args.out:
       ap.error("--out is required when training")
     mlp = (fit_benchmark_cell() if args.recipe == "benchmark"
-           else fit(rounds=args.rounds, refine_steps=args.refine_steps))
+           else fit(passes=args.passes, refine_steps=args.refine_steps))
     mlp.save(args.out)
   if args.eval_json:
     res = evaluate(mlp, ncells=args.eval_cells, nsteps=args.eval_steps)

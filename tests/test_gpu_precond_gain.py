@@ -2,7 +2,7 @@
 weights, trained on records of the Si8 64^3 benchmark cell; four held-out
 strained cells of the evaluation sequence, seed 99, 12 000 steps each).
 
-The judge is the converged plain energy E_ref: the plain run's energy at
+The reference energy is the converged plain energy E_ref: the plain run's energy at
 the end of its 12 000 steps.  Both runs start from the same parameters;
 each is charged the wall time until its energy stays below E_ref + 1e-5
 Ha/atom for the rest of the run (at least as converged as the plain
@@ -18,14 +18,14 @@ pytestmark = pytest.mark.gpu
 
 def test_learned_preconditioner_reaches_converged_plain_energy_sooner():
   from jrystal_gb300 import cells, precond
-  from jrystal_gb300.precond_train import judge_pair, run_pair
+  from jrystal_gb300.precond_train import score_pair, run_pair
   mlp = precond.MLP.load(precond.DEFAULT_WEIGHTS)
   rng = np.random.default_rng(99)
   speedups = []
   for _ in range(4):
     wl = cells.strained_cell(rng, grids=(24, 27, 32))
     nat = wl.positions.shape[0]
-    row = judge_pair(run_pair(wl, mlp, 12000, 4.0, None), nat, 1e-5)
+    row = score_pair(run_pair(wl, mlp, 12000, 4.0, None), nat, 1e-5)
     assert row["plain"]["steps_below"] is not None
     assert row["learned"]["steps_below"] is not None, row
     assert row["learned"]["end_minus_ref_ha_per_atom"] <= 1e-5
