@@ -62,3 +62,17 @@ def test_benchmark_cells(name, ng, nk):
   assert abs(occ.sum() - 2 * wl.num_occ) < 1e-12
   wr, wi = wl.init_params()
   assert wr.shape == (1, nk, ng, wl.num_band)
+
+
+def test_spin_channel_selection():
+  """spin_restricted selects one or two channels; the polarised path is LDA
+  only, so an unrestricted PBE run is refused before any device work."""
+  from jrystal_gb300 import calc
+  cfg = calc._merge({"xc": "lda_x+lda_c_vwn"})
+  assert calc._num_spin(cfg) == 1
+  cfg["spin_restricted"] = False
+  assert calc._num_spin(cfg) == 2
+  cfg["xc"] = "gga_x_pbe+gga_c_pbe"
+  with pytest.raises(NotImplementedError):
+    calc._num_spin(cfg)
+
